@@ -1,0 +1,328 @@
+#!/usr/bin/env python
+"""Benchmark of the GB300 pressure projection (one JSON line on rank 0).
+
+A step is one full projection of the 256^3 dam-break scene: cell classification
+from the level set and the solid primitives, masked divergence, MGPCG to
+relative residual 1e-6 (rel_tol 1e-12 on squared norms, abs_tol 0, at most 200
+iterations, smoother "phases", 6 levels down to 8^3) and the pressure-gradient
+velocity update.  Each step first restores the input velocity (a 200 MB
+device-to-device copy) because the projection updates it in place.
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+
+--impl reference times the CPU restatement of the same path (oracle/, the
+reference's Warp kernels cannot run here) on all host cores, on rank 0 only.
+With N > 1 (torchrun) every rank projects its own seeded scene (replicas, no
+collective on the data path): value = max elapsed over ranks / (K * N).
+"""
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "ms per 256³ pressure solve to 1e-6 rel. residual: learned+mixed vs plain MGPCG"
+UNIT = "ms"
+# canonical algorithmic bytes per cell of the level a kernel runs on
+SMOOTH_HALF_SWEEP_BYTES_PER_CELL = 6.5  # red + black iteration: R z, r, tag; W z = 13 B/cell
+
+
+def parse_args():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
+    ap.add_argument("--config", default="dam256")
+    ap.add_argument("--cpu-baseline-steps", type=int, default=2)
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-e2e", action="store_true")
+    return ap.parse_args()
+
+
+def dist_env():
+    return int(os.environ.get("RANK", 0)), int(os.environ.get("LOCAL_RANK", 0)), int(os.environ.get("WORLD_SIZE", 1))
+
+
+def load_peaks():
+    path = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(path):
+        with open(path) as f:
+            p = json.load(f)
+        return float(p["hbm_gbs"]), "measured"
+    return 6800.0, "fallback"
+
+
+def load_traffic(kernel):
+    path = os.path.join(ROOT, "profiles", "roofline_traffic.json")
+    if not os.path.exists(path):
+        return None
+    with open(path) as f:
+        return json.load(f).get(kernel)
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled every 200 ms."""
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, local_rank):
+        vis = os.environ.get("CUDA_VISIBLE_DEVICES", "")
+        ids = [v.strip() for v in vis.split(",") if v.strip()]
+        self.gpu = ids[local_rank] if local_rank < len(ids) else str(local_rank)
+        self.proc = None
+        self.path = None
+
+    def start(self):
+        fd, self.path = tempfile.mkstemp(suffix=".csv")
+        os.close(fd)
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", self.gpu, f"--query-gpu={self.FIELDS}",
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=open(self.path, "w"), stderr=subprocess.DEVNULL)
+        except (OSError, FileNotFoundError):
+            self.proc = None
+
+    def stop(self):
+        if self.proc is None:
+            return None
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+        rows = []
+        with open(self.path) as f:
+            for line in f:
+                parts = [p.strip() for p in line.split(",")]
+                if len(parts) == 9:
+                    rows.append(parts)
+        os.unlink(self.path)
+        if not rows:
+            return None
+        sm = [float(r[1]) for r in rows if r[1].replace(".", "").isdigit()]
+        mx = [float(r[2]) for r in rows if r[2].replace(".", "").isdigit()]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[q] for r in rows for q in range(4) if r[5 + q].lower().startswith("active")})
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(mx) if mx else None,
+                "reasons": reasons, "samples": len(rows)}
+
+
+def time_cpu_projection(scene, steps):
+    """The oracle's full projection on all host threads; returns ms per step."""
+    import oracle as O
+    O.project(scene, max_iters=200, rel_tol=1e-12, abs_tol=0.0)  # warm (pages, thread pool)
+    t0 = time.perf_counter()
+    for _ in range(steps):
+        res = O.project(scene, max_iters=200, rel_tol=1e-12, abs_tol=0.0)
+    dt = (time.perf_counter() - t0) * 1000.0 / steps
+    return dt, res, O.num_threads()
+
+
+# ---------------------------------------------------------------------------- reference arm
+
+def run_reference(args):
+    rank, _, world = dist_env()
+    if rank != 0:
+        return 0
+    from flub_gb300 import scenes
+    scene = scenes.CONFIGS[args.config]()
+    import oracle as O
+    for _ in range(args.warmup):
+        O.project(scene, max_iters=200, rel_tol=1e-12, abs_tol=0.0)
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        res = O.project(scene, max_iters=200, rel_tol=1e-12, abs_tol=0.0)
+    ms = (time.perf_counter() - t0) * 1000.0 / args.steps
+    cores = O.num_threads()
+    out = {
+        "impl": "reference", "metric": METRIC, "value": ms, "unit": UNIT, "n_gpus": args.gpus, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": False, "scaling": "weak", "vs_baseline": None,
+        "dtype": "f32", "data": "synthetic (seeded dam-break scene, Fourier velocity field)",
+        "config": {"workload": f"{args.config}: 256^3 dam-break projection to rel. residual 1e-6",
+                   "iterations": res["iters"], "converged": res["converged"],
+                   "implementation": "CPU restatement of the reference path (Warp unavailable), OpenMP"},
+        "cpu_baseline": {"value": ms, "unit": UNIT, "cores": cores, "kind": "port",
+                         "sample": f"{args.steps} full {args.config} projections"},
+        "e2e": {"value": ms, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(out), flush=True)
+    return 0
+
+
+# ---------------------------------------------------------------------------- our arm
+
+def run_ours(args):
+    import torch
+    import torch.distributed as dist
+
+    rank, local_rank, world = dist_env()
+    torch.cuda.set_device(local_rank)
+    if world > 1:
+        dist.init_process_group(backend="nccl", device_id=torch.device("cuda", local_rank))
+
+    from flub_gb300 import Projection, _lib, scenes
+    from flub_gb300.fields import Field, MACGrid
+
+    lib = _lib.load()
+    seed_base = {"dam256": 2, "dam512": 2, "sphere128": 1, "box64": 0}.get(args.config, 0)
+    scene = scenes.CONFIGS[args.config](seed=seed_base + rank)
+    n = scene.n_cells
+    proj = Projection(scene.shape, scene.levels)
+
+    def dev(a):
+        return torch.from_numpy(np.ascontiguousarray(a)).cuda()
+
+    phi = dev(scene.phi)
+    vel0 = [dev(a) for a in (scene.u, scene.v, scene.w)]
+    vel = MACGrid(*(Field(a.clone(), d=d + 1) for d, a in enumerate(vel0)))
+    velr = MACGrid(*(Field(dev(a), d=d + 1) for d, a in enumerate((scene.ur, scene.vr, scene.wr))))
+    solve_kw = dict(max_iters=200, eps=1e-12, abs_tol=0.0, rel_tol=1e-12, smoother="phases")
+
+    def step():
+        for a, b in zip((vel.u.f, vel.v.f, vel.w.f), vel0):
+            a.copy_(b)
+        proj.project(vel, velr, phi, scene.prims, sync=False, **solve_kw)
+
+    for _ in range(max(args.warmup, 1)):
+        step()
+    torch.cuda.synchronize()
+    info = proj.mg.info()
+    if not info["converged"]:
+        raise RuntimeError(f"warm-up solve did not converge: {info}")
+    div_after = proj.max_abs_div(vel, velr)
+
+    stream = torch.cuda.current_stream()
+    sampler = ClockSampler(local_rank)
+    if world > 1:
+        dist.barrier()
+    torch.cuda.synchronize()
+    host_l0 = lib.flub_launch_count()
+    dev_l0 = proj.mg.kernels_executed()
+    sampler.start()
+    time.sleep(0.3)
+    ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    ev0.record(stream)
+    for _ in range(args.steps):
+        step()
+    ev1.record(stream)
+    torch.cuda.synchronize()
+    clocks = sampler.stop()
+    if world > 1:
+        dist.barrier()
+    elapsed = ev0.elapsed_time(ev1)
+    launches = (lib.flub_launch_count() - host_l0) + (proj.mg.kernels_executed() - dev_l0)
+    info = proj.mg.info()
+    if world > 1:
+        t = torch.tensor([elapsed], device="cuda")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        elapsed = float(t.item())
+    ms_per_step = elapsed / args.steps
+    value = elapsed / (args.steps * world)
+
+    # ---- end to end through the public API with host buffers
+    e2e = None
+    if not args.no_e2e:
+        pin = lambda a: torch.from_numpy(np.ascontiguousarray(a)).pin_memory()
+        h_in = [pin(scene.phi)] + [pin(a) for a in (scene.u, scene.v, scene.w, scene.ur, scene.vr, scene.wr)]
+        h_out = [torch.empty_like(t).pin_memory() for t in h_in[1:4]] + [torch.empty(scene.shape).pin_memory()]
+        d_in = [phi, vel.u.f, vel.v.f, vel.w.f, velr.u.f, velr.v.f, velr.w.f]
+        d_out = [vel.u.f, vel.v.f, vel.w.f, proj.p.f]
+
+        def step_e2e():
+            for h, d in zip(h_in, d_in):
+                d.copy_(h, non_blocking=True)
+            proj.project(vel, velr, phi, scene.prims, sync=False, **solve_kw)
+            for h, d in zip(h_out, d_out):
+                h.copy_(d, non_blocking=True)
+
+        for _ in range(max(args.warmup, 1)):
+            step_e2e()
+        torch.cuda.synchronize()
+        if world > 1:
+            dist.barrier()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        for _ in range(args.steps):
+            step_e2e()
+        e1.record(stream)
+        torch.cuda.synchronize()
+        et = e0.elapsed_time(e1)
+        if world > 1:
+            t = torch.tensor([et], device="cuda")
+            dist.all_reduce(t, op=dist.ReduceOp.MAX)
+            et = float(t.item())
+        e2e = {"value": et / (args.steps * world), "unit": UNIT,
+               "h2d_bytes_per_step": int(sum(t.numel() * t.element_size() for t in h_in)),
+               "d2h_bytes_per_step": int(sum(t.numel() * t.element_size() for t in h_out))}
+
+    # ---- roofline of the dominant kernel: the level-0 red-black half-sweep
+    peak, peak_kind = load_peaks()
+    reps = 48
+    for ph in (0, 1):
+        proj.mg.smooth(0, ph)
+    torch.cuda.synchronize()
+    k0, k1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    k0.record(stream)
+    for q in range(reps):
+        proj.mg.smooth(0, q & 1)
+    k1.record(stream)
+    torch.cuda.synchronize()
+    launch_ms = k0.elapsed_time(k1) / reps
+    alg_bytes = SMOOTH_HALF_SWEEP_BYTES_PER_CELL * n
+    achieved = alg_bytes / (launch_ms * 1e-3) / 1e9
+    traffic = load_traffic("k_smooth_half")
+    roofline = {"bound": "hbm", "kernel": "k_smooth_half<false> (level-0 red-black half-sweep)",
+                "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
+                "peak_source": f"{peak_kind} hbm_gbs", "traffic": traffic,
+                "alg_bytes_per_launch": alg_bytes, "launch_ms": launch_ms}
+
+    # ---- CPU baseline: the oracle on the host cores (rank 0, N = 1 only)
+    cpu = None
+    if rank == 0 and world == 1 and not args.no_cpu_baseline and args.cpu_baseline_steps > 0:
+        cpu_ms, cpu_res, cores = time_cpu_projection(scene, args.cpu_baseline_steps)
+        cpu = {"value": cpu_ms, "unit": UNIT, "cores": cores, "kind": "port",
+               "sample": f"{args.cpu_baseline_steps} full {args.config} projections "
+                         f"({cpu_res['iters']} CG iterations each), FP32 C restatement with OpenMP"}
+
+    if rank == 0:
+        out = {
+            "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": ms_per_step, "higher_is_better": False, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f32",
+            "data": "synthetic (seeded dam-break scene and Fourier velocity field, generated on the host)",
+            "config": {"workload": f"{args.config}: {scene.shape[0]}^3 dam-break projection (classify + divergence "
+                                   f"+ MGPCG to rel. residual 1e-6 + gradient update)",
+                       "variant": "plain FP32 MGPCG (FP64 inner products)", "levels": scene.levels,
+                       "iterations": info["iterations"], "converged": bool(info["converged"]),
+                       "fluid_cells": int((scene.phi <= 0).sum()), "cells": n,
+                       "cell_iterations_per_s": n * info["iterations"] / (ms_per_step * 1e-3),
+                       "max_abs_div_after": div_after, "l2_flush": "inputs larger than L2 (~1.3 GB working set)",
+                       "parallelism": f"replicas x{world}"},
+            "roofline": roofline, "cpu_baseline": cpu, "e2e": e2e, "gpu_launches": int(launches),
+            "clocks": clocks,
+        }
+        print(json.dumps(out), flush=True)
+    if world > 1:
+        dist.destroy_process_group()
+    return 0
+
+
+def main():
+    args = parse_args()
+    if args.impl == "reference":
+        return run_reference(args)
+    return run_ours(args)
+
+
+if __name__ == "__main__":
+    sys.exit(main())

@@ -1,0 +1,25 @@
+"""flub_gb300: GB300-native (sm_103a) pressure projection for the flub fluid
+simulator -- cell classification + divergence, MGPCG Poisson solve and the
+pressure-gradient update -- behind the reference's own API.
+
+    from flub_gb300 import MGPCG, launch, divergence_tag, mask_with_tag, \\
+        subtract_gradient_tag, scale_by_3d, make_field, make_mac_grid
+
+The CUDA library (flub_gb300/_build/libflub_gb300.so, C ABI in
+include/flub_gb300.h) is built in-tree by ``flub_gb300.build.build()`` and
+loaded on first use; there is no CPU fallback.
+"""
+from .fields import (DEFAULT_SHAPE, Field, IntField, MACGrid, MACGridInt, field_like, field_shape, get_uf,
+                     make_field, make_mac_grid)
+from .kernels import (_tag_dirichlet, _tag_neumann, classify, divergence, divergence_tag, launch, mask_with_tag,
+                      phi_prims, precompute_grid_point_phi_prims, scale_by_3d, subtract_gradient,
+                      subtract_gradient_tag, tag_dirichlet, tag_neumann)
+from .mgpcg import MGPCG
+from .projection import Projection
+
+__all__ = [
+    "DEFAULT_SHAPE", "Field", "IntField", "MACGrid", "MACGridInt", "field_like", "field_shape", "get_uf",
+    "make_field", "make_mac_grid", "_tag_dirichlet", "_tag_neumann", "classify", "divergence", "divergence_tag",
+    "launch", "mask_with_tag", "phi_prims", "precompute_grid_point_phi_prims", "scale_by_3d", "subtract_gradient",
+    "subtract_gradient_tag", "tag_dirichlet", "tag_neumann", "MGPCG", "Projection",
+]

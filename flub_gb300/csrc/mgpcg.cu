@@ -1,0 +1,522 @@
+// MGPCG solver handle: level hierarchy, V-cycle schedule and the CG loop as a
+// CUDA graph (multigrid/mgpcg.py:234-490).
+//
+// The whole solve is one graph:
+//   prologue  [mean removal] rTr0/tol, z = M r, zTr, p = z,
+//             first half of iteration 0: Ap = L p, alpha, r -= alpha Ap, rTr,
+//             convergence test -> while-condition
+//   while     second half of iteration m: z = M r, beta, x += alpha p,
+//             p = z + beta p, it = m + 1;  first half of iteration m + 1
+//   epilogue  x += alpha p if the last test converged
+// which is the reference's loop (mgpcg.py:406-461) rotated so that the
+// convergence test closes the loop body.  The host reads back the state once.
+#include <cstddef>
+#include <cstdlib>
+#include <cstring>
+#include <vector>
+
+#include "mg_kernels.cuh"
+
+namespace flub {
+
+constexpr int kMaxLevels = 12;
+
+struct Level {
+    Dims D;
+    uint8_t *code;
+    float *r;
+    float *z;
+};
+
+struct LaunchCtx {
+    cudaStream_t s;
+    unsigned long long *kc;  // device kernel counter when captured into a graph, else nullptr
+    cudaGraphConditionalHandle h;
+    int set_cond;
+};
+
+}  // namespace flub
+
+struct flub_mg {
+    int nx, ny, nz, levels, precision;
+    int64_t n;
+    void *ws;
+    size_t ws_bytes;
+    bool own_ws;
+    int device;
+    flub::Level lv[flub::kMaxLevels];
+    float *x, *p, *Ap;
+    flub::MgState *st;
+    double *partials;
+    double *hist;
+    bool use_x0;
+    cudaGraphExec_t graph[3];
+    int graph_nodes[3];
+    cudaStream_t cap_stream, cap_stream2;
+    bool host_loop;
+};
+
+namespace flub {
+
+static inline size_t align256(size_t b) { return (b + 255) & ~(size_t)255; }
+
+// Device address of the kernel counter inside the (device-resident) state.
+static inline unsigned long long *kernel_counter(flub_mg *mg) {
+    return reinterpret_cast<unsigned long long *>(reinterpret_cast<char *>(mg->st) + offsetof(MgState, kernels));
+}
+
+// Workspace carve-up; with base == nullptr only the size is computed.
+static size_t carve(flub_mg *mg, char *base) {
+    size_t off = 0;
+    auto take = [&](size_t bytes) -> char * {
+        char *p = base ? base + off : nullptr;
+        off += align256(bytes);
+        return p;
+    };
+    const int64_t n = mg->n;
+    mg->st = (MgState *)take(sizeof(MgState));
+    mg->partials = (double *)take(sizeof(double) * 2 * kMaxRedBlocks);
+    mg->hist = (double *)take(sizeof(double) * kHistory);
+    mg->x = (float *)take(sizeof(float) * n);
+    mg->p = (float *)take(sizeof(float) * n);
+    mg->Ap = (float *)take(sizeof(float) * n);
+    for (int l = 0; l < mg->levels; l++) {
+        Level &L = mg->lv[l];
+        L.D = Dims{mg->nx >> l, mg->ny >> l, mg->nz >> l};
+        const int64_t nl = L.D.n();
+        L.code = (uint8_t *)take(nl);
+        L.r = (float *)take(sizeof(float) * nl);
+        L.z = (float *)take(sizeof(float) * nl);
+    }
+    return off;
+}
+
+static int validate_shape(int nx, int ny, int nz, int levels, int precision) {
+    FLUB_REQUIRE(nx > 0 && ny > 0 && nz > 0, "MGPCG shape (%d, %d, %d) must be positive", nx, ny, nz);
+    FLUB_REQUIRE(levels >= 1 && levels <= kMaxLevels, "n_mg_levels=%d outside [1, %d]", levels, kMaxLevels);
+    FLUB_REQUIRE(precision == FLUB_PRECISION_FP32 || precision == FLUB_PRECISION_MIXED, "unknown precision %d",
+                 precision);
+    const int f = 1 << (levels - 1);
+    FLUB_REQUIRE(nx % f == 0 && ny % f == 0 && nz % f == 0,
+                 "shape (%d, %d, %d) is not divisible by 2**(n_mg_levels-1) = %d", nx, ny, nz, f);
+    FLUB_REQUIRE(((nz >> (levels - 1)) % 2) == 0,
+                 "nz >> (n_mg_levels-1) = %d must be even (red-black launch over k pairs)", nz >> (levels - 1));
+    return FLUB_OK;
+}
+
+static inline unsigned red_blocks(int64_t n) { return blocks_for(n, kRedThreads, 152 * 6); }
+
+// ---------------------------------------------------------------- enqueue helpers
+
+static int smooth(const LaunchCtx &c, const Level &L, int phase, bool from_zero, const float *r, float *z) {
+    const int64_t npairs = L.D.n() / 2;
+    const unsigned b = blocks_for(npairs, 256, 1 << 20);
+    if (from_zero)
+        k_smooth_half<true><<<b, 256, 0, c.s>>>(z, r, L.code, L.D, phase, c.kc);
+    else
+        k_smooth_half<false><<<b, 256, 0, c.s>>>(z, r, L.code, L.D, phase, c.kc);
+    FLUB_CHECK_LAUNCH();
+    return FLUB_OK;
+}
+
+#define FLUB_TRY(x)            \
+    do {                       \
+        int _s = (x);          \
+        if (_s) return _s;     \
+    } while (0)
+
+// multigrid/mgpcg.py:296-349 apply_preconditioner; level 0 uses (r0, z0).
+static int enqueue_vcycle(flub_mg *mg, const LaunchCtx &c, const float *r0, float *z0) {
+    const int Lm = mg->levels;
+    auto R = [&](int l) -> const float * { return l == 0 ? r0 : mg->lv[l].r; };
+    auto Z = [&](int l) -> float * { return l == 0 ? z0 : mg->lv[l].z; };
+    for (int l = 0; l < Lm - 1; l++) {
+        const Level &L = mg->lv[l];
+        const int iters = 6 << l;
+        for (int it = 0; it < iters; it++) {
+            FLUB_TRY(smooth(c, L, 0, it == 0, R(l), Z(l)));
+            FLUB_TRY(smooth(c, L, 1, false, R(l), Z(l)));
+        }
+        const Level &C = mg->lv[l + 1];
+        k_restrict<<<blocks_for(C.D.n(), 256, 1 << 20), 256, 0, c.s>>>(R(l), Z(l), L.code, C.r, C.code, C.D, c.kc);
+        FLUB_CHECK_LAUNCH();
+    }
+    {
+        const Level &L = mg->lv[Lm - 1];
+        for (int it = 0; it < 3; it++) {
+            FLUB_TRY(smooth(c, L, 0, it == 0, R(Lm - 1), Z(Lm - 1)));
+            FLUB_TRY(smooth(c, L, 1, false, R(Lm - 1), Z(Lm - 1)));
+        }
+        for (int it = 0; it < 3; it++) {
+            FLUB_TRY(smooth(c, L, 1, false, R(Lm - 1), Z(Lm - 1)));
+            FLUB_TRY(smooth(c, L, 0, false, R(Lm - 1), Z(Lm - 1)));
+        }
+    }
+    for (int l = Lm - 2; l >= 0; l--) {
+        const Level &L = mg->lv[l];
+        k_prolong<<<blocks_for(L.D.n(), 256, 1 << 20), 256, 0, c.s>>>(Z(l), mg->lv[l + 1].z, L.D, c.kc);
+        FLUB_CHECK_LAUNCH();
+        const int iters = 6 << l;
+        for (int it = 0; it < iters; it++) {
+            FLUB_TRY(smooth(c, L, 1, false, R(l), Z(l)));
+            FLUB_TRY(smooth(c, L, 0, false, R(l), Z(l)));
+        }
+    }
+    return FLUB_OK;
+}
+
+static int enqueue_mean_removal(flub_mg *mg, const LaunchCtx &c, int guard) {
+    const unsigned b = red_blocks(mg->n);
+    k_fluid_mean<<<b, kRedThreads, 0, c.s>>>(mg->st, mg->lv[0].r, mg->lv[0].code, mg->n, mg->partials, guard, c.kc);
+    FLUB_CHECK_LAUNCH();
+    k_sub_mean<<<b, kRedThreads, 0, c.s>>>(mg->st, mg->lv[0].r, mg->lv[0].code, mg->n, guard, c.kc);
+    FLUB_CHECK_LAUNCH();
+    return FLUB_OK;
+}
+
+static int enqueue_prologue(flub_mg *mg, const LaunchCtx &c, int smoother) {
+    const unsigned b = red_blocks(mg->n);
+    const Level &L0 = mg->lv[0];
+    if (smoother == FLUB_SMOOTHER_FRACTION) FLUB_TRY(enqueue_mean_removal(mg, c, 0));
+    k_dot_rr0<<<b, kRedThreads, 0, c.s>>>(mg->st, L0.r, mg->n, mg->partials, c.kc);
+    FLUB_CHECK_LAUNCH();
+    k_residual_x0<<<blocks_for(mg->n, 256), 256, 0, c.s>>>(mg->st, L0.r, mg->x, L0.code, L0.D, c.kc);
+    FLUB_CHECK_LAUNCH();
+    if (smoother == FLUB_SMOOTHER_FRACTION) FLUB_TRY(enqueue_mean_removal(mg, c, 2));
+    FLUB_TRY(enqueue_vcycle(mg, c, L0.r, L0.z));
+    k_dot_zr_init<<<b, kRedThreads, 0, c.s>>>(mg->st, L0.z, L0.r, mg->p, mg->n, mg->partials, c.kc);
+    FLUB_CHECK_LAUNCH();
+    return FLUB_OK;
+}
+
+// Ap, alpha, r update, r.r, convergence test, loop condition.
+static int enqueue_first_half(flub_mg *mg, const LaunchCtx &c, int smoother) {
+    const unsigned b = red_blocks(mg->n);
+    const Level &L0 = mg->lv[0];
+    k_matvec_pap<<<b, kRedThreads, 0, c.s>>>(mg->st, mg->p, mg->Ap, L0.code, L0.D, mg->partials, c.kc);
+    FLUB_CHECK_LAUNCH();
+    if (smoother == FLUB_SMOOTHER_FRACTION) {
+        k_update_r<<<b, kRedThreads, 0, c.s>>>(mg->st, L0.r, mg->Ap, mg->n, c.kc);
+        FLUB_CHECK_LAUNCH();
+        FLUB_TRY(enqueue_mean_removal(mg, c, 1));
+        k_update_r_rr<false><<<b, kRedThreads, 0, c.s>>>(mg->st, L0.r, mg->Ap, mg->n, mg->partials, mg->hist, c.h,
+                                                         c.set_cond, c.kc);
+    } else {
+        k_update_r_rr<true><<<b, kRedThreads, 0, c.s>>>(mg->st, L0.r, mg->Ap, mg->n, mg->partials, mg->hist, c.h,
+                                                        c.set_cond, c.kc);
+    }
+    FLUB_CHECK_LAUNCH();
+    return FLUB_OK;
+}
+
+// z = M r, beta, x += alpha p, p = z + beta p, it += 1.
+static int enqueue_second_half(flub_mg *mg, const LaunchCtx &c) {
+    const unsigned b = red_blocks(mg->n);
+    const Level &L0 = mg->lv[0];
+    FLUB_TRY(enqueue_vcycle(mg, c, L0.r, L0.z));
+    k_dot_zr_beta<<<b, kRedThreads, 0, c.s>>>(mg->st, L0.z, L0.r, mg->n, mg->partials, c.kc);
+    FLUB_CHECK_LAUNCH();
+    k_update_xp<<<blocks_for(mg->n, 256), 256, 0, c.s>>>(mg->st, mg->x, mg->p, L0.z, mg->n, c.kc);
+    FLUB_CHECK_LAUNCH();
+    return FLUB_OK;
+}
+
+static int enqueue_epilogue(flub_mg *mg, const LaunchCtx &c) {
+    k_solve_end<<<blocks_for(mg->n, 256), 256, 0, c.s>>>(mg->st, mg->x, mg->p, mg->n, c.kc);
+    FLUB_CHECK_LAUNCH();
+    return FLUB_OK;
+}
+
+// Builds prologue -> while(body) -> epilogue with stream capture.
+static int build_graph(flub_mg *mg, int smoother, cudaGraphExec_t *out) {
+    cudaStream_t s = mg->cap_stream, s2 = mg->cap_stream2;
+    cudaGraph_t g = nullptr;
+    int rc = FLUB_OK;
+    const int64_t launches_before = flub_launch_count();
+    FLUB_CHECK_CUDA(cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal));
+    auto abort_capture = [&](int code) {
+        cudaGraph_t tmp = nullptr;
+        cudaStreamEndCapture(s, &tmp);
+        if (tmp) cudaGraphDestroy(tmp);
+        cudaGetLastError();
+        return code;
+    };
+    cudaStreamCaptureStatus cs;
+    cudaGraph_t capg = nullptr;
+    if (cudaStreamGetCaptureInfo(s, &cs, nullptr, &capg, nullptr, nullptr, nullptr) != cudaSuccess)
+        return abort_capture((set_last_error("cudaStreamGetCaptureInfo failed"), FLUB_ERR_CUDA));
+    cudaGraphConditionalHandle h;
+    cudaError_t e = cudaGraphConditionalHandleCreate(&h, capg, 0, 0);
+    if (e != cudaSuccess)
+        return abort_capture((set_last_error("cudaGraphConditionalHandleCreate: %s", cudaGetErrorString(e)),
+                              FLUB_ERR_CUDA));
+    LaunchCtx c{s, kernel_counter(mg), h, 1};
+    if ((rc = enqueue_prologue(mg, c, smoother)) || (rc = enqueue_first_half(mg, c, smoother)))
+        return abort_capture(rc);
+    const cudaGraphNode_t *deps = nullptr;
+    size_t ndeps = 0;
+    if (cudaStreamGetCaptureInfo(s, &cs, nullptr, &capg, &deps, nullptr, &ndeps) != cudaSuccess)
+        return abort_capture((set_last_error("cudaStreamGetCaptureInfo failed"), FLUB_ERR_CUDA));
+    cudaGraphNodeParams cp = {cudaGraphNodeTypeConditional};
+    cp.conditional.handle = h;
+    cp.conditional.type = cudaGraphCondTypeWhile;
+    cp.conditional.size = 1;
+    cudaGraphNode_t cnode;
+    e = cudaGraphAddNode(&cnode, capg, deps, nullptr, ndeps, &cp);
+    if (e != cudaSuccess)
+        return abort_capture((set_last_error("cudaGraphAddNode(while): %s", cudaGetErrorString(e)), FLUB_ERR_CUDA));
+    e = cudaStreamUpdateCaptureDependencies(s, &cnode, nullptr, 1, cudaStreamSetCaptureDependencies);
+    if (e != cudaSuccess)
+        return abort_capture((set_last_error("cudaStreamUpdateCaptureDependencies: %s", cudaGetErrorString(e)),
+                              FLUB_ERR_CUDA));
+    cudaGraph_t body = cp.conditional.phGraph_out[0];
+    e = cudaStreamBeginCaptureToGraph(s2, body, nullptr, nullptr, 0, cudaStreamCaptureModeThreadLocal);
+    if (e != cudaSuccess)
+        return abort_capture((set_last_error("cudaStreamBeginCaptureToGraph: %s", cudaGetErrorString(e)),
+                              FLUB_ERR_CUDA));
+    LaunchCtx c2{s2, kernel_counter(mg), h, 1};
+    rc = enqueue_second_half(mg, c2);
+    if (!rc) rc = enqueue_first_half(mg, c2, smoother);
+    cudaGraph_t body_out = nullptr;
+    e = cudaStreamEndCapture(s2, &body_out);
+    if (rc || e != cudaSuccess) {
+        if (!rc) set_last_error("cudaStreamEndCapture(body): %s", cudaGetErrorString(e));
+        return abort_capture(rc ? rc : FLUB_ERR_CUDA);
+    }
+    if ((rc = enqueue_epilogue(mg, c))) return abort_capture(rc);
+    FLUB_CHECK_CUDA(cudaStreamEndCapture(s, &g));
+    e = cudaGraphInstantiate(out, g, 0);
+    cudaGraphDestroy(g);
+    // kernels captured into the graph are counted on the device when they run
+    count_launches(launches_before - flub_launch_count());
+    if (e != cudaSuccess) {
+        set_last_error("cudaGraphInstantiate: %s", cudaGetErrorString(e));
+        return FLUB_ERR_CUDA;
+    }
+    return FLUB_OK;
+}
+
+static int read_info(flub_mg *mg, cudaStream_t s, flub_solve_info *info) {
+    MgState h;
+    FLUB_CHECK_CUDA(cudaMemcpyAsync(&h, mg->st, sizeof(MgState), cudaMemcpyDeviceToHost, s));
+    FLUB_CHECK_CUDA(cudaStreamSynchronize(s));
+    info->iterations = h.it;
+    info->converged = h.converged;
+    info->status = h.status;
+    info->reserved = 0;
+    info->rtr0 = h.rtr0;
+    info->rtr = h.rtr;
+    info->tol = h.tol;
+    return FLUB_OK;
+}
+
+}  // namespace flub
+
+using namespace flub;
+
+extern "C" {
+
+size_t flub_mg_workspace_bytes(int nx, int ny, int nz, int levels, int precision) {
+    if (validate_shape(nx, ny, nz, levels, precision)) return 0;
+    flub_mg tmp;
+    memset(&tmp, 0, sizeof(tmp));
+    tmp.nx = nx; tmp.ny = ny; tmp.nz = nz; tmp.levels = levels; tmp.precision = precision;
+    tmp.n = (int64_t)nx * ny * nz;
+    return carve(&tmp, nullptr);
+}
+
+int flub_mg_create(int nx, int ny, int nz, int levels, int precision, void *workspace, size_t workspace_bytes,
+                   flub_mg **out) {
+    FLUB_REQUIRE(out != nullptr, "flub_mg_create: out is NULL");
+    *out = nullptr;
+    FLUB_TRY(validate_shape(nx, ny, nz, levels, precision));
+    FLUB_REQUIRE(precision == FLUB_PRECISION_FP32, "precision %d not available in this build", precision);
+    flub_mg *mg = new flub_mg;
+    memset(mg, 0, sizeof(*mg));
+    mg->nx = nx; mg->ny = ny; mg->nz = nz; mg->levels = levels; mg->precision = precision;
+    mg->n = (int64_t)nx * ny * nz;
+    const size_t need = carve(mg, nullptr);
+    if (workspace) {
+        if (workspace_bytes < need || ((uintptr_t)workspace & 255)) {
+            delete mg;
+            set_last_error("workspace of %zu bytes at %p: need %zu bytes, 256-byte aligned", workspace_bytes,
+                           workspace, need);
+            return FLUB_ERR_INVALID_ARGUMENT;
+        }
+        mg->ws = workspace;
+        mg->own_ws = false;
+    } else {
+        cudaError_t e = cudaMalloc(&mg->ws, need);
+        if (e != cudaSuccess) {
+            delete mg;
+            set_last_error("cudaMalloc(%zu): %s", need, cudaGetErrorString(e));
+            cudaGetLastError();
+            return FLUB_ERR_OUT_OF_MEMORY;
+        }
+        mg->own_ws = true;
+    }
+    mg->ws_bytes = need;
+    carve(mg, (char *)mg->ws);
+    cudaGetDevice(&mg->device);
+    if (cudaStreamCreateWithFlags(&mg->cap_stream, cudaStreamNonBlocking) != cudaSuccess ||
+        cudaStreamCreateWithFlags(&mg->cap_stream2, cudaStreamNonBlocking) != cudaSuccess) {
+        flub_mg_destroy(mg);
+        set_last_error("cudaStreamCreate failed");
+        return FLUB_ERR_CUDA;
+    }
+    const char *hl = getenv("FLUB_SOLVE_HOST_LOOP");
+    mg->host_loop = hl && hl[0] == '1';
+    // zero the state and all vectors once so that every buffer is defined
+    if (cudaMemset(mg->ws, 0, need) != cudaSuccess || cudaDeviceSynchronize() != cudaSuccess) {
+        flub_mg_destroy(mg);
+        set_last_error("workspace initialisation failed");
+        return FLUB_ERR_CUDA;
+    }
+    *out = mg;
+    return FLUB_OK;
+}
+
+int flub_mg_destroy(flub_mg *mg) {
+    if (!mg) return FLUB_OK;
+    for (int s = 0; s < 3; s++)
+        if (mg->graph[s]) cudaGraphExecDestroy(mg->graph[s]);
+    if (mg->cap_stream) cudaStreamDestroy(mg->cap_stream);
+    if (mg->cap_stream2) cudaStreamDestroy(mg->cap_stream2);
+    if (mg->own_ws && mg->ws) cudaFree(mg->ws);
+    delete mg;
+    return FLUB_OK;
+}
+
+int flub_mg_set_tags(flub_mg *mg, const int32_t *tag, void *stream) {
+    FLUB_REQUIRE(mg && tag, "flub_mg_set_tags: NULL argument");
+    cudaStream_t s = as_stream(stream);
+    k_encode_tags<<<blocks_for(mg->n, 256), 256, 0, s>>>(tag, mg->lv[0].code, mg->n);
+    FLUB_CHECK_LAUNCH();
+    for (int l = 0; l + 1 < mg->levels; l++) {
+        const Level &C = mg->lv[l + 1];
+        k_restrict_codes<<<blocks_for(C.D.n(), 256), 256, 0, s>>>(mg->lv[l].code, C.code, C.D);
+        FLUB_CHECK_LAUNCH();
+    }
+    return FLUB_OK;
+}
+
+int flub_mg_init(flub_mg *mg, const float *rhs, float k, void *stream) {
+    FLUB_REQUIRE(mg && rhs, "flub_mg_init: NULL argument");
+    k_init<<<blocks_for(mg->n, 256), 256, 0, as_stream(stream)>>>(mg->lv[0].r, rhs, k, mg->x, mg->p, mg->n);
+    FLUB_CHECK_LAUNCH();
+    mg->use_x0 = false;
+    return FLUB_OK;
+}
+
+int flub_mg_mask_interior(flub_mg *mg, void *stream) {
+    FLUB_REQUIRE(mg, "flub_mg_mask_interior: NULL handle");
+    k_mask_interior<<<blocks_for(mg->n, 256), 256, 0, as_stream(stream)>>>(mg->lv[0].r, mg->lv[0].code, mg->n);
+    FLUB_CHECK_LAUNCH();
+    return FLUB_OK;
+}
+
+int flub_mg_set_x0(flub_mg *mg, const float *x0, void *stream) {
+    FLUB_REQUIRE(mg && x0, "flub_mg_set_x0: NULL argument");
+    FLUB_CHECK_CUDA(cudaMemcpyAsync(mg->x, x0, sizeof(float) * mg->n, cudaMemcpyDeviceToDevice, as_stream(stream)));
+    mg->use_x0 = true;
+    return FLUB_OK;
+}
+
+int flub_mg_solve(flub_mg *mg, int max_iters, double eps, double abs_tol, double rel_tol, int smoother,
+                  void *stream, flub_solve_info *info) {
+    FLUB_REQUIRE(mg, "flub_mg_solve: NULL handle");
+    if (smoother != FLUB_SMOOTHER_PHASES && smoother != FLUB_SMOOTHER_FRACTION) {
+        set_last_error("smoother %d not supported (only \"phases\" and \"fraction\"; the untagged \"default\" "
+                       "smoother is not part of this library)", smoother);
+        return FLUB_ERR_UNSUPPORTED;
+    }
+    if (max_iters < 0) max_iters = 100000;
+    cudaStream_t s = as_stream(stream);
+    k_solve_begin<<<1, 1, 0, s>>>(mg->st, max_iters, eps, abs_tol, rel_tol, mg->use_x0 ? 1 : 0);
+    FLUB_CHECK_LAUNCH();
+    mg->use_x0 = false;
+    if (mg->host_loop) {
+        LaunchCtx c{s, nullptr, 0, 0};
+        FLUB_TRY(enqueue_prologue(mg, c, smoother));
+        FLUB_TRY(enqueue_first_half(mg, c, smoother));
+        for (int guard = 0; guard <= max_iters; guard++) {
+            MgState h;
+            FLUB_CHECK_CUDA(cudaMemcpyAsync(&h, mg->st, sizeof(MgState), cudaMemcpyDeviceToHost, s));
+            FLUB_CHECK_CUDA(cudaStreamSynchronize(s));
+            if (!h.cond) break;
+            FLUB_TRY(enqueue_second_half(mg, c));
+            FLUB_TRY(enqueue_first_half(mg, c, smoother));
+        }
+        FLUB_TRY(enqueue_epilogue(mg, c));
+    } else {
+        const int gi = smoother;
+        if (!mg->graph[gi]) FLUB_TRY(build_graph(mg, smoother, &mg->graph[gi]));
+        FLUB_CHECK_CUDA(cudaGraphLaunch(mg->graph[gi], s));
+    }
+    if (info) return read_info(mg, s, info);
+    return FLUB_OK;
+}
+
+int flub_mg_get_info(flub_mg *mg, void *stream, flub_solve_info *info) {
+    FLUB_REQUIRE(mg && info, "flub_mg_get_info: NULL argument");
+    return read_info(mg, as_stream(stream), info);
+}
+
+int flub_mg_residual_history(flub_mg *mg, void *stream, double *out, int max_n, int *n_out) {
+    FLUB_REQUIRE(mg && out && n_out && max_n >= 0, "flub_mg_residual_history: bad argument");
+    flub_solve_info info;
+    FLUB_TRY(read_info(mg, as_stream(stream), &info));
+    int n = info.converged ? info.iterations + 1 : info.iterations;
+    if (n > kHistory) n = kHistory;
+    if (n > max_n) n = max_n;
+    if (n > 0) {
+        FLUB_CHECK_CUDA(cudaMemcpy(out, mg->hist, sizeof(double) * n, cudaMemcpyDeviceToHost));
+    }
+    *n_out = n;
+    return FLUB_OK;
+}
+
+float *flub_mg_x(flub_mg *mg) { return mg ? mg->x : nullptr; }
+float *flub_mg_r(flub_mg *mg) { return mg ? mg->lv[0].r : nullptr; }
+
+int flub_mg_get_x(flub_mg *mg, float *out, float scale, void *stream) {
+    FLUB_REQUIRE(mg && out, "flub_mg_get_x: NULL argument");
+    k_scale_copy<<<blocks_for(mg->n, 256), 256, 0, as_stream(stream)>>>(out, mg->x, scale, mg->n);
+    FLUB_CHECK_LAUNCH();
+    return FLUB_OK;
+}
+
+int flub_mg_apply_preconditioner(flub_mg *mg, const float *r, float *z, void *stream) {
+    FLUB_REQUIRE(mg && r && z, "flub_mg_apply_preconditioner: NULL argument");
+    LaunchCtx c{as_stream(stream), nullptr, 0, 0};
+    return enqueue_vcycle(mg, c, r, z);
+}
+
+int flub_mg_matvec(flub_mg *mg, const float *p, float *Ap, void *stream) {
+    FLUB_REQUIRE(mg && p && Ap, "flub_mg_matvec: NULL argument");
+    const Level &L0 = mg->lv[0];
+    k_matvec<<<blocks_for(mg->n, 256), 256, 0, as_stream(stream)>>>(p, Ap, L0.code, L0.D);
+    FLUB_CHECK_LAUNCH();
+    return FLUB_OK;
+}
+
+int flub_mg_smooth(flub_mg *mg, int level, int phase, void *stream) {
+    FLUB_REQUIRE(mg, "flub_mg_smooth: NULL handle");
+    FLUB_REQUIRE(level >= 0 && level < mg->levels, "flub_mg_smooth: level %d outside [0, %d)", level, mg->levels);
+    FLUB_REQUIRE(phase == 0 || phase == 1, "flub_mg_smooth: phase must be 0 or 1");
+    LaunchCtx c{as_stream(stream), nullptr, 0, 0};
+    const Level &L = mg->lv[level];
+    return smooth(c, L, phase, false, L.r, L.z);
+}
+
+int flub_mg_kernels_executed(flub_mg *mg, void *stream, int64_t *out) {
+    FLUB_REQUIRE(mg && out, "flub_mg_kernels_executed: NULL argument");
+    unsigned long long v = 0;
+    cudaStream_t s = as_stream(stream);
+    FLUB_CHECK_CUDA(cudaMemcpyAsync(&v, kernel_counter(mg), sizeof(v), cudaMemcpyDeviceToHost, s));
+    FLUB_CHECK_CUDA(cudaStreamSynchronize(s));
+    *out = (int64_t)v;
+    return FLUB_OK;
+}
+
+}  // extern "C"

@@ -1,0 +1,236 @@
+"""The projection path's kernels under the reference's names, with a
+``launch(kernel, dim, inputs)`` that mirrors ``wp.launch`` so that the call
+sites in example_fluid.py / water_3d.py only change their import line:
+
+    wp.launch(divergence_tag, dim=shape, inputs=[vel, div, vel_rigid, tag])
+    wp.launch(mask_with_tag, dim=shape, inputs=[div, tag])
+    wp.launch(scale_by_3d, dim=shape, inputs=[div, -1.0 / h])
+    wp.launch(subtract_gradient_tag, dim=shapeu, inputs=[vel, vel_rigid, p, tag, 1])
+    wp.launch(_tag_dirichlet, dim=shape, inputs=[tag, phi])
+    wp.launch(_tag_neumann, dim=shape, inputs=[tag, phi_rigid])
+    wp.launch(precompute_grid_point_phi_prims, dim=shape,
+              inputs=[phi, owner, x, q, geometry, stagger])
+
+Every kernel runs on the GPU through the C ABI (include/flub_gb300.h) on the
+current torch stream.  Each function also exists as a plain call
+(``divergence``, ``classify``, ...).
+"""
+import ctypes
+
+import numpy as np
+import torch
+
+from . import _lib
+from .fields import Field, IntField, MACGrid, field_shape
+
+
+def _stream():
+    return ctypes.c_void_p(torch.cuda.current_stream().cuda_stream)
+
+
+def _ptr(t, dtype, shape=None, name="array"):
+    if not isinstance(t, torch.Tensor):
+        raise TypeError(f"{name}: expected a torch tensor, got {type(t).__name__}")
+    if not t.is_cuda:
+        raise ValueError(f"{name}: tensor must be on a CUDA device")
+    if t.dtype != dtype:
+        raise TypeError(f"{name}: dtype {t.dtype}, expected {dtype}")
+    if not t.is_contiguous():
+        raise ValueError(f"{name}: tensor must be contiguous (C-order)")
+    if shape is not None and tuple(t.shape) != tuple(shape):
+        raise ValueError(f"{name}: shape {tuple(t.shape)}, expected {tuple(shape)}")
+    return ctypes.c_void_p(t.data_ptr())
+
+
+def _f(x):
+    return x.f if isinstance(x, (Field, IntField)) else x
+
+
+# ------------------------------------------------------------------ primitives
+
+def prims_array(prims):
+    """Host array of flub_prim from a numpy structured array (fields geometry,
+    x, q, radius) or a sequence of dicts."""
+    n = len(prims)
+    arr = (_lib.Prim * max(n, 1))()
+    for o in range(n):
+        p = prims[o]
+        get = (lambda k: p[k]) if not isinstance(p, dict) else (lambda k: p.get(k))
+        arr[o].geometry = int(get("geometry"))
+        arr[o].x[:] = [float(v) for v in np.asarray(get("x"), np.float32).reshape(3)]
+        q = get("q")
+        arr[o].q[:] = [float(v) for v in (np.asarray(q, np.float32).reshape(4) if q is not None
+                                          else np.array([0, 0, 0, 1], np.float32))]
+        r = np.asarray(get("radius"), np.float32).reshape(-1)
+        if r.size == 1:
+            r = np.repeat(r, 3)
+        arr[o].radius[:] = [float(v) for v in r]
+    return arr, n
+
+
+def prims_from_arrays(x, q, geometry):
+    """Primitive list from the reference's rigid arrays (rigid_coupling.py:
+    x_pair.cur, theta_pair.cur, rigid_geometry with fields geometry, radius)."""
+    x = np.asarray(x.cpu() if isinstance(x, torch.Tensor) else x, np.float32).reshape(-1, 3)
+    q = np.asarray(q.cpu() if isinstance(q, torch.Tensor) else q, np.float32).reshape(-1, 4)
+    out = []
+    for o, g in enumerate(geometry):
+        gg = g if isinstance(g, dict) else {"geometry": g["geometry"], "radius": g["radius"]}
+        out.append(dict(geometry=int(gg["geometry"]), x=x[o], q=q[o], radius=gg["radius"]))
+    return out
+
+
+# ------------------------------------------------------------------ plain calls
+
+def tag_dirichlet(tag, phi):
+    """geometry.py:335-344: tag = 0 where phi > 0, else 1."""
+    tag, phi = _f(tag), _f(phi)
+    _lib.call("flub_tag_dirichlet", _ptr(phi, torch.float32, name="phi"),
+              _ptr(tag, torch.int32, phi.shape, "tag"), phi.numel(), _stream())
+
+
+def tag_neumann(tag, phi_rigid):
+    """geometry.py:390-397: tag = 2 where phi_rigid < 0."""
+    tag, phi_rigid = _f(tag), _f(phi_rigid)
+    _lib.call("flub_tag_neumann", _ptr(phi_rigid, torch.float32, name="phi_rigid"),
+              _ptr(tag, torch.int32, phi_rigid.shape, "tag"), phi_rigid.numel(), _stream())
+
+
+def phi_prims(phi, prims, h, h0, stagger=(0.5, 0.5, 0.5)):
+    """geometry.py:225-239: phi = min primitive SDF below h0 (else 2.0)."""
+    phi = _f(phi)
+    arr, n = prims_array(prims)
+    nx, ny, nz = phi.shape
+    _lib.call("flub_phi_prims", _ptr(phi, torch.float32, name="phi"), nx, ny, nz, float(h), float(h0),
+              float(stagger[0]), float(stagger[1]), float(stagger[2]), ctypes.cast(arr, ctypes.c_void_p), n,
+              _stream())
+
+
+def classify(phi, prims, h, h0, tag=None, phi_rigid=None):
+    """Fused _tag_dirichlet + primitive phi_rigid + _tag_neumann.  Returns tag."""
+    phi = _f(phi)
+    if tag is None:
+        tag = torch.empty(phi.shape, dtype=torch.int32, device=phi.device)
+    tag = _f(tag)
+    arr, n = prims_array(prims)
+    nx, ny, nz = phi.shape
+    pr = _ptr(_f(phi_rigid), torch.float32, phi.shape, "phi_rigid") if phi_rigid is not None else None
+    _lib.call("flub_classify", _ptr(phi, torch.float32, name="phi"), ctypes.cast(arr, ctypes.c_void_p), n, nx, ny,
+              nz, float(h), float(h0), _ptr(tag, torch.int32, phi.shape, "tag"), pr, _stream())
+    return tag
+
+
+def _faces(vel, shape):
+    return [_ptr(_f(a), torch.float32, field_shape(shape, d + 1), n)
+            for d, (a, n) in enumerate(zip((vel.u, vel.v, vel.w), ("u", "v", "w")))]
+
+
+def divergence(vel, vel_rigid, tag, div=None, scale=None):
+    """divergence.py:43-99 divergence_tag; with ``scale`` also mask_with_tag and
+    scale_by_3d fused (example_fluid.py:90-93).  Returns div."""
+    tag = _f(tag)
+    shape = tuple(tag.shape)
+    if div is None:
+        div = torch.empty(shape, dtype=torch.float32, device=tag.device)
+    div = _f(div)
+    args = _faces(vel, shape) + _faces(vel_rigid, shape) + [_ptr(tag, torch.int32, name="tag"),
+                                                            _ptr(div, torch.float32, shape, "div")]
+    if scale is None:
+        _lib.call("flub_divergence_tag", *args, *shape, _stream())
+    else:
+        _lib.call("flub_divergence_masked", *args, float(scale), *shape, _stream())
+    return div
+
+
+def _mask_with_tag(div, tag):
+    """divergence.py:173-180: div = 0 where tag != 1."""
+    div, tag = _f(div), _f(tag)
+    _lib.call("flub_mask_with_tag", _ptr(div, torch.float32, name="div"), _ptr(tag, torch.int32, div.shape, "tag"),
+              div.numel(), _stream())
+
+
+def _scale_by_3d(q, s):
+    """utils/util.py:162-165: q *= s."""
+    q = _f(q)
+    _lib.call("flub_scale", _ptr(q, torch.float32, name="q"), float(s), q.numel(), _stream())
+
+
+def subtract_gradient(vel, vel_rigid, p, tag, d=None, p_scale=1.0):
+    """subtract_gradient.py:37-68.  d in {1, 2, 3} updates one axis as the
+    reference does; d=None updates all three in one fused pass."""
+    p, tag = _f(p), _f(tag)
+    shape = tuple(tag.shape)
+    pp = _ptr(p, torch.float32, shape, "p")
+    tp = _ptr(tag, torch.int32, shape, "tag")
+    if d is None:
+        _lib.call("flub_subtract_gradient", *_faces(vel, shape), *_faces(vel_rigid, shape), pp, float(p_scale), tp,
+                  *shape, _stream())
+    else:
+        if float(p_scale) != 1.0:
+            raise ValueError("p_scale applies to the fused update (d=None) only")
+        uf = _f((vel.u, vel.v, vel.w)[d - 1])
+        urf = _f((vel_rigid.u, vel_rigid.v, vel_rigid.w)[d - 1])
+        fs = field_shape(shape, d)
+        _lib.call("flub_subtract_gradient_tag", _ptr(uf, torch.float32, fs, "uf"), _ptr(urf, torch.float32, fs, "urf"),
+                  pp, tp, *shape, int(d), _stream())
+
+
+# ------------------------------------------------------------------ wp.launch mirror
+
+class Kernel:
+    """A kernel object for ``launch``; calling it directly runs it on its inputs."""
+
+    def __init__(self, name, fn, expect_dim):
+        self.name = name
+        self._fn = fn
+        self._expect_dim = expect_dim
+
+    def __call__(self, *inputs):
+        return self._fn(*inputs)
+
+    def launch(self, dim, inputs):
+        expected = self._expect_dim(inputs)
+        if expected is not None and tuple(dim) != tuple(expected):
+            raise ValueError(f"{self.name}: launch dim {tuple(dim)} does not match the input shape {tuple(expected)}")
+        self._fn(*inputs)
+
+    def __repr__(self):
+        return f"<flub_gb300 kernel {self.name}>"
+
+
+def _dim_of(i):
+    return lambda inputs: tuple(_f(inputs[i]).shape)
+
+
+def _sg_dim(inputs):
+    vel, d = inputs[0], int(inputs[4])
+    return tuple(_f((vel.u, vel.v, vel.w)[d - 1]).shape)
+
+
+def _phi_prims_launch(phi, owner, x, q, geometry, stagger, h=None, h0=None):
+    phi = _f(phi)
+    hh = h if h is not None else 1.0 / phi.shape[0]
+    phi_prims(phi, prims_from_arrays(x, q, geometry), hh, h0 if h0 is not None else hh, stagger)
+
+
+divergence_tag = Kernel("divergence_tag", lambda vels, div, vel_rigid, tag: divergence(vels, vel_rigid, tag, div),
+                        _dim_of(1))
+mask_with_tag = Kernel("mask_with_tag", _mask_with_tag, _dim_of(0))
+scale_by_3d = Kernel("scale_by_3d", _scale_by_3d, _dim_of(0))
+subtract_gradient_tag = Kernel("subtract_gradient_tag",
+                               lambda vel, vel_rigid, pf, tag, d: subtract_gradient(vel, vel_rigid, pf, tag, int(d)),
+                               _sg_dim)
+_tag_dirichlet = Kernel("_tag_dirichlet", tag_dirichlet, _dim_of(1))
+_tag_neumann = Kernel("_tag_neumann", tag_neumann, _dim_of(1))
+precompute_grid_point_phi_prims = Kernel("precompute_grid_point_phi_prims", _phi_prims_launch, _dim_of(0))
+
+
+def launch(kernel, dim, inputs, device=None, stream=None):
+    """wp.launch(kernel, dim=..., inputs=[...]) for the kernels of this module."""
+    if not isinstance(kernel, Kernel):
+        raise TypeError(f"{kernel!r} is not a flub_gb300 kernel")
+    if stream is not None:
+        with torch.cuda.stream(stream):
+            kernel.launch(dim, inputs)
+    else:
+        kernel.launch(dim, inputs)

@@ -1,0 +1,218 @@
+/*
+ * flub_gb300 -- C ABI of the GB300 (sm_103a) pressure projection.
+ *
+ * Drop-in replacement for the three stages of flub's projection path:
+ * cell classification + divergence right-hand side, the MGPCG Poisson solve,
+ * and the pressure-gradient velocity update.  Every entry point takes plain
+ * device pointers (C-order [i][j][k] arrays, k fastest, FP32 fields, int32
+ * tags with the reference's convention 0 air / 1 fluid / 2 solid), sizes and a
+ * cudaStream_t passed as void*, and returns an int status (FLUB_OK == 0).
+ * No entry point synchronises the stream unless its comment says so.
+ *
+ * Each declaration cites the reference code it replaces (paths inside the
+ * flub repository, file:line).  In the reference these are Warp kernels
+ * launched with wp.launch(kernel, dim, inputs=[...]) or methods of
+ * multigrid/mgpcg.py:MGPCG; the Python module flub_gb300 exposes those same
+ * names on top of this ABI.
+ */
+#ifndef FLUB_GB300_H
+#define FLUB_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ---------------------------------------------------------------- status */
+#define FLUB_OK 0
+#define FLUB_ERR_INVALID_ARGUMENT 1 /* bad size, null pointer, unsupported shape */
+#define FLUB_ERR_CUDA 2             /* a CUDA runtime call failed (see flub_last_error) */
+#define FLUB_ERR_UNSUPPORTED 3      /* option not implemented (e.g. smoother "default") */
+#define FLUB_ERR_OUT_OF_MEMORY 4
+#define FLUB_ERR_BREAKDOWN 5        /* CG breakdown: non-finite alpha/beta or residual */
+#define FLUB_ERR_TIMEOUT 6          /* a bounded device-side wait gave up */
+
+/* Human-readable name of a status code. */
+const char *flub_status_string(int status);
+/* Detail of the last error raised on the calling host thread ("" if none). */
+const char *flub_last_error(void);
+/* ABI version (major * 10000 + minor * 100 + patch). */
+int flub_version(void);
+
+/* ---------------------------------------------------------------- classification */
+
+/* Solid primitive, the fields of geometry.py:6-12 GeometryType3D that the
+ * primitive SDF reads, with the body's position x and rotation q
+ * (rigid_coupling.py x_pair.cur / theta_pair.cur).  geometry: 0 none, 1 box,
+ * 2 sphere, 3 box, 4 "x" (two crossed boxes), 5 mesh (SDF 2.0: the mesh pass
+ * is not part of this library). q is (x, y, z, w). */
+typedef struct flub_prim {
+    int32_t geometry;
+    float x[3];
+    float q[4];
+    float radius[3];
+} flub_prim;
+
+#define FLUB_MAX_PRIMS 64
+
+/* geometry.py:335-344 _tag_dirichlet: tag = (phi > 0) ? 0 : 1 over n cells. */
+int flub_tag_dirichlet(const float *phi, int32_t *tag, int64_t n, void *stream);
+
+/* geometry.py:225-239 precompute_grid_point_phi_prims (+ sdf_argmin_prims
+ * :148-169, compute_sdf_atom_prims :82-113, _sdf_cube :17-32): phi at
+ * ((i, j, k) + stagger) * h = min SDF over the primitives that is below h0,
+ * else 2.0.  prims is a HOST array of nprims <= FLUB_MAX_PRIMS entries. */
+int flub_phi_prims(float *phi, int nx, int ny, int nz, float h, float h0, float sx, float sy, float sz,
+                   const flub_prim *prims, int nprims, void *stream);
+
+/* geometry.py:390-397 _tag_neumann: tag = 2 where phi_rigid < 0. */
+int flub_tag_neumann(const float *phi_rigid, int32_t *tag, int64_t n, void *stream);
+
+/* The three above fused in one pass (the classification in
+ * example_fluid.py:96-114 Dh() with water_3d.py:55-56): tag from the water
+ * level set phi, then solid where the primitives' SDF at cell centres is < 0.
+ * phi_rigid may be NULL; when given it receives the cell-centre solid SDF. */
+int flub_classify(const float *phi, const flub_prim *prims, int nprims, int nx, int ny, int nz, float h,
+                  float h0, int32_t *tag, float *phi_rigid, void *stream);
+
+/* ---------------------------------------------------------------- divergence */
+
+/* divergence.py:43-99 divergence_tag: div = (vr - vl) + (vt - vb) + (vn - vf)
+ * per cell; domain-boundary faces count as 0, a face whose outer neighbour is
+ * solid takes the rigid velocity.  u: (nx+1, ny, nz), v: (nx, ny+1, nz),
+ * w: (nx, ny, nz+1); ur/vr/wr the rigid face velocities, same shapes. */
+int flub_divergence_tag(const float *u, const float *v, const float *w, const float *ur, const float *vr,
+                        const float *wr, const int32_t *tag, float *div, int nx, int ny, int nz, void *stream);
+
+/* divergence.py:173-180 mask_with_tag: div = 0 where tag != 1. */
+int flub_mask_with_tag(float *div, const int32_t *tag, int64_t n, void *stream);
+
+/* utils/util.py:162-165 scale_by_3d (and multigrid/mgpcg.py:9-12): q *= s. */
+int flub_scale(float *q, float s, int64_t n, void *stream);
+
+/* divergence_tag + mask_with_tag + scale_by_3d fused (the sequence of
+ * example_fluid.py:84-93): div = (tag == 1) ? divergence * scale : 0. */
+int flub_divergence_masked(const float *u, const float *v, const float *w, const float *ur, const float *vr,
+                           const float *wr, const int32_t *tag, float *div, float scale, int nx, int ny, int nz,
+                           void *stream);
+
+/* ---------------------------------------------------------------- gradient */
+
+/* subtract_gradient.py:37-68 subtract_gradient_tag for axis d (1 = u, 2 = v,
+ * 3 = w) on the face array uf: solid on either side -> rigid velocity, else
+ * fluid on either side -> uf -= p_hi - p_lo, else (and on domain-boundary
+ * faces) 0. */
+int flub_subtract_gradient_tag(float *uf, const float *urf, const float *p, const int32_t *tag, int nx, int ny,
+                               int nz, int d, void *stream);
+
+/* All three axes in one pass, with the pressure read as p * p_scale (the
+ * scale_by_3d(p, 1/h0) of example_fluid.py:134 folded in). */
+int flub_subtract_gradient(float *u, float *v, float *w, const float *ur, const float *vr, const float *wr,
+                           const float *p, float p_scale, const int32_t *tag, int nx, int ny, int nz,
+                           void *stream);
+
+/* ---------------------------------------------------------------- MGPCG */
+
+/* multigrid/mgpcg.py:234-490 class MGPCG.  One handle = one level hierarchy
+ * (shape // 2**l for l < levels) plus the CG vectors; not thread-safe; all
+ * calls on a handle must use the same device.  Solves run entirely on the GPU
+ * as one CUDA graph (a while-loop conditional node around one CG iteration);
+ * the host reads back only the final status. */
+typedef struct flub_mg flub_mg;
+
+#define FLUB_SMOOTHER_PHASES 1   /* tagged red-black smoother, no mean removal (water_3d.py:66) */
+#define FLUB_SMOOTHER_FRACTION 2 /* tagged smoother + zero_centered mean removal (example_fluid.py:43-49) */
+
+#define FLUB_PRECISION_FP32 0    /* every vector FP32, inner products FP64 */
+#define FLUB_PRECISION_MIXED 1   /* V-cycle levels stored in 16-bit floats, flexible CG */
+
+typedef struct flub_solve_info {
+    int iterations; /* as printed by the reference ("finished with N iterations") */
+    int converged;  /* 1 if rTr < max(abs_tol, rel_tol * rTr0) was reached */
+    int status;     /* FLUB_OK or FLUB_ERR_BREAKDOWN */
+    int reserved;
+    double rtr0;    /* initial squared residual norm (x0 = 0 residual) */
+    double rtr;     /* final squared residual norm */
+    double tol;     /* the squared-norm tolerance used */
+} flub_solve_info;
+
+/* Bytes of device workspace a handle of this shape needs. */
+size_t flub_mg_workspace_bytes(int nx, int ny, int nz, int levels, int precision);
+
+/* multigrid/mgpcg.py:235-268 MGPCG.__init__(dim=3, shape, n_mg_levels, real).
+ * Every dimension must be divisible by 2**(levels-1) and nz >> (levels-1)
+ * must be even.  workspace: caller-owned device memory of
+ * flub_mg_workspace_bytes(...) bytes (256-byte aligned), or NULL to let the
+ * handle cudaMalloc its own. */
+int flub_mg_create(int nx, int ny, int nz, int levels, int precision, void *workspace, size_t workspace_bytes,
+                   flub_mg **out);
+int flub_mg_destroy(flub_mg *mg);
+
+/* multigrid/mgpcg.py:360-370 set_tags: copy the int32 tags, build the coarse
+ * levels (restrict_tag :162-174) and the stencil diagonals. */
+int flub_mg_set_tags(flub_mg *mg, const int32_t *tag, void *stream);
+
+/* multigrid/mgpcg.py:276-284 init: x = p = 0, r0 = k * rhs. */
+int flub_mg_init(flub_mg *mg, const float *rhs, float k, void *stream);
+
+/* multigrid/mgpcg.py:464-465, :492-499 mask_interior: r0 = 0 where tag != 1. */
+int flub_mg_mask_interior(flub_mg *mg, void *stream);
+
+/* Optional initial guess (no reference counterpart: the reference always
+ * starts from x = 0, mgpcg.py:282).  Call after init/mask_interior; the next
+ * solve starts from x0 with r = r0 - L x0 and keeps its tolerance relative to
+ * the x0 = 0 residual, so a guess can only change the iteration count. */
+int flub_mg_set_x0(flub_mg *mg, const float *x0, void *stream);
+
+/* multigrid/mgpcg.py:378-462 solve(max_iters, eps, abs_tol, rel_tol, verbose,
+ * smoother).  max_iters = -1 means "no limit" (capped at 100000).  If info is
+ * non-NULL the call synchronises the stream and fills it; with info == NULL
+ * the solve is only enqueued (read the result later with flub_mg_get_info). */
+int flub_mg_solve(flub_mg *mg, int max_iters, double eps, double abs_tol, double rel_tol, int smoother,
+                  void *stream, flub_solve_info *info);
+
+/* Synchronise the stream and read the outcome of the last solve. */
+int flub_mg_get_info(flub_mg *mg, void *stream, flub_solve_info *info);
+
+/* Squared residual norm after each iteration of the last solve (the
+ * reference's verbose print, mgpcg.py:430-431).  Synchronises; returns the
+ * number of entries written (<= max_n) in *n_out. */
+int flub_mg_residual_history(flub_mg *mg, void *stream, double *out, int max_n, int *n_out);
+
+/* Device pointers of the solution x (MGPCG.x) and of the level-0 residual r. */
+float *flub_mg_x(flub_mg *mg);
+float *flub_mg_r(flub_mg *mg);
+
+/* x * scale into out (the wp.copy + scale_by_3d of water_3d.py:67-68). */
+int flub_mg_get_x(flub_mg *mg, float *out, float scale, void *stream);
+
+/* multigrid/mgpcg.py:296-349 apply_preconditioner: z = M r (one V-cycle).
+ * Uses the handle's level hierarchy; r and z are N-cell device arrays. */
+int flub_mg_apply_preconditioner(flub_mg *mg, const float *r, float *z, void *stream);
+
+/* multigrid/mgpcg.py:36-39 compute_Ap_mcadams: Ap = L p with the level-0 tags. */
+int flub_mg_matvec(flub_mg *mg, const float *p, float *Ap, void *stream);
+
+/* multigrid/mgpcg.py:72-86 _smooth_mcadams: one red-black half-sweep (phase 0
+ * updates (i+j+k)-odd cells, phase 1 even ones) on level `level` of the
+ * handle's hierarchy, in place on that level's z with its r (level 0: the CG
+ * vectors z and r).  The same kernel the V-cycle launches. */
+int flub_mg_smooth(flub_mg *mg, int level, int phase, void *stream);
+
+/* Solver kernels executed on the device inside solve graphs by this handle
+ * since it was created (each kernel node counts once per execution).
+ * Synchronises the stream. */
+int flub_mg_kernels_executed(flub_mg *mg, void *stream, int64_t *out);
+
+/* Kernels this library launched directly from the host in this process since
+ * the counter was last reset (kernels inside solve graphs are not included:
+ * see flub_mg_kernels_executed). */
+int64_t flub_launch_count(void);
+void flub_reset_launch_count(void);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* FLUB_GB300_H */

@@ -1,0 +1,240 @@
+/*
+ * flub_oracle -- CPU restatement of flub's pressure projection.
+ *
+ * TEST INFRASTRUCTURE ONLY: used by tests/ as the parity checker, by
+ * __graft_entry__.smoke() as the checker, and by bench.py as the timed CPU
+ * baseline.  Never linked into or called by the product library.
+ *
+ * Parity status: the reference (pure Python + NVIDIA Warp) cannot be run on
+ * these machines (warp is not installed and has no offline wheel), and the
+ * reference ships no tests, fixtures or golden vectors for this path.  This
+ * restatement is therefore "parity unpinned" against the reference's own
+ * outputs; it is pinned instead against hand-derived known-answer vectors and
+ * against an independent NumPy restatement (oracle/np_oracle.py) in tests/.
+ *
+ * Build: oracle/build.py (gcc -O3 -fopenmp -ffp-contract=off -shared).
+ */
+#include <math.h>
+#include <stdint.h>
+#include <stdlib.h>
+#include <string.h>
+
+/* ---------------- precision-generic solver pieces ---------------- */
+#define REAL float
+#define FN(name) name##_f32
+#include "oracle_impl.h"
+static inline float axpy_fma_f32(float a, float x, float y) { return fmaf(a, x, y); }
+#undef REAL
+#undef FN
+
+#define REAL double
+#define FN(name) name##_f64
+#include "oracle_impl.h"
+static inline double axpy_fma_f64(double a, double x, double y) { return fma(a, x, y); }
+#undef REAL
+#undef FN
+
+/* ---------------- geometry (FP32, as the reference computes it) ---------------- */
+
+/* Primitive description, same layout as flub_prim in include/flub_gb300.h. */
+typedef struct {
+    int32_t geometry; /* 0 none, 1 box, 2 sphere, 3 box (rect), 4 "x", 5 mesh */
+    float x[3];       /* centre */
+    float q[4];       /* rotation quaternion (x, y, z, w) */
+    float radius[3];  /* box half extents; sphere radius in radius[0] */
+} oracle_prim;
+
+/* Rotation of v by the conjugate of the unit quaternion q:
+ * v (2w^2 - 1) - 2w (q_v x v) + 2 (q_v . v) q_v, evaluated left to right. */
+static void quat_rotate_inv(const float q[4], const float v[3], float out[3]) {
+    float w = q[3];
+    float c = 2.0f * w * w - 1.0f;
+    float d = 2.0f * ((q[0] * v[0] + q[1] * v[1]) + q[2] * v[2]);
+    float cx = q[1] * v[2] - q[2] * v[1];
+    float cy = q[2] * v[0] - q[0] * v[2];
+    float cz = q[0] * v[1] - q[1] * v[0];
+    float w2 = w * 2.0f;
+    out[0] = (v[0] * c - cx * w2) + q[0] * d;
+    out[1] = (v[1] * c - cy * w2) + q[1] * d;
+    out[2] = (v[2] * c - cz * w2) + q[2] * d;
+}
+
+/* geometry.py:17-32 _sdf_cube. */
+static float sdf_cube(const float p_in[3], const float radius[3], const float q[4]) {
+    float p[3], m[3];
+    quat_rotate_inv(q, p_in, p);
+    for (int a = 0; a < 3; a++) m[a] = fmaxf(p[a], -p[a]) - radius[a];
+    float mx = fmaxf(fmaxf(m[0], m[1]), m[2]);
+    if (mx < 0.0f) return mx; /* -(min(-m)) */
+    for (int a = 0; a < 3; a++) m[a] = fmaxf(m[a], 0.0f);
+    return sqrtf((m[0] * m[0] + m[1] * m[1]) + m[2] * m[2]);
+}
+
+static void quat_mul(const float a[4], const float b[4], float out[4]) {
+    /* Hamilton product, (x, y, z, w) storage */
+    out[0] = ((a[3] * b[0] + b[3] * a[0]) + a[1] * b[2]) - a[2] * b[1];
+    out[1] = ((a[3] * b[1] + b[3] * a[1]) + a[2] * b[0]) - a[0] * b[2];
+    out[2] = ((a[3] * b[2] + b[3] * a[2]) + a[0] * b[1]) - a[1] * b[0];
+    out[3] = a[3] * b[3] - ((a[0] * b[0] + a[1] * b[1]) + a[2] * b[2]);
+}
+
+/* geometry.py:82-113 compute_sdf_atom_prims. */
+static float sdf_atom_prims(float u, float v, float w, const oracle_prim *g) {
+    float p[3] = {u - g->x[0], v - g->x[1], w - g->x[2]};
+    switch (g->geometry) {
+    case 1:
+    case 3:
+        return sdf_cube(p, g->radius, g->q);
+    case 2:
+        return sqrtf((p[0] * p[0] + p[1] * p[1]) + p[2] * p[2]) - g->radius[0];
+    case 4: {
+        const float h = 0.70710678118654752f; /* cos(pi/4) = sin(pi/4) */
+        float zq[4] = {0.0f, 0.0f, h, h}, zi[4] = {0.0f, 0.0f, -h, h}, t[4], q2[4];
+        quat_mul(zq, g->q, t);
+        quat_mul(t, zi, q2);
+        return fminf(sdf_cube(p, g->radius, g->q), sdf_cube(p, g->radius, q2));
+    }
+    case 5:
+        return 2.0f;
+    default:
+        return 1.0f;
+    }
+}
+
+/* geometry.py:225-239 precompute_grid_point_phi_prims + :148-169 sdf_argmin_prims. */
+void oracle_phi_prims(float *phi, int nx, int ny, int nz, float h, float h0, const float stagger[3],
+                      const oracle_prim *prims, int nprims) {
+#pragma omp parallel for schedule(static)
+    for (int i = 0; i < nx; i++)
+        for (int j = 0; j < ny; j++)
+            for (int k = 0; k < nz; k++) {
+                float u = (float)i * h, v = (float)j * h, w = (float)k * h;
+                u = u + stagger[0] * h;
+                v = v + stagger[1] * h;
+                w = w + stagger[2] * h;
+                float interior = 2.0f;
+                for (int o = 0; o < nprims; o++) {
+                    float s = sdf_atom_prims(u, v, w, &prims[o]);
+                    if (s < fminf(h0, interior)) interior = s;
+                }
+                phi[IX(i, j, k)] = interior;
+            }
+}
+
+/* geometry.py:335-344 _tag_dirichlet. */
+void oracle_tag_dirichlet(const float *phi, int32_t *tag, int64_t n) {
+    for (int64_t c = 0; c < n; c++) tag[c] = phi[c] > 0.0f ? 0 : 1;
+}
+
+/* geometry.py:390-397 _tag_neumann. */
+void oracle_tag_neumann(const float *phi_rigid, int32_t *tag, int64_t n) {
+    for (int64_t c = 0; c < n; c++)
+        if (phi_rigid[c] < 0.0f) tag[c] = 2;
+}
+
+/* divergence.py:43-99 divergence_tag.  Boundary faces are 0 and a face whose
+ * outer neighbour is solid takes the rigid velocity.  Per-axis extents are
+ * used (the reference uses nx for all three axes, which only agrees on cubic
+ * grids).  Sum order: vr - vl + vt - vb + vn - vf, left to right. */
+void oracle_divergence(const float *u, const float *v, const float *w, const float *ur, const float *vr_,
+                       const float *wr, const int32_t *tag, float *div, int nx, int ny, int nz) {
+#pragma omp parallel for schedule(static)
+    for (int i = 0; i < nx; i++)
+        for (int j = 0; j < ny; j++)
+            for (int k = 0; k < nz; k++) {
+                /* u: (nx+1, ny, nz), v: (nx, ny+1, nz), w: (nx, ny, nz+1) */
+                int64_t uL = ((int64_t)i * ny + j) * nz + k, uR = ((int64_t)(i + 1) * ny + j) * nz + k;
+                int64_t vB = ((int64_t)i * (ny + 1) + j) * nz + k, vT = ((int64_t)i * (ny + 1) + j + 1) * nz + k;
+                int64_t wF = ((int64_t)i * ny + j) * (nz + 1) + k, wN = wF + 1;
+                float fl = u[uL], fr = u[uR], fb = v[vB], ft = v[vT], ff = w[wF], fn = w[wN];
+                if (i == 0) fl = 0.0f; else if (tag[IX(i - 1, j, k)] == 2) fl = ur[uL];
+                if (i == nx - 1) fr = 0.0f; else if (tag[IX(i + 1, j, k)] == 2) fr = ur[uR];
+                if (j == 0) fb = 0.0f; else if (tag[IX(i, j - 1, k)] == 2) fb = vr_[vB];
+                if (j == ny - 1) ft = 0.0f; else if (tag[IX(i, j + 1, k)] == 2) ft = vr_[vT];
+                if (k == 0) ff = 0.0f; else if (tag[IX(i, j, k - 1)] == 2) ff = wr[wF];
+                if (k == nz - 1) fn = 0.0f; else if (tag[IX(i, j, k + 1)] == 2) fn = wr[wN];
+                div[IX(i, j, k)] = ((((fr - fl) + ft) - fb) + fn) - ff;
+            }
+}
+
+/* divergence.py:173-180 mask_with_tag. */
+void oracle_mask_with_tag(float *div, const int32_t *tag, int64_t n) {
+    for (int64_t c = 0; c < n; c++)
+        if (tag[c] != 1) div[c] = 0.0f;
+}
+
+/* utils/util.py:162-165 scale_by_3d. */
+void oracle_scale(float *q, float s, int64_t n) {
+    for (int64_t c = 0; c < n; c++) q[c] = q[c] * s;
+}
+
+/* subtract_gradient.py:37-68 subtract_gradient_tag for axis d = 1, 2, 3 on the
+ * face array uf of shape (nx+[d==1], ny+[d==2], nz+[d==3]). */
+void oracle_subtract_gradient(float *uf, const float *urf, const float *p, const int32_t *tag, int nx, int ny,
+                              int nz, int d) {
+    int fx = nx + (d == 1), fy = ny + (d == 2), fz = nz + (d == 3);
+    int nd = d == 1 ? nx : (d == 2 ? ny : nz);
+#pragma omp parallel for schedule(static)
+    for (int i = 0; i < fx; i++)
+        for (int j = 0; j < fy; j++)
+            for (int k = 0; k < fz; k++) {
+                int64_t f = ((int64_t)i * fy + j) * fz + k;
+                int ii = d == 1 ? i : (d == 2 ? j : k);
+                if (0 < ii && ii < nd) {
+                    int il = i - (d == 1), jl = j - (d == 2), kl = k - (d == 3);
+                    float pl = p[IX(il, jl, kl)], pr = p[IX(i, j, k)];
+                    int tl = tag[IX(il, jl, kl)], tr = tag[IX(i, j, k)];
+                    if (tl == 2 || tr == 2) uf[f] = urf[f];
+                    else if (tl == 1 || tr == 1) uf[f] = uf[f] - (pr - pl);
+                    else uf[f] = 0.0f;
+                } else {
+                    uf[f] = 0.0f;
+                }
+            }
+}
+
+/* multigrid/mgpcg.py:360-370 set_tags: coarse tag levels (restrict_tag). */
+void oracle_tag_levels(int32_t **tagl, int levels, int nx, int ny, int nz) {
+    for (int l = 0; l + 1 < levels; l++)
+        oracle_restrict_tag_f32(tagl[l], tagl[l + 1], (nx >> l) / 2, (ny >> l) / 2, (nz >> l) / 2);
+}
+
+/* Level-hierarchy helpers so that Python can drive the V-cycle directly. */
+void oracle_vcycle_levels_f32(float *r0, float *z0, int32_t **tagl, int levels, int nx, int ny, int nz) {
+    float **rl = (float **)malloc(sizeof(float *) * (size_t)levels);
+    float **zl = (float **)malloc(sizeof(float *) * (size_t)levels);
+    rl[0] = r0;
+    zl[0] = z0;
+    for (int l = 1; l < levels; l++) {
+        int64_t nl = (int64_t)(nx >> l) * (ny >> l) * (nz >> l);
+        rl[l] = (float *)calloc((size_t)nl, sizeof(float));
+        zl[l] = (float *)calloc((size_t)nl, sizeof(float));
+    }
+    oracle_vcycle_f32(rl, zl, tagl, levels, nx, ny, nz);
+    for (int l = 1; l < levels; l++) { free(rl[l]); free(zl[l]); }
+    free(rl); free(zl);
+}
+
+void oracle_vcycle_levels_f64(double *r0, double *z0, int32_t **tagl, int levels, int nx, int ny, int nz) {
+    double **rl = (double **)malloc(sizeof(double *) * (size_t)levels);
+    double **zl = (double **)malloc(sizeof(double *) * (size_t)levels);
+    rl[0] = r0;
+    zl[0] = z0;
+    for (int l = 1; l < levels; l++) {
+        int64_t nl = (int64_t)(nx >> l) * (ny >> l) * (nz >> l);
+        rl[l] = (double *)calloc((size_t)nl, sizeof(double));
+        zl[l] = (double *)calloc((size_t)nl, sizeof(double));
+    }
+    oracle_vcycle_f64(rl, zl, tagl, levels, nx, ny, nz);
+    for (int l = 1; l < levels; l++) { free(rl[l]); free(zl[l]); }
+    free(rl); free(zl);
+}
+
+int oracle_num_threads(void) {
+#ifdef _OPENMP
+    extern int omp_get_max_threads(void);
+    return omp_get_max_threads();
+#else
+    return 1;
+#endif
+}

@@ -1,0 +1,384 @@
+"""GPU parity: every kernel of the path, called through the C ABI, against the
+CPU oracle on the same inputs.
+
+Bit-exact (np.array_equal) for integer work (tags) and for the FP32 kernels whose
+operation order the oracle mirrors (classification SDF, divergence, gradient,
+matvec, one V-cycle).  Solves are compared within tolerance: the FP64 inner
+products are summed in a different order on the GPU, so alpha/beta can differ
+in the last bit; the iteration count must agree within 1 and the pressure
+must be within relative L2 1e-5 of the FP64 oracle's solve (same algorithm,
+same tolerance)."""
+import os
+
+import numpy as np
+import pytest
+import torch
+
+import oracle as O
+from flub_gb300 import MGPCG, Projection, launch, scenes
+from flub_gb300 import kernels as K
+from flub_gb300._lib import FlubError
+from flub_gb300.fields import Field, IntField, MACGrid
+from tests.golden.make_golden import CASES, load
+
+pytestmark = pytest.mark.gpu
+
+PRESSURE_RTOL = 1e-5  # relative L2 of the pressure vs the FP64 oracle
+
+
+def dev(a):
+    return torch.from_numpy(np.ascontiguousarray(a)).cuda()
+
+
+def host(t):
+    torch.cuda.synchronize()
+    return t.detach().cpu().numpy()
+
+
+def mac(u, v, w):
+    return MACGrid(Field(dev(u), d=1), Field(dev(v), d=2), Field(dev(w), d=3))
+
+
+SCENES = {
+    "box32": lambda: scenes.box(32, seed=21, levels=3),
+    "sphere32": lambda: scenes.sphere(32, seed=22, levels=3),
+    "dam32": lambda: scenes.dam(32, seed=23, levels=3),
+    "dam64": lambda: scenes.dam(64, seed=24, levels=4),
+    "rand32": lambda: scenes.random_scene(32, 25, levels=3),
+    "rand32b": lambda: scenes.random_scene(32, 26, levels=4),
+}
+
+
+@pytest.fixture(scope="module", params=sorted(SCENES))
+def scene(request):
+    return SCENES[request.param]()
+
+
+# ---------------------------------------------------------------- classification
+
+def test_classify_bit_exact(scene):
+    tag_o, phr_o = O.classify(scene.phi, scene.prims, scene.h, scene.h0)
+    phr = torch.empty(scene.shape, dtype=torch.float32, device="cuda")
+    tag = K.classify(dev(scene.phi), scene.prims, scene.h, scene.h0, phi_rigid=phr)
+    assert np.array_equal(host(tag), tag_o)
+    assert np.array_equal(host(phr), phr_o)
+
+
+def test_classify_unfused_kernels_bit_exact(scene):
+    tag_o, phr_o = O.classify(scene.phi, scene.prims, scene.h, scene.h0)
+    tag = IntField(torch.empty(scene.shape, dtype=torch.int32, device="cuda"))
+    phi = Field(dev(scene.phi))
+    phr = torch.full(scene.shape, 1.0, device="cuda")
+    launch(K._tag_dirichlet, scene.shape, [tag, phi])
+    prims = scenes.make_prims([]) if len(scene.prims) == 0 else scene.prims
+    launch(K.precompute_grid_point_phi_prims, scene.shape,
+           [phr, None, prims["x"], prims["q"], [dict(geometry=g, radius=r) for g, r in
+                                               zip(prims["geometry"], prims["radius"])], (0.5, 0.5, 0.5)])
+    launch(K._tag_neumann, scene.shape, [tag, Field(phr)])
+    assert np.array_equal(host(tag.f), tag_o)
+    assert np.array_equal(host(phr), phr_o)
+
+
+# ---------------------------------------------------------------- divergence / gradient
+
+def test_divergence_bit_exact(scene):
+    tag_o, _ = O.classify(scene.phi, scene.prims, scene.h, scene.h0)
+    div_o = O.divergence(scene.u, scene.v, scene.w, scene.ur, scene.vr, scene.wr, tag_o)
+    vel, velr = mac(scene.u, scene.v, scene.w), mac(scene.ur, scene.vr, scene.wr)
+    div = Field(torch.empty(scene.shape, device="cuda"))
+    launch(K.divergence_tag, scene.shape, [vel, div, velr, IntField(dev(tag_o))])
+    assert np.array_equal(host(div.f), div_o)
+    # mask + scale (example_fluid.py:90-93), unfused and fused
+    launch(K.mask_with_tag, scene.shape, [div, IntField(dev(tag_o))])
+    launch(K.scale_by_3d, scene.shape, [div, -1.0 / scene.h])
+    O.mask_with_tag(div_o, tag_o)
+    O.scale(div_o, np.float32(-1.0 / scene.h))
+    assert np.array_equal(host(div.f), div_o)
+    fused = K.divergence(vel, velr, dev(tag_o), scale=-1.0 / scene.h)
+    assert np.array_equal(host(fused), div_o)
+
+
+def test_subtract_gradient_bit_exact(scene):
+    tag_o, _ = O.classify(scene.phi, scene.prims, scene.h, scene.h0)
+    rng = np.random.default_rng(5)
+    p = rng.standard_normal(scene.shape).astype(np.float32)
+    outs = [np.array(a, copy=True) for a in (scene.u, scene.v, scene.w)]
+    for d, (a, ar) in enumerate(zip(outs, (scene.ur, scene.vr, scene.wr))):
+        O.subtract_gradient(a, ar, p, tag_o, d + 1)
+    vel, velr = mac(scene.u, scene.v, scene.w), mac(scene.ur, scene.vr, scene.wr)
+    for d in (1, 2, 3):
+        shp = list(scene.shape)
+        shp[d - 1] += 1
+        launch(K.subtract_gradient_tag, tuple(shp), [vel, velr, Field(dev(p)), IntField(dev(tag_o)), d])
+    for a, o in zip((vel.u.f, vel.v.f, vel.w.f), outs):
+        assert np.array_equal(host(a), o)
+    # fused three-axis form with the 1/h0 read scale
+    ps = (p * np.float32(scene.h0)).astype(np.float32)
+    vel2 = mac(scene.u, scene.v, scene.w)
+    K.subtract_gradient(vel2, velr, dev(ps), dev(tag_o), p_scale=1.0 / scene.h0)
+    pg = ps.copy()
+    O.scale(pg, np.float32(1.0 / scene.h0))
+    outs2 = [np.array(a, copy=True) for a in (scene.u, scene.v, scene.w)]
+    for d, (a, ar) in enumerate(zip(outs2, (scene.ur, scene.vr, scene.wr))):
+        O.subtract_gradient(a, ar, pg, tag_o, d + 1)
+    for a, o in zip((vel2.u.f, vel2.v.f, vel2.w.f), outs2):
+        assert np.array_equal(host(a), o)
+
+
+# ---------------------------------------------------------------- multigrid
+
+def _setup(scene):
+    tag_o, _ = O.classify(scene.phi, scene.prims, scene.h, scene.h0)
+    div = O.divergence(scene.u, scene.v, scene.w, scene.ur, scene.vr, scene.wr, tag_o)
+    r0 = np.where(tag_o == 1, div, 0).astype(np.float32)
+    mg = MGPCG(3, scene.shape, scene.levels, float)
+    mg.set_tags(dev(tag_o))
+    mg.init(dev(r0), 1.0)
+    mg.mask_interior()
+    return tag_o, r0, mg
+
+
+def test_matvec_bit_exact(scene):
+    tag_o, r0, mg = _setup(scene)
+    p = np.random.default_rng(7).standard_normal(scene.shape).astype(np.float32)
+    assert np.array_equal(host(mg.matvec(dev(p))), O.matvec(p, tag_o))
+
+
+def test_vcycle_bit_exact(scene):
+    tag_o, r0, mg = _setup(scene)
+    z = mg.apply_preconditioner(dev(r0))
+    z_o = O.vcycle(r0, O.tag_levels(tag_o, scene.levels), np.float32)
+    assert np.array_equal(host(z), z_o)
+
+
+def test_solve_matches_oracle(scene):
+    tag_o, r0, mg = _setup(scene)
+    info = mg.solve(200, 1e-12, 0.0, 1e-12, smoother="phases")
+    tags = O.tag_levels(tag_o, scene.levels)
+    ref32 = O.pcg(r0, tags, max_iters=200, abs_tol=0.0, rel_tol=1e-12)
+    ref64 = O.pcg(r0, tags, max_iters=200, abs_tol=0.0, rel_tol=1e-12, dtype=np.float64)
+    assert info["converged"] and ref64["converged"]
+    assert abs(info["iterations"] - ref32["iters"]) <= 1
+    assert abs(info["iterations"] - ref64["iters"]) <= 1
+    x = host(mg.x)
+    err = np.linalg.norm(x - ref64["x"]) / np.linalg.norm(ref64["x"])
+    assert err <= PRESSURE_RTOL, err
+    assert info["rtr"] < info["tol"] == pytest.approx(1e-12 * ref64["rtr0"], rel=1e-9)
+
+
+def test_projection_matches_oracle(scene):
+    proj = Projection(scene.shape, scene.levels)
+    vel, velr = mac(scene.u, scene.v, scene.w), mac(scene.ur, scene.vr, scene.wr)
+    info = proj.project(vel, velr, dev(scene.phi), scene.prims)
+    ref = O.project(scene, dtype=np.float64)
+    assert np.array_equal(host(proj.tag.f), ref["tag"])
+    assert info["converged"] and abs(info["iterations"] - ref["iters"]) <= 1
+    for a, k in zip((vel.u.f, vel.v.f, vel.w.f), "uvw"):
+        o = ref[k]
+        assert np.linalg.norm(host(a) - o) <= 1e-5 * np.linalg.norm(o), k
+    p = host(proj.p.f)
+    assert np.linalg.norm(p - ref["p"]) <= PRESSURE_RTOL * np.linalg.norm(ref["p"])
+    # post-projection divergence (example_fluid.py:146-147) falls by orders of magnitude
+    before = np.abs(ref["div"]).max() * scene.h
+    after = proj.max_abs_div(vel, velr)
+    assert after < 1e-4 * max(before, 1e-30)
+
+
+# ---------------------------------------------------------------- golden fixtures
+
+@pytest.mark.parametrize("name", sorted(CASES))
+def test_golden_fixture(name):
+    d = load(name)
+    shape = d["phi"].shape
+    h = float(d["h"])
+    proj = Projection(shape, int(d["levels"]), h=h)
+    vel, velr = mac(d["u"], d["v"], d["w"]), mac(d["ur"], d["vr"], d["wr"])
+    info = proj.project(vel, velr, dev(d["phi"]), d["prims"])
+    assert np.array_equal(host(proj.tag.f), d["tag"])
+    assert np.array_equal(host(proj.div.f), d["div"])
+    assert abs(info["iterations"] - int(d["iters"])) <= 1
+    x = host(proj.mg.x)
+    assert np.linalg.norm(x - d["x64"]) <= PRESSURE_RTOL * np.linalg.norm(d["x64"])
+    z = proj.mg.apply_preconditioner(dev(d["r0"]))
+    assert np.array_equal(host(z), d["vcycle_r0"])
+
+
+# ---------------------------------------------------------------- edge cases and options
+
+def test_fraction_smoother_matches_oracle():
+    s = scenes.box(32, seed=30, levels=3)
+    tag_o, _ = O.classify(s.phi, s.prims, s.h, s.h0)
+    tag_o[tag_o == 0] = 1  # all fluid, all-Neumann walls: the singular problem "fraction" handles
+    div = O.divergence(s.u, s.v, s.w, s.ur, s.vr, s.wr, tag_o)
+    mg = MGPCG(3, s.shape, 3)
+    mg.set_tags(dev(tag_o))
+    mg.init(dev(div), 1.0)
+    mg.mask_interior()
+    info = mg.solve(200, 1e-12, 0.0, 1e-12, smoother="fraction")
+    ref = O.pcg(div, O.tag_levels(tag_o, 3), max_iters=200, abs_tol=0.0, rel_tol=1e-12, smoother="fraction",
+                dtype=np.float64)
+    assert abs(info["iterations"] - ref["iters"]) <= 1
+    x = host(mg.x)
+    x = x - x.mean()
+    xr = ref["x"] - ref["x"].mean()
+    assert np.linalg.norm(x - xr) <= 1e-4 * np.linalg.norm(xr)
+
+
+def test_warm_start_reduces_iterations():
+    s = scenes.dam(32, seed=31, levels=3)
+    tag_o, r0, mg = _setup(s)
+    cold = mg.solve(200, 1e-12, 0.0, 1e-12, smoother="phases")
+    xstar = mg.x.clone()
+    mg.init(dev(r0), 1.0)
+    mg.mask_interior()
+    warm = mg.solve(200, 1e-12, 0.0, 1e-12, smoother="phases", x0=xstar)
+    assert warm["converged"] and warm["iterations"] <= 1 < cold["iterations"]
+    assert warm["rtr0"] == pytest.approx(cold["rtr0"])  # tolerance stays relative to the x0 = 0 residual
+    mg.init(dev(r0), 1.0)
+    mg.mask_interior()
+    half = mg.solve(200, 1e-12, 0.0, 1e-12, smoother="phases", x0=0.9 * xstar)
+    assert half["iterations"] < cold["iterations"]
+    assert np.linalg.norm(host(mg.x) - host(xstar)) <= 1e-3 * np.linalg.norm(host(xstar))
+
+
+def test_max_iters_zero_and_one():
+    s = scenes.box(32, seed=32, levels=3)
+    tag_o, r0, mg = _setup(s)
+    info = mg.solve(0, 1e-12, 0.0, 1e-12, smoother="phases")
+    assert info["iterations"] == 0 and not info["converged"]
+    assert float(mg.x.abs().max()) == 0.0
+    mg.init(dev(r0), 1.0)
+    mg.mask_interior()
+    info = mg.solve(1, 1e-12, 0.0, 1e-12, smoother="phases")
+    ref = O.pcg(r0, O.tag_levels(tag_o, 3), max_iters=1, abs_tol=0.0, rel_tol=1e-12)
+    assert info["iterations"] == ref["iters"] == 1
+    assert np.linalg.norm(host(mg.x) - ref["x"]) <= 1e-6 * np.linalg.norm(ref["x"])
+
+
+def test_no_fluid():
+    shape = (16, 16, 16)
+    mg = MGPCG(3, shape, 2)
+    mg.set_tags(torch.zeros(shape, dtype=torch.int32, device="cuda"))
+    mg.init(torch.ones(shape, device="cuda"), 1.0)
+    mg.mask_interior()
+    info = mg.solve(200, 1e-12, 1e-12, 1e-12, smoother="phases")  # rTr0 = 0 < abs_tol
+    assert info["converged"] and info["iterations"] == 0 and info["rtr0"] == 0.0
+    assert float(mg.x.abs().max()) == 0.0
+    info = mg.solve(5, 1e-12, 0.0, 1e-12, smoother="phases")      # tol 0: runs to max_iters, like the reference
+    assert info["iterations"] == 5 and not info["converged"]
+
+
+def test_non_cubic_grid_matches_oracle():
+    """The reference's default grid is 256 x 64 x 256 (const_param.py:34-37); a
+    32 x 8 x 32 version of it with 3 levels."""
+    shape = (32, 8, 32)
+    rng = np.random.default_rng(33)
+    phi = (rng.uniform(-1, 1, shape) + 0.3).astype(np.float32)
+    tag_o = O.tag_dirichlet(phi)
+    tag_o[:, 0, :] = 1
+    tag_o[0, 0, 0] = 0
+    u, v, w = scenes.fourier_faces(shape, 33)
+    zeros = [np.zeros_like(a) for a in (u, v, w)]
+    div = O.divergence(u, v, w, *zeros, tag_o)
+    r0 = np.where(tag_o == 1, div, 0).astype(np.float32)
+    vel, velr = mac(u, v, w), mac(*zeros)
+    assert np.array_equal(host(K.divergence(vel, velr, dev(tag_o))), div)
+    mg = MGPCG(3, shape, 3)
+    mg.set_tags(dev(tag_o))
+    mg.init(dev(r0), 1.0)
+    mg.mask_interior()
+    tags = O.tag_levels(tag_o, 3)
+    assert np.array_equal(host(mg.apply_preconditioner(dev(r0))), O.vcycle(r0, tags, np.float32))
+    info = mg.solve(200, 1e-12, 0.0, 1e-12, smoother="phases")
+    ref = O.pcg(r0, tags, max_iters=200, abs_tol=0.0, rel_tol=1e-12, dtype=np.float64)
+    assert abs(info["iterations"] - ref["iters"]) <= 1
+    assert np.linalg.norm(host(mg.x) - ref["x"]) <= PRESSURE_RTOL * np.linalg.norm(ref["x"])
+
+
+def test_host_loop_equals_graph(monkeypatch):
+    s = scenes.dam(32, seed=34, levels=3)
+    tag_o, r0, mg = _setup(s)
+    info_g = mg.solve(200, 1e-12, 0.0, 1e-12, smoother="phases")
+    xg = host(mg.x)
+    monkeypatch.setenv("FLUB_SOLVE_HOST_LOOP", "1")
+    tag_o, r0, mg2 = _setup(s)
+    info_h = mg2.solve(200, 1e-12, 0.0, 1e-12, smoother="phases")
+    assert info_h == info_g
+    assert np.array_equal(host(mg2.x), xg)
+
+
+def test_repeat_solves_are_deterministic():
+    s = scenes.random_scene(32, 35, levels=3)
+    tag_o, r0, mg = _setup(s)
+    mg.solve(200, 1e-12, 0.0, 1e-12, smoother="phases")
+    x1 = host(mg.x)
+    mg.init(dev(r0), 1.0)
+    mg.mask_interior()
+    mg.solve(200, 1e-12, 0.0, 1e-12, smoother="phases")
+    assert np.array_equal(host(mg.x), x1)
+
+
+def test_nan_rhs_reports_breakdown():
+    """A NaN in the right-hand side (made on the host) is reported as a CG
+    breakdown, and the handle stays usable."""
+    s = scenes.box(32, seed=36, levels=3)
+    tag_o, r0, mg = _setup(s)
+    bad = r0.copy()
+    bad[tuple(np.argwhere(tag_o == 1)[0])] = np.nan
+    mg.init(dev(bad), 1.0)
+    mg.mask_interior()
+    with pytest.raises(FlubError):
+        mg.solve(50, 1e-12, 0.0, 1e-12, smoother="phases")
+    mg.init(dev(r0), 1.0)
+    mg.mask_interior()
+    assert mg.solve(200, 1e-12, 0.0, 1e-12, smoother="phases")["converged"]
+
+
+def test_rejects_bad_arguments():
+    with pytest.raises(ValueError):
+        MGPCG(3, (30, 32, 32), 3)
+    mg = MGPCG(3, (16, 16, 16), 2)
+    with pytest.raises(NotImplementedError):
+        mg.solve(1, smoother="default")
+    with pytest.raises(ValueError):
+        mg.set_tags(torch.zeros((8, 8, 8), dtype=torch.int32, device="cuda"))
+
+
+def test_kernel_counter_advances():
+    s = scenes.box(32, seed=37, levels=3)
+    tag_o, r0, mg = _setup(s)
+    k0 = mg.kernels_executed()
+    info = mg.solve(200, 1e-12, 0.0, 1e-12, smoother="phases")
+    assert mg.kernels_executed() > k0 + 10 * info["iterations"]
+
+
+def test_reference_call_sequence():
+    """example_fluid.py:84-147 with water_3d.py:58-68, written with launch()
+    exactly as the reference writes it, against the fused Projection."""
+    s = scenes.dam(32, seed=38, levels=3)
+    shape = s.shape
+    h = h0 = s.h
+    tag = IntField(K.classify(dev(s.phi), s.prims, h, h0))
+    vel, velr = mac(s.u, s.v, s.w), mac(s.ur, s.vr, s.wr)
+    div = Field(torch.zeros(shape, device="cuda"))
+    launch(K.divergence_tag, shape, [vel, div, velr, tag])
+    launch(K.mask_with_tag, shape, [div, tag])
+    launch(K.scale_by_3d, shape, [div, -1.0 / h])
+    p0 = Field(torch.zeros(shape, device="cuda"))
+    mg = MGPCG(3, shape, 3, float)
+    mg.set_tags(tag.f)
+    mg.init(div.f, -h0)
+    mg.mask_interior()
+    mg.solve(200, rel_tol=1e-12, abs_tol=0.0, smoother="phases")
+    p0.f.copy_(mg.x)
+    launch(K.scale_by_3d, shape, [p0, h0])
+    launch(K.scale_by_3d, shape, [p0, 1.0 / h0])
+    for d in (1, 2, 3):
+        fs = list(shape)
+        fs[d - 1] += 1
+        launch(K.subtract_gradient_tag, tuple(fs), [vel, velr, p0, tag, d])
+    proj = Projection(shape, 3)
+    vel2 = mac(s.u, s.v, s.w)
+    proj.project(vel2, velr, dev(s.phi), s.prims)
+    for a, b in zip((vel.u.f, vel.v.f, vel.w.f), (vel2.u.f, vel2.v.f, vel2.w.f)):
+        assert torch.equal(a, b)
