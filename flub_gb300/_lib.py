@@ -70,6 +70,7 @@ SIGNATURES = {
     "flub_mg_matvec": (_i32, [_vp, _vp, _vp, _vp]),
     "flub_mg_kernels_executed": (_i32, [_vp, _vp, ctypes.POINTER(_i64)]),
     "flub_mg_smooth": (_i32, [_vp, _i32, _i32, _vp]),
+    "flub_vcycle_noalloc": (_i32, [_vp, _vp, _vp, _i32, _i32, _i32, _i32, _vp]),
     "flub_launch_count": (_i64, []),
     "flub_reset_launch_count": (None, []),
 }

@@ -13,6 +13,7 @@
 #include <cstddef>
 #include <cstdlib>
 #include <cstring>
+#include <mutex>
 #include <vector>
 
 #include "mg_kernels.cuh"
@@ -520,3 +521,98 @@ int flub_mg_kernels_executed(flub_mg *mg, void *stream, int64_t *out) {
 }
 
 }  // extern "C"
+
+// ---------------------------------------------------------------- allocation-free V-cycle
+//
+// For callers that cannot allocate device memory: a plugin whose host
+// application owns every device allocation (and forbids cudaMalloc inside its
+// frame loop), or a real-time caller that cannot afford cudaMalloc's implicit
+// synchronisation.  flub_vcycle_noalloc keeps the whole level hierarchy in the
+// file-scope device array below instead of a workspace; the caller only passes
+// the tags, r and z.  The array holds grids of up to FLUB_NOALLOC_MAX_CELLS
+// cells and stays resident on every device that loads this library until the
+// process exits.
+
+namespace flub {
+
+constexpr size_t kNoallocScratchBytes = size_t(1) << 20;  // 1 MiB
+
+static __device__ __align__(256) unsigned char g_noalloc_scratch[kNoallocScratchBytes];
+
+// Layout inside the array: level-0 cell codes, then (codes, r, z) of every
+// coarser level, each 256-byte aligned.  Returns the bytes used.
+static size_t noalloc_layout(flub_mg *mg, char *base) {
+    size_t off = 0;
+    auto take = [&](size_t bytes) -> char * {
+        char *p = base ? base + off : nullptr;
+        off += align256(bytes);
+        return p;
+    };
+    for (int l = 0; l < mg->levels; l++) {
+        Level &L = mg->lv[l];
+        L.D = Dims{mg->nx >> l, mg->ny >> l, mg->nz >> l};
+        L.code = (uint8_t *)take((size_t)L.D.n());
+        L.r = l ? (float *)take(sizeof(float) * L.D.n()) : nullptr;
+        L.z = l ? (float *)take(sizeof(float) * L.D.n()) : nullptr;
+    }
+    return off;
+}
+
+static std::mutex g_noalloc_mutex;
+static void *g_noalloc_addr[64];
+
+// Device address of g_noalloc_scratch on the current device, looked up once per
+// device with that device current (a host-side use of the symbol's name is not
+// a device address).
+static int noalloc_scratch_address(void **out) {
+    int dev = 0;
+    FLUB_CHECK_CUDA(cudaGetDevice(&dev));
+    FLUB_REQUIRE(dev >= 0 && dev < 64, "device ordinal %d out of range", dev);
+    std::lock_guard<std::mutex> lock(g_noalloc_mutex);
+    if (!g_noalloc_addr[dev]) {
+        void *p = nullptr;
+        cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
+        if (e != cudaSuccess || p == nullptr) {
+            set_last_error("cudaGetSymbolAddress(g_noalloc_scratch) on device %d: %s", dev, cudaGetErrorString(e));
+            cudaGetLastError();
+            return FLUB_ERR_CUDA;
+        }
+        g_noalloc_addr[dev] = p;
+    }
+    *out = g_noalloc_addr[dev];
+    return FLUB_OK;
+}
+
+}  // namespace flub
+
+extern "C" int flub_vcycle_noalloc(const int32_t *tag, const float *r, float *z, int nx, int ny, int nz, int levels,
+                                   void *stream) {
+    FLUB_REQUIRE(tag && r && z, "flub_vcycle_noalloc: NULL argument");
+    FLUB_TRY(validate_shape(nx, ny, nz, levels, FLUB_PRECISION_FP32));
+    const int64_t n = (int64_t)nx * ny * nz;
+    FLUB_REQUIRE(n <= FLUB_NOALLOC_MAX_CELLS,
+                 "flub_vcycle_noalloc: %lld cells exceed the allocation-free limit of %d cells (64^3)", (long long)n,
+                 FLUB_NOALLOC_MAX_CELLS);
+    flub_mg mg;  // host-side descriptor only; every level pointer points into the static array
+    memset(&mg, 0, sizeof(mg));
+    mg.nx = nx; mg.ny = ny; mg.nz = nz; mg.levels = levels; mg.n = n;
+    const size_t need = noalloc_layout(&mg, nullptr);
+    FLUB_REQUIRE(need <= kNoallocScratchBytes, "flub_vcycle_noalloc: hierarchy needs %zu bytes > %zu", need,
+                 kNoallocScratchBytes);
+    void *base = nullptr;
+    FLUB_TRY(noalloc_scratch_address(&base));
+    noalloc_layout(&mg, (char *)base);
+    cudaStream_t s = as_stream(stream);
+    // every scratch element is written before it is read: the codes by these two
+    // kernels, z_l by the first (from-zero) sweep of its level, r_l by the
+    // restriction, so nothing has to be cleared between calls
+    k_encode_tags<<<blocks_for(n, 256), 256, 0, s>>>(tag, mg.lv[0].code, n);
+    FLUB_CHECK_LAUNCH();
+    for (int l = 0; l + 1 < levels; l++) {
+        const Level &C = mg.lv[l + 1];
+        k_restrict_codes<<<blocks_for(C.D.n(), 256), 256, 0, s>>>(mg.lv[l].code, C.code, C.D);
+        FLUB_CHECK_LAUNCH();
+    }
+    LaunchCtx c{s, nullptr, 0, 0};
+    return enqueue_vcycle(&mg, c, r, z);
+}

@@ -201,6 +201,24 @@ int flub_mg_matvec(flub_mg *mg, const float *p, float *Ap, void *stream);
  * vectors z and r).  The same kernel the V-cycle launches. */
 int flub_mg_smooth(flub_mg *mg, int level, int phase, void *stream);
 
+/* Allocation-free V-cycle.  No counterpart in the reference: it exists for
+ * callers that cannot allocate device memory themselves -- a plugin whose host
+ * application owns every device allocation and forbids cudaMalloc in its frame
+ * loop, or a real-time caller that cannot pay for cudaMalloc's implicit
+ * synchronisation.  Computes z = M r exactly as flub_mg_set_tags(tag) followed
+ * by flub_mg_apply_preconditioner(r, z) would (same kernels, same results),
+ * but keeps the level hierarchy in a 1 MiB array compiled into the library
+ * (resident on every device that loads it, until the process exits) and
+ * allocates nothing.  Limits: nx * ny * nz <= FLUB_NOALLOC_MAX_CELLS, plus
+ * the shape rules of flub_mg_create; larger grids are rejected with
+ * FLUB_ERR_INVALID_ARGUMENT.  The first call on each device looks up the
+ * array's device address; make that first call before any stream capture.
+ * Every call shares the one array: calls that can overlap on the GPU (other
+ * streams, other host threads) race and must be serialised by the caller. */
+#define FLUB_NOALLOC_MAX_CELLS 262144 /* 64^3 */
+int flub_vcycle_noalloc(const int32_t *tag, const float *r, float *z, int nx, int ny, int nz, int levels,
+                        void *stream);
+
 /* Solver kernels executed on the device inside solve graphs by this handle
  * since it was created (each kernel node counts once per execution).
  * Synchronises the stream. */
