@@ -32,8 +32,16 @@ struct Dims {
     __host__ __device__ int64_t n() const { return (int64_t)nx * ny * nz; }
 };
 
+// Entry of every solver kernel.  Programmatic dependent launch: let the next
+// kernel of the stream start launching now, then wait until the previous one
+// has completed and its writes are visible (both are no-ops for a launch
+// without the programmatic-serialisation attribute).  Then one increment of the
+// kernel counter per launch (first thread of the first block).
 __device__ __forceinline__ void count_kernel(unsigned long long *kc) {
-    if (kc && blockIdx.x == 0 && threadIdx.x == 0) atomicAdd(kc, 1ull);
+    asm volatile("griddepcontrol.launch_dependents;" ::: "memory");
+    asm volatile("griddepcontrol.wait;" ::: "memory");
+    if (kc && (blockIdx.x | blockIdx.y | blockIdx.z | threadIdx.x | threadIdx.y | threadIdx.z) == 0)
+        atomicAdd(kc, 1ull);
 }
 
 // L x at cell c (i, j, k); returns the value and the diagonal count d.
@@ -236,8 +244,9 @@ __global__ void __launch_bounds__(256) k_restrict(const float *__restrict__ rf, 
     }
 }
 
-// multigrid/mgpcg.py:113-116 _prolongate: z_h += z_2h[I/2].
-__global__ void __launch_bounds__(256) k_prolong(float *__restrict__ zf, const float *__restrict__ zc, Dims F,
+// multigrid/mgpcg.py:113-116 _prolongate: z_h += z_2h[I/2], written to zout
+// (zout may equal zin).
+__global__ void __launch_bounds__(256) k_prolong(float *zout, const float *zin, const float *__restrict__ zc, Dims F,
                                                  unsigned long long *kc) {
     count_kernel(kc);
     const int64_t n = F.n();
@@ -245,7 +254,7 @@ __global__ void __launch_bounds__(256) k_prolong(float *__restrict__ zf, const f
     for (int64_t c = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; c < n; c += (int64_t)gridDim.x * blockDim.x) {
         int i, j, k;
         unflatten(c, F, i, j, k);
-        zf[c] = __fadd_rn(zf[c], zc[((int64_t)(i >> 1) * cy + (j >> 1)) * cz + (k >> 1)]);
+        zout[c] = __fadd_rn(zin[c], zc[((int64_t)(i >> 1) * cy + (j >> 1)) * cz + (k >> 1)]);
     }
 }
 

@@ -17,16 +17,25 @@
 #include <vector>
 
 #include "mg_kernels.cuh"
+#include "smooth8.cuh"
+#include "tail.cuh"
 
 namespace flub {
 
 constexpr int kMaxLevels = 12;
+constexpr size_t kTailMaxSmem = 200 * 1024;  // dynamic shared memory of the tail kernel
 
+// Per level: cell codes, residual r, and two correction buffers.  Pre-smoothing
+// and the restriction work on z2; the prolongation writes z2 + P z_coarse into
+// z while it runs the first post-smoothing sweep, and post-smoothing finishes
+// in place on z, which therefore holds the level's final correction (at level
+// 0 the caller's z).
 struct Level {
     Dims D;
     uint8_t *code;
     float *r;
     float *z;
+    float *z2;
 };
 
 struct LaunchCtx {
@@ -55,6 +64,9 @@ struct flub_mg {
     int graph_nodes[3];
     cudaStream_t cap_stream, cap_stream2;
     bool host_loop;
+    bool skip_ok;  // internal z buffers keep z = 0 off the fluid (see k_smooth8)
+    int tail_start;  // first level run by the one-block tail kernel (== levels: none)
+    size_t tail_smem;
 };
 
 namespace flub {
@@ -88,8 +100,56 @@ static size_t carve(flub_mg *mg, char *base) {
         L.code = (uint8_t *)take(nl);
         L.r = (float *)take(sizeof(float) * nl);
         L.z = (float *)take(sizeof(float) * nl);
+        L.z2 = (float *)take(sizeof(float) * nl);
     }
     return off;
+}
+
+// Shared-memory layout of the tail kernel from level lt down; returns the
+// bytes needed (0 if the tail does not qualify).
+static size_t tail_layout(const flub_mg *mg, int lt, TailParams *P) {
+    if (lt >= mg->levels || mg->levels - lt > kTailMaxLevels) return 0;
+    size_t off = 0;
+    auto take = [&](size_t b) {
+        size_t o = off;
+        off += (b + 15) & ~(size_t)15;
+        return (int)o;
+    };
+    for (int l = lt; l < mg->levels; l++) {
+        const Dims D{mg->nx >> l, mg->ny >> l, mg->nz >> l};
+        const size_t n = (size_t)D.n();
+        TailLevel &T = P->lv[l - lt];
+        T.D = D;
+        T.code = mg->lv[l].code;
+        T.abs_level = l;
+        T.off_z = take(sizeof(float) * n);
+        T.off_r = take(sizeof(float) * n);
+        T.off_c = take(n);
+    }
+    P->nt = mg->levels - lt;
+    return off;
+}
+
+static int set_tail_smem_limit() {
+    FLUB_CHECK_CUDA(cudaFuncSetAttribute(k_tail_vcycle, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kTailMaxSmem));
+    return FLUB_OK;
+}
+
+static int choose_tail(flub_mg *mg) {
+    mg->tail_start = mg->levels;
+    mg->tail_smem = 0;
+    for (int l = 0; l < mg->levels; l++) {
+        const Dims D{mg->nx >> l, mg->ny >> l, mg->nz >> l};
+        if (D.n() > kTailMaxCells) continue;
+        TailParams P;
+        const size_t b = tail_layout(mg, l, &P);
+        if (b > 0 && b <= kTailMaxSmem) {
+            mg->tail_start = l;
+            mg->tail_smem = b;
+        }
+        break;
+    }
+    return FLUB_OK;
 }
 
 static int validate_shape(int nx, int ny, int nz, int levels, int precision) {
@@ -109,58 +169,117 @@ static inline unsigned red_blocks(int64_t n) { return blocks_for(n, kRedThreads,
 
 // ---------------------------------------------------------------- enqueue helpers
 
-static int smooth(const LaunchCtx &c, const Level &L, int phase, bool from_zero, const float *r, float *z) {
-    const int64_t npairs = L.D.n() / 2;
-    const unsigned b = blocks_for(npairs, 256, 1 << 20);
-    if (from_zero)
-        k_smooth_half<true><<<b, 256, 0, c.s>>>(z, r, L.code, L.D, phase, c.kc);
-    else
-        k_smooth_half<false><<<b, 256, 0, c.s>>>(z, r, L.code, L.D, phase, c.kc);
-    FLUB_CHECK_LAUNCH();
-    return FLUB_OK;
-}
-
 #define FLUB_TRY(x)            \
     do {                       \
         int _s = (x);          \
         if (_s) return _s;     \
     } while (0)
 
+// Kernel launch with programmatic stream serialisation (the kernel's entry
+// waits on griddepcontrol.wait, see count_kernel), counted like the others.
+template <typename... KArgs, typename... Args>
+static int launch_pdl(void (*kern)(KArgs...), dim3 g, dim3 b, size_t smem, cudaStream_t s, Args... args) {
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = g;
+    cfg.blockDim = b;
+    cfg.dynamicSmemBytes = smem;
+    cfg.stream = s;
+    cudaLaunchAttribute attr[1];
+    attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+    attr[0].val.programmaticStreamSerializationAllowed = 1;
+    cfg.attrs = attr;
+    cfg.numAttrs = 1;
+    cudaError_t e = cudaLaunchKernelEx(&cfg, kern, ((KArgs)args)...);
+    if (e != cudaSuccess) {
+        set_last_error("cudaLaunchKernelEx: %s", cudaGetErrorString(e));
+        cudaGetLastError();
+        return FLUB_ERR_CUDA;
+    }
+    count_launches(1);
+    return FLUB_OK;
+}
+
+enum SweepMode { kSweepInPlace = 0, kSweepFromZero = 1, kSweepProlong = 2 };
+
+// One red-black half-sweep on level L (multigrid/mgpcg.py:72-86):
+//   kSweepInPlace   zout = sweep(zout)
+//   kSweepFromZero  zout = sweep(0)
+//   kSweepProlong   zout = sweep(zin + P zc)   (mgpcg.py:113-116 fused in)
+static int sweep(const LaunchCtx &c, const Level &L, int phase, int mode, int skip, const float *r,
+                 const float *zin, float *zout, const float *zc) {
+    const Dims D = L.D;
+    if (D.nz % 8 == 0) {
+        const int nz8 = D.nz >> 3;
+        const int bx = nz8 < 32 ? nz8 : 32, by = 256 / bx;
+        const dim3 blk(bx, by), grd((nz8 + bx - 1) / bx, (D.ny + by - 1) / by, D.nx);
+        if (mode == kSweepFromZero)
+            return launch_pdl(k_smooth8<true, false>, grd, blk, 0, c.s, zout, (const float *)zout,
+                              (const float *)nullptr, r, (const uint8_t *)L.code, D, phase, skip, c.kc);
+        if (mode == kSweepProlong)
+            return launch_pdl(k_smooth8<false, true>, grd, blk, 0, c.s, zout, zin, zc, r, (const uint8_t *)L.code, D,
+                              phase, skip, c.kc);
+        return launch_pdl(k_smooth8<false, false>, grd, blk, 0, c.s, zout, (const float *)zout,
+                          (const float *)nullptr, r, (const uint8_t *)L.code, D, phase, skip, c.kc);
+    }
+    // scalar path for levels whose nz is not a multiple of 8
+    if (mode == kSweepProlong)
+        FLUB_TRY(launch_pdl(k_prolong, dim3(blocks_for(D.n(), 256, 1 << 20)), dim3(256), 0, c.s, zout, zin, zc, D,
+                            c.kc));
+    const unsigned b = blocks_for(D.n() / 2, 256, 1 << 20);
+    if (mode == kSweepFromZero)
+        return launch_pdl(k_smooth_half<true>, dim3(b), dim3(256), 0, c.s, zout, r, (const uint8_t *)L.code, D, phase,
+                          c.kc);
+    return launch_pdl(k_smooth_half<false>, dim3(b), dim3(256), 0, c.s, zout, r, (const uint8_t *)L.code, D, phase,
+                      c.kc);
+}
+
+
 // multigrid/mgpcg.py:296-349 apply_preconditioner; level 0 uses (r0, z0).
-static int enqueue_vcycle(flub_mg *mg, const LaunchCtx &c, const float *r0, float *z0) {
-    const int Lm = mg->levels;
+// z0_clean: z0 holds 0 on every non-fluid cell (true for the handle's own z).
+static int enqueue_vcycle(flub_mg *mg, const LaunchCtx &c, const float *r0, float *z0, bool z0_clean) {
+    const int Lm = mg->levels, lt = mg->tail_start;
+    const int sk = mg->skip_ok ? 1 : 0;
+    auto SK = [&](int l) { return (l == 0 && !z0_clean) ? 0 : sk; };
     auto R = [&](int l) -> const float * { return l == 0 ? r0 : mg->lv[l].r; };
-    auto Z = [&](int l) -> float * { return l == 0 ? z0 : mg->lv[l].z; };
-    for (int l = 0; l < Lm - 1; l++) {
+    auto ZF = [&](int l) -> float * { return l == 0 ? z0 : mg->lv[l].z; };
+    auto ZP = [&](int l) -> float * { return mg->lv[l].z2; };
+    const int lg = lt < Lm - 1 ? lt : Lm - 1;  // levels 0 .. lg-1 restrict to a coarser level
+    for (int l = 0; l < lg; l++) {
         const Level &L = mg->lv[l];
         const int iters = 6 << l;
         for (int it = 0; it < iters; it++) {
-            FLUB_TRY(smooth(c, L, 0, it == 0, R(l), Z(l)));
-            FLUB_TRY(smooth(c, L, 1, false, R(l), Z(l)));
+            FLUB_TRY(sweep(c, L, 0, it == 0 ? kSweepFromZero : kSweepInPlace, sk, R(l), ZP(l), ZP(l), nullptr));
+            FLUB_TRY(sweep(c, L, 1, kSweepInPlace, sk, R(l), ZP(l), ZP(l), nullptr));
         }
         const Level &C = mg->lv[l + 1];
-        k_restrict<<<blocks_for(C.D.n(), 256, 1 << 20), 256, 0, c.s>>>(R(l), Z(l), L.code, C.r, C.code, C.D, c.kc);
-        FLUB_CHECK_LAUNCH();
+        FLUB_TRY(launch_pdl(k_restrict, dim3(blocks_for(C.D.n(), 256, 1 << 20)), dim3(256), 0, c.s, R(l), ZP(l),
+                            L.code, C.r, C.code, C.D, c.kc));
     }
-    {
-        const Level &L = mg->lv[Lm - 1];
+    if (lt < Lm) {
+        TailParams P;
+        tail_layout(mg, lt, &P);
+        P.r_top = R(lt);
+        P.z_top = ZF(lt);
+        FLUB_TRY(launch_pdl(k_tail_vcycle, dim3(1), dim3(kTailThreads), mg->tail_smem, c.s, P, c.kc));
+    } else {
+        const int b = Lm - 1;
+        const Level &L = mg->lv[b];
         for (int it = 0; it < 3; it++) {
-            FLUB_TRY(smooth(c, L, 0, it == 0, R(Lm - 1), Z(Lm - 1)));
-            FLUB_TRY(smooth(c, L, 1, false, R(Lm - 1), Z(Lm - 1)));
+            FLUB_TRY(sweep(c, L, 0, it == 0 ? kSweepFromZero : kSweepInPlace, SK(b), R(b), ZF(b), ZF(b), nullptr));
+            FLUB_TRY(sweep(c, L, 1, kSweepInPlace, SK(b), R(b), ZF(b), ZF(b), nullptr));
         }
         for (int it = 0; it < 3; it++) {
-            FLUB_TRY(smooth(c, L, 1, false, R(Lm - 1), Z(Lm - 1)));
-            FLUB_TRY(smooth(c, L, 0, false, R(Lm - 1), Z(Lm - 1)));
+            FLUB_TRY(sweep(c, L, 1, kSweepInPlace, SK(b), R(b), ZF(b), ZF(b), nullptr));
+            FLUB_TRY(sweep(c, L, 0, kSweepInPlace, SK(b), R(b), ZF(b), ZF(b), nullptr));
         }
     }
-    for (int l = Lm - 2; l >= 0; l--) {
+    for (int l = lg - 1; l >= 0; l--) {
         const Level &L = mg->lv[l];
-        k_prolong<<<blocks_for(L.D.n(), 256, 1 << 20), 256, 0, c.s>>>(Z(l), mg->lv[l + 1].z, L.D, c.kc);
-        FLUB_CHECK_LAUNCH();
         const int iters = 6 << l;
         for (int it = 0; it < iters; it++) {
-            FLUB_TRY(smooth(c, L, 1, false, R(l), Z(l)));
-            FLUB_TRY(smooth(c, L, 0, false, R(l), Z(l)));
+            FLUB_TRY(sweep(c, L, 1, it == 0 ? kSweepProlong : kSweepInPlace, SK(l), R(l), ZP(l), ZF(l),
+                           mg->lv[l + 1].z));
+            FLUB_TRY(sweep(c, L, 0, kSweepInPlace, SK(l), R(l), ZF(l), ZF(l), nullptr));
         }
     }
     return FLUB_OK;
@@ -168,10 +287,8 @@ static int enqueue_vcycle(flub_mg *mg, const LaunchCtx &c, const float *r0, floa
 
 static int enqueue_mean_removal(flub_mg *mg, const LaunchCtx &c, int guard) {
     const unsigned b = red_blocks(mg->n);
-    k_fluid_mean<<<b, kRedThreads, 0, c.s>>>(mg->st, mg->lv[0].r, mg->lv[0].code, mg->n, mg->partials, guard, c.kc);
-    FLUB_CHECK_LAUNCH();
-    k_sub_mean<<<b, kRedThreads, 0, c.s>>>(mg->st, mg->lv[0].r, mg->lv[0].code, mg->n, guard, c.kc);
-    FLUB_CHECK_LAUNCH();
+    FLUB_TRY(launch_pdl(k_fluid_mean, dim3(b), dim3(kRedThreads), 0, c.s, mg->st, mg->lv[0].r, mg->lv[0].code, mg->n, mg->partials, guard, c.kc));
+    FLUB_TRY(launch_pdl(k_sub_mean, dim3(b), dim3(kRedThreads), 0, c.s, mg->st, mg->lv[0].r, mg->lv[0].code, mg->n, guard, c.kc));
     return FLUB_OK;
 }
 
@@ -179,14 +296,12 @@ static int enqueue_prologue(flub_mg *mg, const LaunchCtx &c, int smoother) {
     const unsigned b = red_blocks(mg->n);
     const Level &L0 = mg->lv[0];
     if (smoother == FLUB_SMOOTHER_FRACTION) FLUB_TRY(enqueue_mean_removal(mg, c, 0));
-    k_dot_rr0<<<b, kRedThreads, 0, c.s>>>(mg->st, L0.r, mg->n, mg->partials, c.kc);
-    FLUB_CHECK_LAUNCH();
-    k_residual_x0<<<blocks_for(mg->n, 256), 256, 0, c.s>>>(mg->st, L0.r, mg->x, L0.code, L0.D, c.kc);
-    FLUB_CHECK_LAUNCH();
+    FLUB_TRY(launch_pdl(k_dot_rr0, dim3(b), dim3(kRedThreads), 0, c.s, mg->st, L0.r, mg->n, mg->partials, c.kc));
+    FLUB_TRY(launch_pdl(k_residual_x0, dim3(blocks_for(mg->n, 256)), dim3(256), 0, c.s, mg->st, L0.r, mg->x, L0.code,
+                        L0.D, c.kc));
     if (smoother == FLUB_SMOOTHER_FRACTION) FLUB_TRY(enqueue_mean_removal(mg, c, 2));
-    FLUB_TRY(enqueue_vcycle(mg, c, L0.r, L0.z));
-    k_dot_zr_init<<<b, kRedThreads, 0, c.s>>>(mg->st, L0.z, L0.r, mg->p, mg->n, mg->partials, c.kc);
-    FLUB_CHECK_LAUNCH();
+    FLUB_TRY(enqueue_vcycle(mg, c, L0.r, L0.z, true));
+    FLUB_TRY(launch_pdl(k_dot_zr_init, dim3(b), dim3(kRedThreads), 0, c.s, mg->st, L0.z, L0.r, mg->p, mg->n, mg->partials, c.kc));
     return FLUB_OK;
 }
 
@@ -194,38 +309,30 @@ static int enqueue_prologue(flub_mg *mg, const LaunchCtx &c, int smoother) {
 static int enqueue_first_half(flub_mg *mg, const LaunchCtx &c, int smoother) {
     const unsigned b = red_blocks(mg->n);
     const Level &L0 = mg->lv[0];
-    k_matvec_pap<<<b, kRedThreads, 0, c.s>>>(mg->st, mg->p, mg->Ap, L0.code, L0.D, mg->partials, c.kc);
-    FLUB_CHECK_LAUNCH();
+    FLUB_TRY(launch_pdl(k_matvec_pap, dim3(b), dim3(kRedThreads), 0, c.s, mg->st, mg->p, mg->Ap, L0.code, L0.D, mg->partials, c.kc));
     if (smoother == FLUB_SMOOTHER_FRACTION) {
-        k_update_r<<<b, kRedThreads, 0, c.s>>>(mg->st, L0.r, mg->Ap, mg->n, c.kc);
-        FLUB_CHECK_LAUNCH();
+        FLUB_TRY(launch_pdl(k_update_r, dim3(b), dim3(kRedThreads), 0, c.s, mg->st, L0.r, mg->Ap, mg->n, c.kc));
         FLUB_TRY(enqueue_mean_removal(mg, c, 1));
-        k_update_r_rr<false><<<b, kRedThreads, 0, c.s>>>(mg->st, L0.r, mg->Ap, mg->n, mg->partials, mg->hist, c.h,
-                                                         c.set_cond, c.kc);
-    } else {
-        k_update_r_rr<true><<<b, kRedThreads, 0, c.s>>>(mg->st, L0.r, mg->Ap, mg->n, mg->partials, mg->hist, c.h,
-                                                        c.set_cond, c.kc);
+        return launch_pdl(k_update_r_rr<false>, dim3(b), dim3(kRedThreads), 0, c.s, mg->st, L0.r, mg->Ap, mg->n,
+                          mg->partials, mg->hist, c.h, c.set_cond, c.kc);
     }
-    FLUB_CHECK_LAUNCH();
-    return FLUB_OK;
+    return launch_pdl(k_update_r_rr<true>, dim3(b), dim3(kRedThreads), 0, c.s, mg->st, L0.r, mg->Ap, mg->n,
+                      mg->partials, mg->hist, c.h, c.set_cond, c.kc);
 }
 
 // z = M r, beta, x += alpha p, p = z + beta p, it += 1.
 static int enqueue_second_half(flub_mg *mg, const LaunchCtx &c) {
     const unsigned b = red_blocks(mg->n);
     const Level &L0 = mg->lv[0];
-    FLUB_TRY(enqueue_vcycle(mg, c, L0.r, L0.z));
-    k_dot_zr_beta<<<b, kRedThreads, 0, c.s>>>(mg->st, L0.z, L0.r, mg->n, mg->partials, c.kc);
-    FLUB_CHECK_LAUNCH();
-    k_update_xp<<<blocks_for(mg->n, 256), 256, 0, c.s>>>(mg->st, mg->x, mg->p, L0.z, mg->n, c.kc);
-    FLUB_CHECK_LAUNCH();
-    return FLUB_OK;
+    FLUB_TRY(enqueue_vcycle(mg, c, L0.r, L0.z, true));
+    FLUB_TRY(launch_pdl(k_dot_zr_beta, dim3(b), dim3(kRedThreads), 0, c.s, mg->st, L0.z, L0.r, mg->n, mg->partials, c.kc));
+    return launch_pdl(k_update_xp, dim3(blocks_for(mg->n, 256)), dim3(256), 0, c.s, mg->st, mg->x, mg->p, L0.z, mg->n,
+                      c.kc);
 }
 
 static int enqueue_epilogue(flub_mg *mg, const LaunchCtx &c) {
-    k_solve_end<<<blocks_for(mg->n, 256), 256, 0, c.s>>>(mg->st, mg->x, mg->p, mg->n, c.kc);
-    FLUB_CHECK_LAUNCH();
-    return FLUB_OK;
+    return launch_pdl(k_solve_end, dim3(blocks_for(mg->n, 256)), dim3(256), 0, c.s, mg->st, mg->x, mg->p, mg->n,
+                      c.kc);
 }
 
 // Builds prologue -> while(body) -> epilogue with stream capture.
@@ -367,6 +474,12 @@ int flub_mg_create(int nx, int ny, int nz, int levels, int precision, void *work
     }
     const char *hl = getenv("FLUB_SOLVE_HOST_LOOP");
     mg->host_loop = hl && hl[0] == '1';
+    mg->skip_ok = true;  // the workspace is zeroed below and set_tags re-zeroes the z buffers
+    choose_tail(mg);
+    if (set_tail_smem_limit() != FLUB_OK) {
+        flub_mg_destroy(mg);
+        return FLUB_ERR_CUDA;
+    }
     // zero the state and all vectors once so that every buffer is defined
     if (cudaMemset(mg->ws, 0, need) != cudaSuccess || cudaDeviceSynchronize() != cudaSuccess) {
         flub_mg_destroy(mg);
@@ -397,6 +510,12 @@ int flub_mg_set_tags(flub_mg *mg, const int32_t *tag, void *stream) {
         const Level &C = mg->lv[l + 1];
         k_restrict_codes<<<blocks_for(C.D.n(), 256), 256, 0, s>>>(mg->lv[l].code, C.code, C.D);
         FLUB_CHECK_LAUNCH();
+    }
+    // new tags: re-establish z = 0 off the fluid in every correction buffer
+    for (int l = 0; l < mg->levels; l++) {
+        const size_t b = sizeof(float) * (size_t)mg->lv[l].D.n();
+        FLUB_CHECK_CUDA(cudaMemsetAsync(mg->lv[l].z, 0, b, s));
+        FLUB_CHECK_CUDA(cudaMemsetAsync(mg->lv[l].z2, 0, b, s));
     }
     return FLUB_OK;
 }
@@ -490,7 +609,7 @@ int flub_mg_get_x(flub_mg *mg, float *out, float scale, void *stream) {
 int flub_mg_apply_preconditioner(flub_mg *mg, const float *r, float *z, void *stream) {
     FLUB_REQUIRE(mg && r && z, "flub_mg_apply_preconditioner: NULL argument");
     LaunchCtx c{as_stream(stream), nullptr, 0, 0};
-    return enqueue_vcycle(mg, c, r, z);
+    return enqueue_vcycle(mg, c, r, z, false);
 }
 
 int flub_mg_matvec(flub_mg *mg, const float *p, float *Ap, void *stream) {
@@ -507,7 +626,7 @@ int flub_mg_smooth(flub_mg *mg, int level, int phase, void *stream) {
     FLUB_REQUIRE(phase == 0 || phase == 1, "flub_mg_smooth: phase must be 0 or 1");
     LaunchCtx c{as_stream(stream), nullptr, 0, 0};
     const Level &L = mg->lv[level];
-    return smooth(c, L, phase, false, L.r, L.z);
+    return sweep(c, L, phase, kSweepInPlace, mg->skip_ok ? 1 : 0, L.r, L.z, L.z, nullptr);
 }
 
 int flub_mg_kernels_executed(flub_mg *mg, void *stream, int64_t *out) {
@@ -535,12 +654,13 @@ int flub_mg_kernels_executed(flub_mg *mg, void *stream, int64_t *out) {
 
 namespace flub {
 
-constexpr size_t kNoallocScratchBytes = size_t(1) << 20;  // 1 MiB
+constexpr size_t kNoallocScratchBytes = size_t(2) << 20;  // 2 MiB
 
 static __device__ __align__(256) unsigned char g_noalloc_scratch[kNoallocScratchBytes];
 
-// Layout inside the array: level-0 cell codes, then (codes, r, z) of every
-// coarser level, each 256-byte aligned.  Returns the bytes used.
+// Layout inside the array: level-0 cell codes and pre-smoothing buffer, then
+// (codes, r, z, z2) of every coarser level, each 256-byte aligned.  Returns
+// the bytes used.
 static size_t noalloc_layout(flub_mg *mg, char *base) {
     size_t off = 0;
     auto take = [&](size_t bytes) -> char * {
@@ -554,6 +674,7 @@ static size_t noalloc_layout(flub_mg *mg, char *base) {
         L.code = (uint8_t *)take((size_t)L.D.n());
         L.r = l ? (float *)take(sizeof(float) * L.D.n()) : nullptr;
         L.z = l ? (float *)take(sizeof(float) * L.D.n()) : nullptr;
+        L.z2 = (float *)take(sizeof(float) * L.D.n());
     }
     return off;
 }
@@ -602,6 +723,8 @@ extern "C" int flub_vcycle_noalloc(const int32_t *tag, const float *r, float *z,
     void *base = nullptr;
     FLUB_TRY(noalloc_scratch_address(&base));
     noalloc_layout(&mg, (char *)base);
+    choose_tail(&mg);
+    FLUB_TRY(set_tail_smem_limit());
     cudaStream_t s = as_stream(stream);
     // every scratch element is written before it is read: the codes by these two
     // kernels, z_l by the first (from-zero) sweep of its level, r_l by the
@@ -614,5 +737,5 @@ extern "C" int flub_vcycle_noalloc(const int32_t *tag, const float *r, float *z,
         FLUB_CHECK_LAUNCH();
     }
     LaunchCtx c{s, nullptr, 0, 0};
-    return enqueue_vcycle(&mg, c, r, z);
+    return enqueue_vcycle(&mg, c, r, z, false);  // mg.skip_ok is false: every sweep writes every cell
 }

@@ -1,0 +1,166 @@
+// Vectorised red-black smoothing: one thread owns 8 consecutive cells along k.
+//
+// Same arithmetic as k_smooth_half (multigrid/mgpcg.py:72-86) cell by cell, in
+// the reference's order, so results stay bit-identical; the gain is in the
+// instruction count: every row of 8 values is one pair of 16-byte loads (z, r)
+// or one 8-byte load (cell codes), and indices are 32-bit.
+#pragma once
+
+#include "mg_kernels.cuh"
+
+namespace flub {
+
+struct Row8 {
+    float v[8];
+};
+
+__device__ __forceinline__ void load_row8(const float *__restrict__ p, Row8 &o) {
+    const float4 a = __ldg(reinterpret_cast<const float4 *>(p));
+    const float4 b = __ldg(reinterpret_cast<const float4 *>(p) + 1);
+    o.v[0] = a.x; o.v[1] = a.y; o.v[2] = a.z; o.v[3] = a.w;
+    o.v[4] = b.x; o.v[5] = b.y; o.v[6] = b.z; o.v[7] = b.w;
+}
+
+// Row of z that may be written by other threads of the same launch (other
+// colour only): plain loads, not the read-only path.
+__device__ __forceinline__ void load_row8_rw(const float *p, Row8 &o) {
+    const float4 a = reinterpret_cast<const float4 *>(p)[0];
+    const float4 b = reinterpret_cast<const float4 *>(p)[1];
+    o.v[0] = a.x; o.v[1] = a.y; o.v[2] = a.z; o.v[3] = a.w;
+    o.v[4] = b.x; o.v[5] = b.y; o.v[6] = b.z; o.v[7] = b.w;
+}
+
+__device__ __forceinline__ void zero_row8(Row8 &o) {
+#pragma unroll
+    for (int m = 0; m < 8; m++) o.v[m] = 0.0f;
+}
+
+__device__ __forceinline__ uint2 load_codes8(const uint8_t *__restrict__ p) {
+    return __ldg(reinterpret_cast<const uint2 *>(p));
+}
+
+__device__ __forceinline__ uint8_t code_at(uint2 c, int m) {
+    return (uint8_t)(((m < 4 ? c.x : c.y) >> (8 * (m & 3))) & 0xffu);
+}
+
+// z_eff[m] += zc[parent] for the 8 cells of a row whose coarse row starts at pc
+// (4 coarse values: cell m has parent m / 2).
+__device__ __forceinline__ void add_coarse_row8(Row8 &o, const float *__restrict__ pc) {
+    const float4 c = __ldg(reinterpret_cast<const float4 *>(pc));
+    const float cv[4] = {c.x, c.y, c.z, c.w};
+#pragma unroll
+    for (int m = 0; m < 8; m++) o.v[m] = __fadd_rn(o.v[m], cv[m >> 1]);
+}
+
+// One half-sweep over 8 cells per thread.
+//   kFromZero: z is 0 before the sweep (first sweep of a level in the V-cycle);
+//              zin and zc are not read.
+//   kProlong:  the sweep reads zin + zc[I/2] (multigrid/mgpcg.py:113-116 fused
+//              into the first post-smoothing sweep) and writes every cell to
+//              zout != zin; otherwise zout == zin (in place).
+// Every non-fluid cell is written as 0 (its value is never read by a fluid
+// cell's update, and the reference's sweeps leave it 0 by the end of the
+// V-cycle), so a buffer that starts at 0 keeps z = 0 off the fluid.  With
+// skip_inactive set the caller asserts that invariant for zout, and a thread
+// whose 8 cells hold no fluid cell returns without touching z or r.
+// Grid: x over k groups of 8, y over j, z over i.  Requires nz % 8 == 0.
+template <bool kFromZero, bool kProlong>
+__global__ void __launch_bounds__(256, 4) k_smooth8(float *zout, const float *zin, const float *__restrict__ zc,
+                                                    const float *__restrict__ r, const uint8_t *__restrict__ code,
+                                                    Dims D, int phase, int skip_inactive, unsigned long long *kc) {
+    count_kernel(kc);
+    const int nz8 = D.nz >> 3;
+    const int kg = blockIdx.x * blockDim.x + threadIdx.x;
+    const int j = blockIdx.y * blockDim.y + threadIdx.y;
+    const int i = blockIdx.z;
+    if (kg >= nz8 || j >= D.ny) return;
+    const int k0 = kg << 3;
+    const int sj = D.nz, si = D.ny * D.nz;
+    const int c0 = (i * D.ny + j) * D.nz + k0;
+    const bool hip = i + 1 < D.nx, him = i > 0, hjp = j + 1 < D.ny, hjm = j > 0;
+    const bool hkp = k0 + 8 < D.nz, hkm = k0 > 0;
+    const int par = 1 - phase;
+    const int b0 = (i + j + k0 + par) & 1;  // cell m is updated iff (m & 1) == b0
+
+    // cell codes: centre row, +-i rows, +-j rows, and the two k neighbours
+    const uint2 cc = load_codes8(code + c0);
+    if (skip_inactive && ((cc.x | cc.y) & 0x02020202u) == 0u) return;  // no fluid cell (code 2) in the row
+    const uint2 cip = hip ? load_codes8(code + c0 + si) : make_uint2(0u, 0u);
+    const uint2 cim = him ? load_codes8(code + c0 - si) : make_uint2(0u, 0u);
+    const uint2 cjp = hjp ? load_codes8(code + c0 + sj) : make_uint2(0u, 0u);
+    const uint2 cjm = hjm ? load_codes8(code + c0 - sj) : make_uint2(0u, 0u);
+    const uint8_t ckm = hkm ? __ldg(code + c0 - 1) : (uint8_t)0;
+    const uint8_t ckp = hkp ? __ldg(code + c0 + 8) : (uint8_t)0;
+
+    Row8 rr;
+    load_row8(r + c0, rr);
+    Row8 zc0, zip, zim, zjp, zjm;
+    float zkm = 0.0f, zkp = 0.0f;
+    if (kFromZero) {
+        zero_row8(zc0);
+    } else {
+        load_row8_rw(zin + c0, zc0);
+        if (hip) load_row8_rw(zin + c0 + si, zip); else zero_row8(zip);
+        if (him) load_row8_rw(zin + c0 - si, zim); else zero_row8(zim);
+        if (hjp) load_row8_rw(zin + c0 + sj, zjp); else zero_row8(zjp);
+        if (hjm) load_row8_rw(zin + c0 - sj, zjm); else zero_row8(zjm);
+        if (hkm) zkm = zin[c0 - 1];
+        if (hkp) zkp = zin[c0 + 8];
+        if (kProlong) {
+            const int cy = D.ny >> 1, cz = D.nz >> 1;
+            const int ci = i >> 1, cj = j >> 1, ck = k0 >> 1;
+            const int cb = (ci * cy + cj) * cz + ck;
+            add_coarse_row8(zc0, zc + cb);
+            if (hip) add_coarse_row8(zip, zc + (((i + 1) >> 1) * cy + cj) * cz + ck);
+            if (him) add_coarse_row8(zim, zc + (((i - 1) >> 1) * cy + cj) * cz + ck);
+            if (hjp) add_coarse_row8(zjp, zc + (ci * cy + ((j + 1) >> 1)) * cz + ck);
+            if (hjm) add_coarse_row8(zjm, zc + (ci * cy + ((j - 1) >> 1)) * cz + ck);
+            if (hkm) zkm = __fadd_rn(zkm, __ldg(zc + cb - 1));
+            if (hkp) zkp = __fadd_rn(zkp, __ldg(zc + cb + 4));
+        }
+    }
+
+    float out[8];
+#pragma unroll
+    for (int m = 0; m < 8; m++) {
+        const uint8_t cm = code_at(cc, m);
+        out[m] = cm == kCodeFluid ? zc0.v[m] : 0.0f;
+        if ((m & 1) != b0) continue;
+        float zn = 0.0f;
+        if (cm == kCodeFluid) {
+            const float xc = zc0.v[m];
+            int d = 0;
+            float tp, tm, ret = 0.0f;
+            uint8_t cn;
+            // axis i
+            tp = 0.0f; tm = 0.0f;
+            cn = code_at(cip, m); if (cn != kCodeSolid) { tp = __fsub_rn(cn == kCodeAir ? 0.0f : zip.v[m], xc); d++; }
+            cn = code_at(cim, m); if (cn != kCodeSolid) { tm = __fsub_rn(cn == kCodeAir ? 0.0f : zim.v[m], xc); d++; }
+            ret = __fadd_rn(ret, __fadd_rn(tp, tm));
+            // axis j
+            tp = 0.0f; tm = 0.0f;
+            cn = code_at(cjp, m); if (cn != kCodeSolid) { tp = __fsub_rn(cn == kCodeAir ? 0.0f : zjp.v[m], xc); d++; }
+            cn = code_at(cjm, m); if (cn != kCodeSolid) { tm = __fsub_rn(cn == kCodeAir ? 0.0f : zjm.v[m], xc); d++; }
+            ret = __fadd_rn(ret, __fadd_rn(tp, tm));
+            // axis k
+            tp = 0.0f; tm = 0.0f;
+            cn = m < 7 ? code_at(cc, m + 1) : ckp;
+            if (cn != kCodeSolid) { tp = __fsub_rn(cn == kCodeAir ? 0.0f : (m < 7 ? zc0.v[m + 1] : zkp), xc); d++; }
+            cn = m > 0 ? code_at(cc, m - 1) : ckm;
+            if (cn != kCodeSolid) { tm = __fsub_rn(cn == kCodeAir ? 0.0f : (m > 0 ? zc0.v[m - 1] : zkm), xc); d++; }
+            ret = __fadd_rn(ret, __fadd_rn(tp, tm));
+            if (d != 0) {
+                if (kFromZero)
+                    zn = __fdiv_rn(rr.v[m], (float)d);  // 0 + (r + L 0) / d, L 0 = 0
+                else
+                    zn = __fadd_rn(xc, __fdiv_rn(__fadd_rn(rr.v[m], ret), (float)d));
+            }
+        }
+        out[m] = zn;
+    }
+    float4 *o = reinterpret_cast<float4 *>(zout + c0);
+    o[0] = make_float4(out[0], out[1], out[2], out[3]);
+    o[1] = make_float4(out[4], out[5], out[6], out[7]);
+}
+
+}  // namespace flub

@@ -1,0 +1,234 @@
+// The coarse tail of the V-cycle in one thread block.
+//
+// Below a few thousand cells a level is pure launch latency: the reference
+// schedule runs 6 << l red-black iterations per side at level l (384
+// half-sweeps at 16^3 for a 256^3 grid).  This kernel keeps z, r and the cell
+// codes of every tail level in shared memory and runs the whole sub-V-cycle
+// (multigrid/mgpcg.py:296-349 from level lt down to the bottom and back) with
+// __syncthreads between half-sweeps.  Arithmetic is the same as the global
+// kernels, cell by cell, so the result is bit-identical.
+#pragma once
+
+#include "mg_kernels.cuh"
+
+namespace flub {
+
+constexpr int kTailThreads = 1024;
+constexpr int kTailMaxLevels = 8;
+constexpr int kTailMaxCells = 4096;  // the first tail level has at most this many cells
+
+struct TailLevel {
+    Dims D;
+    const uint8_t *code;  // global cell codes of this level
+    int abs_level;        // level index in the full hierarchy (sets 6 << l)
+    int off_z, off_r, off_c;  // byte offsets in shared memory
+};
+
+struct TailParams {
+    int nt;
+    TailLevel lv[kTailMaxLevels];
+    const float *r_top;  // restricted residual of the first tail level (global)
+    float *z_top;        // its correction (global)
+};
+
+// ---------------------------------------------------------------- lean smoothing
+// Each thread owns up to kTailPairs pairs of k-adjacent cells (one of each
+// colour) of the level being smoothed.  On entering a level it caches, per
+// cell, its shared-memory index, a neighbour mask and its r, so the
+// half-sweeps themselves are a handful of shared loads per update.
+// mask bits: 0-5 neighbour (+i, -i, +j, -j, +k, -k) in the domain and not
+// solid; 6-11 that neighbour is air; 12 the cell is fluid.
+constexpr int kTailPairs = (kTailMaxCells / 2 + kTailThreads - 1) / kTailThreads;
+
+struct TailCache {
+    int idx[kTailPairs];      // index of the pair's even-k cell, -1 if unused
+    uint32_t msk[kTailPairs]; // low 16 bits: even cell, high 16 bits: odd cell
+    float r0[kTailPairs], r1[kTailPairs];
+    int upd0;                 // bit q: in phase 0 the odd-k cell of pair q is updated
+};
+
+__device__ __forceinline__ uint32_t cell_mask(const uint8_t *code, const Dims D, int i, int j, int k, int c) {
+    const int si = D.ny * D.nz, sj = D.nz;
+    uint32_t m = 0;
+    auto nb = [&](bool inside, int off, int bit) {
+        if (!inside) return;
+        const uint8_t cn = code[c + off];
+        if (cn != kCodeSolid) m |= 1u << bit;
+        if (cn == kCodeAir) m |= 1u << (bit + 6);
+    };
+    nb(i + 1 < D.nx, si, 0);
+    nb(i > 0, -si, 1);
+    nb(j + 1 < D.ny, sj, 2);
+    nb(j > 0, -sj, 3);
+    nb(k + 1 < D.nz, 1, 4);
+    nb(k > 0, -1, 5);
+    if (code[c] == kCodeFluid) m |= 1u << 12;
+    return m;
+}
+
+__device__ __forceinline__ void tail_cache(TailCache &tc, const uint8_t *code, const float *r, const Dims D) {
+    const int hz = D.nz >> 1, npairs = D.nx * D.ny * hz;
+    tc.upd0 = 0;
+#pragma unroll
+    for (int q = 0; q < kTailPairs; q++) {
+        const int t = threadIdx.x + q * kTailThreads;
+        tc.idx[q] = -1;
+        tc.msk[q] = 0;
+        tc.r0[q] = tc.r1[q] = 0.0f;
+        if (t < npairs) {
+            const int kk = t % hz, qq = t / hz;
+            const int j = qq % D.ny, i = qq / D.ny;
+            const int c = (i * D.ny + j) * D.nz + 2 * kk;
+            tc.idx[q] = c;
+            tc.msk[q] = cell_mask(code, D, i, j, 2 * kk, c) | (cell_mask(code, D, i, j, 2 * kk + 1, c + 1) << 16);
+            tc.r0[q] = r[c];
+            tc.r1[q] = r[c + 1];
+            // phase 0 updates (i+j+k) odd cells: the odd-k cell iff i+j is even
+            if (((i + j) & 1) == 0) tc.upd0 |= 1 << q;
+        }
+    }
+}
+
+// z update of one cell with the mask m (same operation order as lap_at).
+__device__ __forceinline__ float tail_update(const float *z, int c, uint32_t m, float rc, int si, int sj,
+                                             bool from_zero) {
+    if (!(m & (1u << 12))) return 0.0f;
+    const int d = __popc(m & 63u);
+    if (d == 0) return 0.0f;
+    if (from_zero) return __fdiv_rn(rc, (float)d);
+    const float xc = z[c];
+    float tp, tm, ret = 0.0f;
+    tp = (m & 1u) ? __fsub_rn((m & 64u) ? 0.0f : z[c + si], xc) : 0.0f;
+    tm = (m & 2u) ? __fsub_rn((m & 128u) ? 0.0f : z[c - si], xc) : 0.0f;
+    ret = __fadd_rn(ret, __fadd_rn(tp, tm));
+    tp = (m & 4u) ? __fsub_rn((m & 256u) ? 0.0f : z[c + sj], xc) : 0.0f;
+    tm = (m & 8u) ? __fsub_rn((m & 512u) ? 0.0f : z[c - sj], xc) : 0.0f;
+    ret = __fadd_rn(ret, __fadd_rn(tp, tm));
+    tp = (m & 16u) ? __fsub_rn((m & 1024u) ? 0.0f : z[c + 1], xc) : 0.0f;
+    tm = (m & 32u) ? __fsub_rn((m & 2048u) ? 0.0f : z[c - 1], xc) : 0.0f;
+    ret = __fadd_rn(ret, __fadd_rn(tp, tm));
+    return __fadd_rn(xc, __fdiv_rn(__fadd_rn(rc, ret), (float)d));
+}
+
+__device__ __forceinline__ void tail_half_lean(float *z, const TailCache &tc, const Dims D, int phase,
+                                               bool from_zero) {
+    const int si = D.ny * D.nz, sj = D.nz;
+#pragma unroll
+    for (int q = 0; q < kTailPairs; q++) {
+        const int c = tc.idx[q];
+        if (c < 0) continue;
+        const bool odd = (((tc.upd0 >> q) & 1) != 0) == (phase == 0);
+        const uint32_t m = odd ? (tc.msk[q] >> 16) : (tc.msk[q] & 0xffffu);
+        const int cu = c + (odd ? 1 : 0);
+        const float zn = tail_update(z, cu, m, odd ? tc.r1[q] : tc.r0[q], si, sj, from_zero);
+        z[cu] = zn;
+        if (from_zero) z[odd ? c : c + 1] = 0.0f;
+    }
+    __syncthreads();
+}
+
+__device__ __forceinline__ void tail_restrict(const float *rf, const float *zf, const uint8_t *cf, float *rc,
+                                              const uint8_t *cc, const Dims C) {
+    const Dims F{2 * C.nx, 2 * C.ny, 2 * C.nz};
+    const int n = C.nx * C.ny * C.nz;
+    for (int q = threadIdx.x; q < n; q += blockDim.x) {
+        if (cc[q] != kCodeFluid) {
+            rc[q] = 0.0f;
+            continue;
+        }
+        const int K = q % C.nz, J = (q / C.nz) % C.ny, I = q / (C.nz * C.ny);
+        float s = 0.0f;
+        bool first = true;
+#pragma unroll
+        for (int ii = 0; ii < 2; ii++)
+#pragma unroll
+            for (int jj = 0; jj < 2; jj++)
+#pragma unroll
+                for (int kk = 0; kk < 2; kk++) {
+                    const int i = 2 * I + ii, j = 2 * J + jj, k = 2 * K + kk;
+                    const int64_t c = ((int64_t)i * F.ny + j) * F.nz + k;
+                    float lz = 0.0f;
+                    if (cf[c] == kCodeFluid) {
+                        int d;
+                        lz = lap_at(zf, cf, i, j, k, F, c, zf[c], d);
+                    }
+                    const float v = __fadd_rn(rf[c], lz);
+                    s = first ? v : __fadd_rn(s, v);
+                    first = false;
+                }
+        rc[q] = s;
+    }
+    __syncthreads();
+}
+
+__device__ __forceinline__ void tail_prolong(float *zf, const float *zc, const Dims F) {
+    const int n = F.nx * F.ny * F.nz;
+    const int cy = F.ny >> 1, cz = F.nz >> 1;
+    for (int c = threadIdx.x; c < n; c += blockDim.x) {
+        const int k = c % F.nz, j = (c / F.nz) % F.ny, i = c / (F.nz * F.ny);
+        zf[c] = __fadd_rn(zf[c], zc[((i >> 1) * cy + (j >> 1)) * cz + (k >> 1)]);
+    }
+    __syncthreads();
+}
+
+__global__ void __launch_bounds__(kTailThreads) k_tail_vcycle(const TailParams P, unsigned long long *kc) {
+    extern __shared__ __align__(16) unsigned char tail_smem[];
+    count_kernel(kc);
+    auto Z = [&](int t) { return reinterpret_cast<float *>(tail_smem + P.lv[t].off_z); };
+    auto R = [&](int t) { return reinterpret_cast<float *>(tail_smem + P.lv[t].off_r); };
+    auto C = [&](int t) { return reinterpret_cast<uint8_t *>(tail_smem + P.lv[t].off_c); };
+    for (int t = 0; t < P.nt; t++) {
+        const int n = P.lv[t].D.nx * P.lv[t].D.ny * P.lv[t].D.nz;
+        uint8_t *c = C(t);
+        for (int q = threadIdx.x; q < n; q += blockDim.x) c[q] = P.lv[t].code[q];
+    }
+    {
+        const Dims D = P.lv[0].D;
+        const int n = D.nx * D.ny * D.nz;
+        float *r = R(0);
+        for (int q = threadIdx.x; q < n; q += blockDim.x) r[q] = P.r_top[q];
+    }
+    __syncthreads();
+    const int nb = P.nt - 1;
+    TailCache tc;
+    for (int t = 0; t < nb; t++) {
+        const Dims D = P.lv[t].D;
+        tail_cache(tc, C(t), R(t), D);
+        const int iters = 6 << P.lv[t].abs_level;
+        for (int it = 0; it < iters; it++) {
+            tail_half_lean(Z(t), tc, D, 0, it == 0);
+            tail_half_lean(Z(t), tc, D, 1, false);
+        }
+        tail_restrict(R(t), Z(t), C(t), R(t + 1), C(t + 1), P.lv[t + 1].D);
+    }
+    {
+        const Dims D = P.lv[nb].D;
+        tail_cache(tc, C(nb), R(nb), D);
+        for (int it = 0; it < 3; it++) {
+            tail_half_lean(Z(nb), tc, D, 0, it == 0);
+            tail_half_lean(Z(nb), tc, D, 1, false);
+        }
+        for (int it = 0; it < 3; it++) {
+            tail_half_lean(Z(nb), tc, D, 1, false);
+            tail_half_lean(Z(nb), tc, D, 0, false);
+        }
+    }
+    for (int t = nb - 1; t >= 0; t--) {
+        const Dims D = P.lv[t].D;
+        tail_prolong(Z(t), Z(t + 1), D);
+        tail_cache(tc, C(t), R(t), D);
+        const int iters = 6 << P.lv[t].abs_level;
+        for (int it = 0; it < iters; it++) {
+            tail_half_lean(Z(t), tc, D, 1, false);
+            tail_half_lean(Z(t), tc, D, 0, false);
+        }
+    }
+    {
+        const Dims D = P.lv[0].D;
+        const int n = D.nx * D.ny * D.nz;
+        const float *z = Z(0);
+        for (int q = threadIdx.x; q < n; q += blockDim.x) P.z_top[q] = z[q];
+    }
+}
+
+}  // namespace flub

@@ -207,7 +207,7 @@ int flub_mg_smooth(flub_mg *mg, int level, int phase, void *stream);
  * loop, or a real-time caller that cannot pay for cudaMalloc's implicit
  * synchronisation.  Computes z = M r exactly as flub_mg_set_tags(tag) followed
  * by flub_mg_apply_preconditioner(r, z) would (same kernels, same results),
- * but keeps the level hierarchy in a 1 MiB array compiled into the library
+ * but keeps the level hierarchy in a 2 MiB array compiled into the library
  * (resident on every device that loads it, until the process exits) and
  * allocates nothing.  Limits: nx * ny * nz <= FLUB_NOALLOC_MAX_CELLS, plus
  * the shape rules of flub_mg_create; larger grids are rejected with

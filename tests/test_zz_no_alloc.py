@@ -1,7 +1,7 @@
 """The allocation-free V-cycle (flub_vcycle_noalloc), for callers that cannot
 allocate device memory themselves -- e.g. a plugin inside a host application
 that owns all device memory, or a real-time caller that cannot afford
-cudaMalloc.  It keeps its level hierarchy in a fixed 1 MiB device array inside
+cudaMalloc.  It keeps its level hierarchy in a fixed 2 MiB device array inside
 the library (grids up to 64^3 cells).
 
 Called through the C ABI and compared with the regular path
