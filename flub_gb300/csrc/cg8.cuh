@@ -1,0 +1,251 @@
+// CG vector kernels over groups of 8 consecutive cells (multigrid/mgpcg.py:
+// 207-232 and the array_inner calls of :391-451), float4 rows, FP64 partial
+// sums, 32-bit indices.
+//
+// Skipping: on a group without a fluid cell the CG vectors hold values that
+// cannot change the result -- L p = Ap = 0, z = 0, p = 0 (p starts at 0 and is
+// z + beta p) -- so such a group is not read at all.  The one vector that the
+// caller could leave non-zero off the fluid is r (init without mask_interior);
+// the r.r kernels therefore skip only when the solver state says r was
+// masked (MgState::skip_r).
+#pragma once
+
+#include "mg_kernels.cuh"
+#include "smooth8.cuh"
+
+namespace flub {
+
+__device__ __forceinline__ bool group_has_fluid(uint2 c) { return ((c.x | c.y) & 0x02020202u) != 0u; }
+
+__device__ __forceinline__ void store_row8(float *p, const float v[8]) {
+    float4 *o = reinterpret_cast<float4 *>(p);
+    o[0] = make_float4(v[0], v[1], v[2], v[3]);
+    o[1] = make_float4(v[4], v[5], v[6], v[7]);
+}
+
+// L x for the 8 cells of the row starting at c0 (group g), same operation
+// order as lap_at.  Non-fluid cells get 0.
+__device__ __forceinline__ void lap_row8(const float *__restrict__ x, const uint8_t *__restrict__ code, const Dims D,
+                                         int g, uint2 cc, float out[8], Row8 &xc) {
+    const int nz8 = D.nz >> 3;
+    const int kg = g % nz8, q = g / nz8;
+    const int j = q % D.ny, i = q / D.ny;
+    const int k0 = kg << 3;
+    const int sj = D.nz, si = D.ny * D.nz;
+    const int c0 = g << 3;
+    const bool hip = i + 1 < D.nx, him = i > 0, hjp = j + 1 < D.ny, hjm = j > 0;
+    const bool hkp = k0 + 8 < D.nz, hkm = k0 > 0;
+    const uint2 z2 = make_uint2(0u, 0u);
+    const uint2 cip = hip ? load_codes8(code + c0 + si) : z2;
+    const uint2 cim = him ? load_codes8(code + c0 - si) : z2;
+    const uint2 cjp = hjp ? load_codes8(code + c0 + sj) : z2;
+    const uint2 cjm = hjm ? load_codes8(code + c0 - sj) : z2;
+    const uint8_t ckm = hkm ? __ldg(code + c0 - 1) : (uint8_t)0;
+    const uint8_t ckp = hkp ? __ldg(code + c0 + 8) : (uint8_t)0;
+    Row8 xip, xim, xjp, xjm;
+    load_row8(x + c0, xc);
+    if (hip) load_row8(x + c0 + si, xip); else zero_row8(xip);
+    if (him) load_row8(x + c0 - si, xim); else zero_row8(xim);
+    if (hjp) load_row8(x + c0 + sj, xjp); else zero_row8(xjp);
+    if (hjm) load_row8(x + c0 - sj, xjm); else zero_row8(xjm);
+    const float xkm = hkm ? __ldg(x + c0 - 1) : 0.0f;
+    const float xkp = hkp ? __ldg(x + c0 + 8) : 0.0f;
+#pragma unroll
+    for (int m = 0; m < 8; m++) {
+        out[m] = 0.0f;
+        if (code_at(cc, m) != kCodeFluid) continue;
+        const float c = xc.v[m];
+        float tp, tm, ret = 0.0f;
+        uint8_t cn;
+        tp = 0.0f; tm = 0.0f;
+        cn = code_at(cip, m); if (cn != kCodeSolid) tp = __fsub_rn(cn == kCodeAir ? 0.0f : xip.v[m], c);
+        cn = code_at(cim, m); if (cn != kCodeSolid) tm = __fsub_rn(cn == kCodeAir ? 0.0f : xim.v[m], c);
+        ret = __fadd_rn(ret, __fadd_rn(tp, tm));
+        tp = 0.0f; tm = 0.0f;
+        cn = code_at(cjp, m); if (cn != kCodeSolid) tp = __fsub_rn(cn == kCodeAir ? 0.0f : xjp.v[m], c);
+        cn = code_at(cjm, m); if (cn != kCodeSolid) tm = __fsub_rn(cn == kCodeAir ? 0.0f : xjm.v[m], c);
+        ret = __fadd_rn(ret, __fadd_rn(tp, tm));
+        tp = 0.0f; tm = 0.0f;
+        cn = m < 7 ? code_at(cc, m + 1) : ckp;
+        if (cn != kCodeSolid) tp = __fsub_rn(cn == kCodeAir ? 0.0f : (m < 7 ? xc.v[m + 1] : xkp), c);
+        cn = m > 0 ? code_at(cc, m - 1) : ckm;
+        if (cn != kCodeSolid) tm = __fsub_rn(cn == kCodeAir ? 0.0f : (m > 0 ? xc.v[m - 1] : xkm), c);
+        ret = __fadd_rn(ret, __fadd_rn(tp, tm));
+        out[m] = ret;
+    }
+}
+
+#define FLUB_GROUP_LOOP(g, ng) for (int g = blockIdx.x * blockDim.x + threadIdx.x; g < (ng); g += gridDim.x * blockDim.x)
+
+// Ap = L p, p.Ap -> alpha (mgpcg.py:410-419); guarded like k_matvec_pap.
+__global__ void __launch_bounds__(kRedThreads) k8_matvec_pap(MgState *st, const float *__restrict__ p,
+                                                             float *__restrict__ Ap, const uint8_t *__restrict__ code,
+                                                             Dims D, double *partials, unsigned long long *kc) {
+    __shared__ double red[32];
+    count_kernel(kc);
+    if (st->it >= st->max_iters || st->converged || st->status) return;
+    const int ng = (int)(D.n() >> 3);
+    double s = 0.0;
+    FLUB_GROUP_LOOP(g, ng) {
+        const uint2 cc = load_codes8(code + (g << 3));
+        if (!group_has_fluid(cc)) continue;  // Ap = 0 there already
+        float a[8];
+        Row8 pc;
+        lap_row8(p, code, D, g, cc, a, pc);
+        store_row8(Ap + (g << 3), a);
+#pragma unroll
+        for (int m = 0; m < 8; m++) s = fma((double)pc.v[m], (double)a[m], s);
+    }
+    double total;
+    if (finish_partials(s, partials, &st->ticket, red, &total) && threadIdx.x == 0) {
+        st->pap = total;
+        const double alpha = st->zr_old / (total + st->eps);
+        st->alpha = alpha;
+        if (!isfinite(alpha)) st->status = FLUB_ERR_BREAKDOWN;
+    }
+}
+
+// r -= alpha Ap, r.r, convergence test and loop condition (mgpcg.py:421-446).
+template <bool kUpdate>
+__global__ void __launch_bounds__(kRedThreads) k8_update_r_rr(MgState *st, float *__restrict__ r,
+                                                              const float *__restrict__ Ap,
+                                                              const uint8_t *__restrict__ code, int64_t n,
+                                                              double *partials, double *hist,
+                                                              cudaGraphConditionalHandle h, int set_cond,
+                                                              unsigned long long *kc) {
+    __shared__ double red[32];
+    count_kernel(kc);
+    if (st->it >= st->max_iters || st->converged || st->status) {
+        if ((blockIdx.x | threadIdx.x) == 0) publish_cond(st, 0, h, set_cond);
+        return;
+    }
+    const float a = (float)st->alpha;
+    const int skip = st->skip_r;
+    const int ng = (int)(n >> 3);
+    double s = 0.0;
+    FLUB_GROUP_LOOP(g, ng) {
+        if (skip && !group_has_fluid(load_codes8(code + (g << 3)))) continue;
+        Row8 rv;
+        load_row8_rw(r + (g << 3), rv);
+        if (kUpdate) {
+            Row8 av;
+            load_row8(Ap + (g << 3), av);
+#pragma unroll
+            for (int m = 0; m < 8; m++) rv.v[m] = __fmaf_rn(-a, av.v[m], rv.v[m]);
+            store_row8(r + (g << 3), rv.v);
+        }
+#pragma unroll
+        for (int m = 0; m < 8; m++) s = fma((double)rv.v[m], (double)rv.v[m], s);
+    }
+    double total;
+    if (finish_partials(s, partials, &st->ticket, red, &total) && threadIdx.x == 0) {
+        st->rtr = total;
+        if (st->it < kHistory) hist[st->it] = total;
+        if (!isfinite(total)) st->status = FLUB_ERR_BREAKDOWN;
+        const int conv = total < st->tol;
+        st->converged = conv;
+        publish_cond(st, (!conv && st->status == FLUB_OK) ? 1 : 0, h, set_cond);
+    }
+}
+
+// rTr0 and the tolerance (mgpcg.py:391-393).
+__global__ void __launch_bounds__(kRedThreads) k8_dot_rr0(MgState *st, const float *__restrict__ r,
+                                                          const uint8_t *__restrict__ code, int64_t n,
+                                                          double *partials, unsigned long long *kc) {
+    __shared__ double red[32];
+    count_kernel(kc);
+    const int skip = st->skip_r;
+    const int ng = (int)(n >> 3);
+    double s = 0.0;
+    FLUB_GROUP_LOOP(g, ng) {
+        if (skip && !group_has_fluid(load_codes8(code + (g << 3)))) continue;
+        Row8 rv;
+        load_row8(r + (g << 3), rv);
+#pragma unroll
+        for (int m = 0; m < 8; m++) s = fma((double)rv.v[m], (double)rv.v[m], s);
+    }
+    double total;
+    if (finish_partials(s, partials, &st->ticket, red, &total) && threadIdx.x == 0) {
+        st->rtr0 = total;
+        st->rtr = total;
+        const double rel = total * st->rel_tol;
+        st->tol = st->abs_tol > rel ? st->abs_tol : rel;
+    }
+}
+
+// z.r; kInit: old_zTr = z.r and p = z (mgpcg.py:396-401), else beta (:451-455).
+template <bool kInit>
+__global__ void __launch_bounds__(kRedThreads) k8_dot_zr(MgState *st, const float *__restrict__ z,
+                                                         const float *__restrict__ r, float *__restrict__ p,
+                                                         const uint8_t *__restrict__ code, int64_t n,
+                                                         double *partials, unsigned long long *kc) {
+    __shared__ double red[32];
+    count_kernel(kc);
+    const int ng = (int)(n >> 3);
+    double s = 0.0;
+    FLUB_GROUP_LOOP(g, ng) {
+        if (!group_has_fluid(load_codes8(code + (g << 3)))) continue;  // z = 0 (and p = 0) there
+        Row8 zv, rv;
+        load_row8(z + (g << 3), zv);
+        load_row8(r + (g << 3), rv);
+#pragma unroll
+        for (int m = 0; m < 8; m++) s = fma((double)zv.v[m], (double)rv.v[m], s);
+        if (kInit) store_row8(p + (g << 3), zv.v);
+    }
+    double total;
+    if (finish_partials(s, partials, &st->ticket, red, &total) && threadIdx.x == 0) {
+        if (kInit) {
+            st->zr_old = total;
+        } else {
+            const double beta = total / (st->zr_old + st->eps);
+            st->beta = beta;
+            st->zr_old = total;
+            if (!isfinite(beta)) st->status = FLUB_ERR_BREAKDOWN;
+        }
+    }
+}
+
+// x += alpha p; p = z + beta p; it += 1 (mgpcg.py:457-461).
+__global__ void __launch_bounds__(256) k8_update_xp(MgState *st, float *__restrict__ x, float *__restrict__ p,
+                                                    const float *__restrict__ z, const uint8_t *__restrict__ code,
+                                                    int64_t n, unsigned long long *kc) {
+    count_kernel(kc);
+    const float a = (float)st->alpha, b = (float)st->beta;
+    const int ng = (int)(n >> 3);
+    FLUB_GROUP_LOOP(g, ng) {
+        if (!group_has_fluid(load_codes8(code + (g << 3)))) continue;  // p = z = 0 there
+        Row8 xv, pv, zv;
+        load_row8_rw(x + (g << 3), xv);
+        load_row8_rw(p + (g << 3), pv);
+        load_row8(z + (g << 3), zv);
+#pragma unroll
+        for (int m = 0; m < 8; m++) {
+            xv.v[m] = __fmaf_rn(a, pv.v[m], xv.v[m]);
+            pv.v[m] = __fmaf_rn(b, pv.v[m], zv.v[m]);
+        }
+        store_row8(x + (g << 3), xv.v);
+        store_row8(p + (g << 3), pv.v);
+    }
+    if ((blockIdx.x | threadIdx.x) == 0) st->it += 1;
+}
+
+// On convergence: x += alpha p (mgpcg.py:444-446).
+__global__ void __launch_bounds__(256) k8_solve_end(MgState *st, float *__restrict__ x, const float *__restrict__ p,
+                                                    const uint8_t *__restrict__ code, int64_t n,
+                                                    unsigned long long *kc) {
+    count_kernel(kc);
+    if (!st->converged) return;
+    const float a = (float)st->alpha;
+    const int ng = (int)(n >> 3);
+    FLUB_GROUP_LOOP(g, ng) {
+        if (!group_has_fluid(load_codes8(code + (g << 3)))) continue;
+        Row8 xv, pv;
+        load_row8_rw(x + (g << 3), xv);
+        load_row8(p + (g << 3), pv);
+#pragma unroll
+        for (int m = 0; m < 8; m++) xv.v[m] = __fmaf_rn(a, pv.v[m], xv.v[m]);
+        store_row8(x + (g << 3), xv.v);
+    }
+}
+
+}  // namespace flub

@@ -24,7 +24,7 @@ struct MgState {
     unsigned long long kernels;  // solver kernels executed inside graphs
     int it, max_iters, converged, status, cond, use_x0;
     unsigned int ticket;
-    int pad;
+    int skip_r;  // r is 0 off the fluid (masked), so r.r may skip groups without fluid
 };
 
 struct Dims {
@@ -260,7 +260,9 @@ __global__ void __launch_bounds__(256) k_prolong(float *zout, const float *zin, 
 
 // ---------------------------------------------------------------- CG kernels
 
-__global__ void k_solve_begin(MgState *st, int max_iters, double eps, double abs_tol, double rel_tol, int use_x0) {
+__global__ void k_solve_begin(MgState *st, int max_iters, double eps, double abs_tol, double rel_tol, int use_x0,
+                              int skip_r) {
+    st->skip_r = skip_r;
     st->max_iters = max_iters;
     st->eps = eps;
     st->abs_tol = abs_tol;

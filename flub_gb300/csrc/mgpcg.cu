@@ -17,6 +17,7 @@
 #include <vector>
 
 #include "mg_kernels.cuh"
+#include "cg8.cuh"
 #include "smooth8.cuh"
 #include "tail.cuh"
 
@@ -64,7 +65,8 @@ struct flub_mg {
     int graph_nodes[3];
     cudaStream_t cap_stream, cap_stream2;
     bool host_loop;
-    bool skip_ok;  // internal z buffers keep z = 0 off the fluid (see k_smooth8)
+    bool skip_ok;   // internal z buffers keep z = 0 off the fluid (see k_smooth8)
+    bool r_masked;  // r is 0 off the fluid (mask_interior since the last init)
     int tail_start;  // first level run by the one-block tail kernel (== levels: none)
     size_t tail_smem;
 };
@@ -295,27 +297,49 @@ static int enqueue_mean_removal(flub_mg *mg, const LaunchCtx &c, int guard) {
 static int enqueue_prologue(flub_mg *mg, const LaunchCtx &c, int smoother) {
     const unsigned b = red_blocks(mg->n);
     const Level &L0 = mg->lv[0];
+    const bool v8 = (L0.D.nz % 8) == 0;  // group-of-8 kernels; the scalar ones otherwise
+    const unsigned bg = red_blocks(mg->n / 8 + 1);
     if (smoother == FLUB_SMOOTHER_FRACTION) FLUB_TRY(enqueue_mean_removal(mg, c, 0));
-    FLUB_TRY(launch_pdl(k_dot_rr0, dim3(b), dim3(kRedThreads), 0, c.s, mg->st, L0.r, mg->n, mg->partials, c.kc));
+    if (v8)
+        FLUB_TRY(launch_pdl(k8_dot_rr0, dim3(bg), dim3(kRedThreads), 0, c.s, mg->st, L0.r, L0.code, mg->n,
+                            mg->partials, c.kc));
+    else
+        FLUB_TRY(launch_pdl(k_dot_rr0, dim3(b), dim3(kRedThreads), 0, c.s, mg->st, L0.r, mg->n, mg->partials, c.kc));
     FLUB_TRY(launch_pdl(k_residual_x0, dim3(blocks_for(mg->n, 256)), dim3(256), 0, c.s, mg->st, L0.r, mg->x, L0.code,
                         L0.D, c.kc));
     if (smoother == FLUB_SMOOTHER_FRACTION) FLUB_TRY(enqueue_mean_removal(mg, c, 2));
     FLUB_TRY(enqueue_vcycle(mg, c, L0.r, L0.z, true));
-    FLUB_TRY(launch_pdl(k_dot_zr_init, dim3(b), dim3(kRedThreads), 0, c.s, mg->st, L0.z, L0.r, mg->p, mg->n, mg->partials, c.kc));
-    return FLUB_OK;
+    if (v8)
+        return launch_pdl(k8_dot_zr<true>, dim3(bg), dim3(kRedThreads), 0, c.s, mg->st, L0.z, L0.r, mg->p, L0.code,
+                          mg->n, mg->partials, c.kc);
+    return launch_pdl(k_dot_zr_init, dim3(b), dim3(kRedThreads), 0, c.s, mg->st, L0.z, L0.r, mg->p, mg->n,
+                      mg->partials, c.kc);
 }
 
 // Ap, alpha, r update, r.r, convergence test, loop condition.
 static int enqueue_first_half(flub_mg *mg, const LaunchCtx &c, int smoother) {
     const unsigned b = red_blocks(mg->n);
     const Level &L0 = mg->lv[0];
-    FLUB_TRY(launch_pdl(k_matvec_pap, dim3(b), dim3(kRedThreads), 0, c.s, mg->st, mg->p, mg->Ap, L0.code, L0.D, mg->partials, c.kc));
+    const bool v8 = (L0.D.nz % 8) == 0;
+    const unsigned bg = red_blocks(mg->n / 8 + 1);
+    if (v8)
+        FLUB_TRY(launch_pdl(k8_matvec_pap, dim3(bg), dim3(kRedThreads), 0, c.s, mg->st, mg->p, mg->Ap, L0.code, L0.D,
+                            mg->partials, c.kc));
+    else
+        FLUB_TRY(launch_pdl(k_matvec_pap, dim3(b), dim3(kRedThreads), 0, c.s, mg->st, mg->p, mg->Ap, L0.code, L0.D,
+                            mg->partials, c.kc));
     if (smoother == FLUB_SMOOTHER_FRACTION) {
         FLUB_TRY(launch_pdl(k_update_r, dim3(b), dim3(kRedThreads), 0, c.s, mg->st, L0.r, mg->Ap, mg->n, c.kc));
         FLUB_TRY(enqueue_mean_removal(mg, c, 1));
+        if (v8)
+            return launch_pdl(k8_update_r_rr<false>, dim3(bg), dim3(kRedThreads), 0, c.s, mg->st, L0.r, mg->Ap,
+                              L0.code, mg->n, mg->partials, mg->hist, c.h, c.set_cond, c.kc);
         return launch_pdl(k_update_r_rr<false>, dim3(b), dim3(kRedThreads), 0, c.s, mg->st, L0.r, mg->Ap, mg->n,
                           mg->partials, mg->hist, c.h, c.set_cond, c.kc);
     }
+    if (v8)
+        return launch_pdl(k8_update_r_rr<true>, dim3(bg), dim3(kRedThreads), 0, c.s, mg->st, L0.r, mg->Ap, L0.code,
+                          mg->n, mg->partials, mg->hist, c.h, c.set_cond, c.kc);
     return launch_pdl(k_update_r_rr<true>, dim3(b), dim3(kRedThreads), 0, c.s, mg->st, L0.r, mg->Ap, mg->n,
                       mg->partials, mg->hist, c.h, c.set_cond, c.kc);
 }
@@ -325,12 +349,24 @@ static int enqueue_second_half(flub_mg *mg, const LaunchCtx &c) {
     const unsigned b = red_blocks(mg->n);
     const Level &L0 = mg->lv[0];
     FLUB_TRY(enqueue_vcycle(mg, c, L0.r, L0.z, true));
-    FLUB_TRY(launch_pdl(k_dot_zr_beta, dim3(b), dim3(kRedThreads), 0, c.s, mg->st, L0.z, L0.r, mg->n, mg->partials, c.kc));
+    if ((L0.D.nz % 8) == 0) {
+        const unsigned bg = red_blocks(mg->n / 8 + 1);
+        FLUB_TRY(launch_pdl(k8_dot_zr<false>, dim3(bg), dim3(kRedThreads), 0, c.s, mg->st, L0.z, L0.r,
+                            (float *)nullptr, L0.code, mg->n, mg->partials, c.kc));
+        return launch_pdl(k8_update_xp, dim3(blocks_for(mg->n / 8, 256)), dim3(256), 0, c.s, mg->st, mg->x, mg->p,
+                          L0.z, L0.code, mg->n, c.kc);
+    }
+    FLUB_TRY(launch_pdl(k_dot_zr_beta, dim3(b), dim3(kRedThreads), 0, c.s, mg->st, L0.z, L0.r, mg->n, mg->partials,
+                        c.kc));
     return launch_pdl(k_update_xp, dim3(blocks_for(mg->n, 256)), dim3(256), 0, c.s, mg->st, mg->x, mg->p, L0.z, mg->n,
                       c.kc);
 }
 
 static int enqueue_epilogue(flub_mg *mg, const LaunchCtx &c) {
+    const Level &L0 = mg->lv[0];
+    if ((L0.D.nz % 8) == 0)
+        return launch_pdl(k8_solve_end, dim3(blocks_for(mg->n / 8, 256)), dim3(256), 0, c.s, mg->st, mg->x, mg->p,
+                          L0.code, mg->n, c.kc);
     return launch_pdl(k_solve_end, dim3(blocks_for(mg->n, 256)), dim3(256), 0, c.s, mg->st, mg->x, mg->p, mg->n,
                       c.kc);
 }
@@ -511,12 +547,15 @@ int flub_mg_set_tags(flub_mg *mg, const int32_t *tag, void *stream) {
         k_restrict_codes<<<blocks_for(C.D.n(), 256), 256, 0, s>>>(mg->lv[l].code, C.code, C.D);
         FLUB_CHECK_LAUNCH();
     }
-    // new tags: re-establish z = 0 off the fluid in every correction buffer
+    // new tags: re-establish z = p = Ap = 0 off the fluid (the kernels skip
+    // 8-cell groups without fluid and rely on it)
     for (int l = 0; l < mg->levels; l++) {
         const size_t b = sizeof(float) * (size_t)mg->lv[l].D.n();
         FLUB_CHECK_CUDA(cudaMemsetAsync(mg->lv[l].z, 0, b, s));
         FLUB_CHECK_CUDA(cudaMemsetAsync(mg->lv[l].z2, 0, b, s));
     }
+    FLUB_CHECK_CUDA(cudaMemsetAsync(mg->p, 0, sizeof(float) * (size_t)mg->n, s));
+    FLUB_CHECK_CUDA(cudaMemsetAsync(mg->Ap, 0, sizeof(float) * (size_t)mg->n, s));
     return FLUB_OK;
 }
 
@@ -525,6 +564,7 @@ int flub_mg_init(flub_mg *mg, const float *rhs, float k, void *stream) {
     k_init<<<blocks_for(mg->n, 256), 256, 0, as_stream(stream)>>>(mg->lv[0].r, rhs, k, mg->x, mg->p, mg->n);
     FLUB_CHECK_LAUNCH();
     mg->use_x0 = false;
+    mg->r_masked = false;
     return FLUB_OK;
 }
 
@@ -532,6 +572,7 @@ int flub_mg_mask_interior(flub_mg *mg, void *stream) {
     FLUB_REQUIRE(mg, "flub_mg_mask_interior: NULL handle");
     k_mask_interior<<<blocks_for(mg->n, 256), 256, 0, as_stream(stream)>>>(mg->lv[0].r, mg->lv[0].code, mg->n);
     FLUB_CHECK_LAUNCH();
+    mg->r_masked = true;
     return FLUB_OK;
 }
 
@@ -552,7 +593,10 @@ int flub_mg_solve(flub_mg *mg, int max_iters, double eps, double abs_tol, double
     }
     if (max_iters < 0) max_iters = 100000;
     cudaStream_t s = as_stream(stream);
-    k_solve_begin<<<1, 1, 0, s>>>(mg->st, max_iters, eps, abs_tol, rel_tol, mg->use_x0 ? 1 : 0);
+    // r.r may skip groups without fluid once r is 0 there: after mask_interior,
+    // or with "fraction", whose mean removal zeroes r off the fluid first
+    const int skip_r = (mg->r_masked || smoother == FLUB_SMOOTHER_FRACTION) ? 1 : 0;
+    k_solve_begin<<<1, 1, 0, s>>>(mg->st, max_iters, eps, abs_tol, rel_tol, mg->use_x0 ? 1 : 0, skip_r);
     FLUB_CHECK_LAUNCH();
     mg->use_x0 = false;
     if (mg->host_loop) {
