@@ -45,7 +45,7 @@ def parse_args():
     ap.add_argument("--cpu-baseline-steps", type=int, default=2)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
-    ap.add_argument("--profile-kernel", choices=["smooth", "restrict", "matvec"], default=None,
+    ap.add_argument("--profile-kernel", choices=["smooth", "restrict", "matvec", "solve"], default=None,
                     help="set up the 256^3 solver state and launch only this kernel 3 times (for ncu)")
     return ap.parse_args()
 
@@ -80,6 +80,9 @@ def run_profile_kernel(args):
     elif args.profile_kernel == "matvec":
         for _ in range(3):
             mg.matvec(mg.r0)
+    elif args.profile_kernel == "solve":
+        # two CG iterations (with FLUB_SOLVE_HOST_LOOP=1 every kernel is a separate launch)
+        mg.solve(2, 1e-12, 0.0, 1e-12, smoother="phases")
     else:
         for _ in range(3):
             mg.apply_preconditioner()

@@ -1,0 +1,278 @@
+// The coarse part of the V-cycle (from a level of at most 32^3 cells down to
+// the bottom) in ONE thread-block cluster.
+//
+// Below ~32^3 cells a red-black half-sweep is a few microseconds of launch
+// latency for a fraction of a microsecond of work, and the reference schedule
+// runs 6 << l iterations per side at level l.  Here a cluster of C blocks (16
+// where the GPU allows it) keeps every coarse level in distributed shared
+// memory: level l is split into slabs of P_l = nx_l / C_l consecutive i-planes
+// over C_l = min(C, nx_l / 2) blocks.  Each slab carries one ghost plane on
+// either side; a block that updates a cell on its first or last plane also
+// stores the new value into the neighbour block's ghost plane (DSMEM), so one
+// cluster barrier per half-sweep keeps every ghost plane current.  Restriction
+// writes the coarse residual straight into the owning block's shared memory,
+// prolongation reads the coarse correction from it.
+//
+// Same operations in the same order as the global kernels (mgpcg.py:72-116),
+// so results are bit-identical.  All blocks run the same sequence of cluster
+// barriers (uniform control flow); blocks that own no slab of a level simply
+// wait at them.
+#pragma once
+
+#include <cooperative_groups.h>
+
+#include "mg_kernels.cuh"
+
+namespace flub {
+
+namespace cg = cooperative_groups;
+
+constexpr int kClusterThreads = 1024;
+constexpr int kClusterMaxLevels = 8;
+
+struct ClusterLevel {
+    Dims D;
+    int abs_level;  // index in the full hierarchy (sets 6 << l)
+    int ncta;       // blocks holding a slab of this level
+    int P;          // i-planes per slab
+    int lg_ny, lg_nz;
+    const uint8_t *code;  // global cell codes of the level
+    int off_z, off_c, off_r;  // shared-memory byte offsets
+};
+
+struct ClusterParams {
+    int nl;
+    ClusterLevel lv[kClusterMaxLevels];
+    const float *r_top;  // residual of the first cluster level (global)
+    float *z_top;        // its final correction (global)
+};
+
+struct ClusterCtx {
+    cg::cluster_group cl;
+    unsigned rank;
+    unsigned char *smem;
+};
+
+__device__ __forceinline__ float *cl_z(const ClusterCtx &x, const ClusterLevel &L) {
+    return reinterpret_cast<float *>(x.smem + L.off_z);
+}
+__device__ __forceinline__ uint8_t *cl_c(const ClusterCtx &x, const ClusterLevel &L) {
+    return reinterpret_cast<uint8_t *>(x.smem + L.off_c);
+}
+__device__ __forceinline__ float *cl_r(const ClusterCtx &x, const ClusterLevel &L) {
+    return reinterpret_cast<float *>(x.smem + L.off_r);
+}
+
+// Update of one cell from shared memory.  zs/cs use the ghost-padded layout
+// (plane 0 and P+1 are ghosts); c is the index of the cell in that layout.
+__device__ __forceinline__ float cl_update(const float *zs, const uint8_t *cs, int c, int j, int k, const Dims D,
+                                           float rc, bool from_zero) {
+    if (cs[c] != kCodeFluid) return 0.0f;
+    const int sj = D.nz, si = D.ny * D.nz;
+    const uint8_t cip = cs[c + si], cim = cs[c - si];
+    const uint8_t cjp = j + 1 < D.ny ? cs[c + sj] : kCodeSolid, cjm = j > 0 ? cs[c - sj] : kCodeSolid;
+    const uint8_t ckp = k + 1 < D.nz ? cs[c + 1] : kCodeSolid, ckm = k > 0 ? cs[c - 1] : kCodeSolid;
+    const int d = (cip != kCodeSolid) + (cim != kCodeSolid) + (cjp != kCodeSolid) + (cjm != kCodeSolid) +
+                  (ckp != kCodeSolid) + (ckm != kCodeSolid);
+    if (d == 0) return 0.0f;
+    if (from_zero) return __fdiv_rn(rc, (float)d);
+    const float xc = zs[c];
+    float ret = 0.0f;
+    ret = __fadd_rn(ret, __fadd_rn(nb_term(cip, cip == kCodeFluid ? zs[c + si] : 0.0f, xc),
+                                   nb_term(cim, cim == kCodeFluid ? zs[c - si] : 0.0f, xc)));
+    ret = __fadd_rn(ret, __fadd_rn(nb_term(cjp, cjp == kCodeFluid ? zs[c + sj] : 0.0f, xc),
+                                   nb_term(cjm, cjm == kCodeFluid ? zs[c - sj] : 0.0f, xc)));
+    ret = __fadd_rn(ret, __fadd_rn(nb_term(ckp, ckp == kCodeFluid ? zs[c + 1] : 0.0f, xc),
+                                   nb_term(ckm, ckm == kCodeFluid ? zs[c - 1] : 0.0f, xc)));
+    return __fadd_rn(xc, __fdiv_rn(__fadd_rn(rc, ret), (float)d));
+}
+
+// r of an owned cell (the first level's r is copied from global memory at start).
+__device__ __forceinline__ float cl_rval(const ClusterCtx &x, const ClusterLevel &L, const ClusterParams &P, int il,
+                                         int j, int k) {
+    return cl_r(x, L)[((il << L.lg_ny) + j) * L.D.nz + k];
+}
+
+// Store v into cell (il, j, k) of this block and, for a cell on the first or
+// last plane of the slab, into the matching ghost plane of the neighbour.
+__device__ __forceinline__ void cl_store(const ClusterCtx &x, const ClusterLevel &L, float *zs, int il, int j, int k,
+                                         float v) {
+    const int plane = L.D.ny * L.D.nz;
+    const int off = (j << L.lg_nz) + k;
+    zs[(il + 1) * plane + off] = v;
+    if (il == 0 && x.rank > 0) {
+        float *zn = x.cl.map_shared_rank(zs, x.rank - 1);
+        zn[(L.P + 1) * plane + off] = v;
+    }
+    if (il == L.P - 1 && x.rank + 1 < (unsigned)L.ncta) {
+        float *zn = x.cl.map_shared_rank(zs, x.rank + 1);
+        zn[off] = v;
+    }
+}
+
+// L z at an owned cell (0 off the fluid), for the restriction.
+__device__ __forceinline__ float cl_lap(const float *zs, const uint8_t *cs, int c, int j, int k, const Dims D) {
+    if (cs[c] != kCodeFluid) return 0.0f;
+    const int sj = D.nz, si = D.ny * D.nz;
+    const uint8_t cip = cs[c + si], cim = cs[c - si];
+    const uint8_t cjp = j + 1 < D.ny ? cs[c + sj] : kCodeSolid, cjm = j > 0 ? cs[c - sj] : kCodeSolid;
+    const uint8_t ckp = k + 1 < D.nz ? cs[c + 1] : kCodeSolid, ckm = k > 0 ? cs[c - 1] : kCodeSolid;
+    const float xc = zs[c];
+    float ret = 0.0f;
+    ret = __fadd_rn(ret, __fadd_rn(nb_term(cip, cip == kCodeFluid ? zs[c + si] : 0.0f, xc),
+                                   nb_term(cim, cim == kCodeFluid ? zs[c - si] : 0.0f, xc)));
+    ret = __fadd_rn(ret, __fadd_rn(nb_term(cjp, cjp == kCodeFluid ? zs[c + sj] : 0.0f, xc),
+                                   nb_term(cjm, cjm == kCodeFluid ? zs[c - sj] : 0.0f, xc)));
+    ret = __fadd_rn(ret, __fadd_rn(nb_term(ckp, ckp == kCodeFluid ? zs[c + 1] : 0.0f, xc),
+                                   nb_term(ckm, ckm == kCodeFluid ? zs[c - 1] : 0.0f, xc)));
+    return ret;
+}
+
+// One red-black half-sweep of level t (mgpcg.py:72-86), then a cluster barrier.
+__device__ __forceinline__ void cl_half(const ClusterCtx &x, const ClusterParams &P, int t, int phase,
+                                        bool from_zero) {
+    const ClusterLevel &L = P.lv[t];
+    if (x.rank < (unsigned)L.ncta) {
+        float *zs = cl_z(x, L);
+        const uint8_t *cs = cl_c(x, L);
+        const int lg_hz = L.lg_nz - 1;
+        const int npairs = L.P << (L.lg_ny + lg_hz);
+        const int par = 1 - phase;
+        for (int q = threadIdx.x; q < npairs; q += blockDim.x) {
+            const int kk = q & ((1 << lg_hz) - 1);
+            const int j = (q >> lg_hz) & (L.D.ny - 1);
+            const int il = q >> (lg_hz + L.lg_ny);
+            const int b = (par + (int)x.rank * L.P + il + j) & 1;
+            const int k = 2 * kk + b;
+            const int c = ((il + 1) << (L.lg_ny + L.lg_nz)) + (j << L.lg_nz) + k;
+            const float v = cl_update(zs, cs, c, j, k, L.D, cl_rval(x, L, P, il, j, k), from_zero);
+            cl_store(x, L, zs, il, j, k, v);
+            if (from_zero) cl_store(x, L, zs, il, j, b ? k - 1 : k + 1, 0.0f);
+        }
+    }
+    x.cl.sync();
+}
+
+// Residual + restriction of level t into level t+1 (mgpcg.py:94-101 as a
+// gather, children summed in (ii, jj, kk) order), written into the shared
+// memory of the block that owns the coarse plane; then a cluster barrier.
+__device__ __forceinline__ void cl_restrict(const ClusterCtx &x, const ClusterParams &P, int t) {
+    const ClusterLevel &F = P.lv[t], &C = P.lv[t + 1];
+    if (x.rank < (unsigned)F.ncta) {
+        const float *zs = cl_z(x, F);
+        const uint8_t *cs = cl_c(x, F);
+        const int cpl = F.P >> 1;
+        const int n = cpl << (C.lg_ny + C.lg_nz);
+        for (int q = threadIdx.x; q < n; q += blockDim.x) {
+            const int K = q & (C.D.nz - 1), J = (q >> C.lg_nz) & (C.D.ny - 1), Il = q >> (C.lg_ny + C.lg_nz);
+            const int gI = (int)x.rank * cpl + Il;
+            const int owner = gI / C.P, lcp = gI - owner * C.P;
+            float s = 0.0f;
+            if (__ldg(C.code + (gI << (C.lg_ny + C.lg_nz)) + (J << C.lg_nz) + K) == kCodeFluid) {
+                bool first = true;
+#pragma unroll
+                for (int ii = 0; ii < 2; ii++)
+#pragma unroll
+                    for (int jj = 0; jj < 2; jj++)
+#pragma unroll
+                        for (int kk = 0; kk < 2; kk++) {
+                            const int il = 2 * Il + ii, j = 2 * J + jj, k = 2 * K + kk;
+                            const int c = ((il + 1) << (F.lg_ny + F.lg_nz)) + (j << F.lg_nz) + k;
+                            const float v = __fadd_rn(cl_rval(x, F, P, il, j, k), cl_lap(zs, cs, c, j, k, F.D));
+                            s = first ? v : __fadd_rn(s, v);
+                            first = false;
+                        }
+            }
+            float *rdst = x.cl.map_shared_rank(cl_r(x, C), (unsigned)owner);
+            rdst[(lcp << (C.lg_ny + C.lg_nz)) + (J << C.lg_nz) + K] = s;
+        }
+    }
+    x.cl.sync();
+}
+
+// z_t += z_{t+1}[I/2] (mgpcg.py:113-116), ghost planes included; then a barrier.
+__device__ __forceinline__ void cl_prolong(const ClusterCtx &x, const ClusterParams &P, int t) {
+    const ClusterLevel &F = P.lv[t], &C = P.lv[t + 1];
+    if (x.rank < (unsigned)F.ncta) {
+        float *zs = cl_z(x, F);
+        const int n = F.P << (F.lg_ny + F.lg_nz);
+        for (int q = threadIdx.x; q < n; q += blockDim.x) {
+            const int k = q & (F.D.nz - 1), j = (q >> F.lg_nz) & (F.D.ny - 1), il = q >> (F.lg_ny + F.lg_nz);
+            const int gI = ((int)x.rank * F.P + il) >> 1;
+            const int owner = gI / C.P, lcp = gI - owner * C.P;
+            const float *zc = x.cl.map_shared_rank(cl_z(x, C), (unsigned)owner);
+            const float add = zc[((lcp + 1) << (C.lg_ny + C.lg_nz)) + ((j >> 1) << C.lg_nz) + (k >> 1)];
+            const int c = ((il + 1) << (F.lg_ny + F.lg_nz)) + (j << F.lg_nz) + k;
+            cl_store(x, F, zs, il, j, k, __fadd_rn(zs[c], add));
+        }
+    }
+    x.cl.sync();
+}
+
+__global__ void __launch_bounds__(kClusterThreads, 1) k_cluster_vcycle(const ClusterParams P, unsigned long long *kc) {
+    extern __shared__ __align__(16) unsigned char cluster_smem[];
+    count_kernel(kc);
+    ClusterCtx x{cg::this_cluster(), 0u, cluster_smem};
+    x.rank = x.cl.block_rank();
+    // cell codes of the owned planes and both ghost planes (0 outside the domain)
+    for (int t = 0; t < P.nl; t++) {
+        const ClusterLevel &L = P.lv[t];
+        if (x.rank >= (unsigned)L.ncta) continue;
+        uint8_t *cs = cl_c(x, L);
+        float *zs = cl_z(x, L);
+        const int lg_pl = L.lg_ny + L.lg_nz;
+        const int n = (L.P + 2) << lg_pl;
+        for (int q = threadIdx.x; q < n; q += blockDim.x) {
+            const int gp = (int)x.rank * L.P - 1 + (q >> lg_pl);
+            cs[q] = (gp >= 0 && gp < L.D.nx) ? __ldg(L.code + (gp << lg_pl) + (q & ((1 << lg_pl) - 1))) : kCodeSolid;
+            zs[q] = 0.0f;
+        }
+    }
+    {
+        // the first level's residual comes from global memory once
+        const ClusterLevel &L = P.lv[0];
+        if (x.rank < (unsigned)L.ncta) {
+            float *rs = cl_r(x, L);
+            const int lg_pl = L.lg_ny + L.lg_nz;
+            const int n = L.P << lg_pl;
+            const float *src = P.r_top + ((int)x.rank * L.P << lg_pl);
+            for (int q = threadIdx.x; q < n; q += blockDim.x) rs[q] = __ldg(src + q);
+        }
+    }
+    x.cl.sync();
+    const int nb = P.nl - 1;
+    for (int t = 0; t < nb; t++) {
+        const int iters = 6 << P.lv[t].abs_level;
+        for (int it = 0; it < iters; it++) {
+            cl_half(x, P, t, 0, it == 0);
+            cl_half(x, P, t, 1, false);
+        }
+        cl_restrict(x, P, t);
+    }
+    for (int it = 0; it < 3; it++) {
+        cl_half(x, P, nb, 0, it == 0);
+        cl_half(x, P, nb, 1, false);
+    }
+    for (int it = 0; it < 3; it++) {
+        cl_half(x, P, nb, 1, false);
+        cl_half(x, P, nb, 0, false);
+    }
+    for (int t = nb - 1; t >= 0; t--) {
+        cl_prolong(x, P, t);
+        const int iters = 6 << P.lv[t].abs_level;
+        for (int it = 0; it < iters; it++) {
+            cl_half(x, P, t, 1, false);
+            cl_half(x, P, t, 0, false);
+        }
+    }
+    const ClusterLevel &L = P.lv[0];
+    if (x.rank < (unsigned)L.ncta) {
+        const float *zs = cl_z(x, L);
+        const int lg_pl = L.lg_ny + L.lg_nz;
+        const int n = L.P << lg_pl;
+        const int base = (int)x.rank * L.P << lg_pl;
+        for (int q = threadIdx.x; q < n; q += blockDim.x) P.z_top[base + q] = zs[(1 << lg_pl) + q];
+    }
+}
+
+}  // namespace flub

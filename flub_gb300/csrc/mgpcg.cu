@@ -18,6 +18,7 @@
 
 #include "mg_kernels.cuh"
 #include "cg8.cuh"
+#include "cluster.cuh"
 #include "smooth8.cuh"
 #include "tail.cuh"
 
@@ -69,6 +70,9 @@ struct flub_mg {
     bool r_masked;  // r is 0 off the fluid (mask_interior since the last init)
     int tail_start;  // first level run by the one-block tail kernel (== levels: none)
     size_t tail_smem;
+    int cl_start;    // first level run by the cluster kernel (== levels: none)
+    int cl_size;     // blocks per cluster
+    size_t cl_smem;
 };
 
 namespace flub {
@@ -150,6 +154,114 @@ static int choose_tail(flub_mg *mg) {
             mg->tail_smem = b;
         }
         break;
+    }
+    return FLUB_OK;
+}
+
+static inline bool is_pow2(int v) { return v > 0 && (v & (v - 1)) == 0; }
+static inline int ilog2(int v) {
+    int l = 0;
+    while ((1 << l) < v) l++;
+    return l;
+}
+
+// Distributed-shared-memory layout of the cluster kernel from level lc down
+// with C blocks; returns the bytes per block (0 if the levels do not qualify:
+// every dimension a power of two, nx and nz at least 2 at every level).
+static size_t cluster_layout(const flub_mg *mg, int lc, int C, ClusterParams *P) {
+    if (lc >= mg->levels || mg->levels - lc > kClusterMaxLevels) return 0;
+    size_t off = 0;
+    auto take = [&](size_t b) {
+        size_t o = off;
+        off += (b + 15) & ~(size_t)15;
+        return (int)o;
+    };
+    for (int l = lc; l < mg->levels; l++) {
+        const Dims D{mg->nx >> l, mg->ny >> l, mg->nz >> l};
+        if (!is_pow2(D.nx) || !is_pow2(D.ny) || !is_pow2(D.nz) || D.nx < 2 || D.nz < 2) return 0;
+        ClusterLevel &L = P->lv[l - lc];
+        L.D = D;
+        L.abs_level = l;
+        L.ncta = D.nx / 2 < C ? D.nx / 2 : C;
+        L.P = D.nx / L.ncta;
+        L.lg_ny = ilog2(D.ny);
+        L.lg_nz = ilog2(D.nz);
+        L.code = mg->lv[l].code;
+        const size_t plane = (size_t)D.ny * D.nz;
+        L.off_z = take(sizeof(float) * (L.P + 2) * plane);
+        L.off_c = take((L.P + 2) * plane);
+        L.off_r = take(sizeof(float) * L.P * plane);
+    }
+    P->nl = mg->levels - lc;
+    return off;
+}
+
+static cudaError_t cluster_launch_config(int C, size_t smem, cudaStream_t s, cudaLaunchConfig_t *cfg,
+                                         cudaLaunchAttribute *attr) {
+    memset(cfg, 0, sizeof(*cfg));
+    cfg->gridDim = dim3(C);
+    cfg->blockDim = dim3(kClusterThreads);
+    cfg->dynamicSmemBytes = smem;
+    cfg->stream = s;
+    attr[0].id = cudaLaunchAttributeClusterDimension;
+    attr[0].val.clusterDim.x = C;
+    attr[0].val.clusterDim.y = 1;
+    attr[0].val.clusterDim.z = 1;
+    attr[1].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+    attr[1].val.programmaticStreamSerializationAllowed = 1;
+    cfg->attrs = attr;
+    cfg->numAttrs = 2;
+    return cudaSuccess;
+}
+
+// Picks the first level of at most 32^3 cells whose coarse hierarchy fits one
+// cluster (16 blocks, else 8); none if the GPU cannot run it or
+// FLUB_NO_CLUSTER=1.
+static int choose_cluster(flub_mg *mg) {
+    mg->cl_start = mg->levels;
+    mg->cl_size = 0;
+    mg->cl_smem = 0;
+    const char *off = getenv("FLUB_NO_CLUSTER");
+    if (off && off[0] == '1') return FLUB_OK;
+    int dev = 0, max_smem = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess ||
+        cudaDeviceGetAttribute(&max_smem, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev) != cudaSuccess) {
+        cudaGetLastError();
+        return FLUB_OK;
+    }
+    // larger levels keep the 152-SM global sweeps: on 8-16 SMs a 64^3 half-sweep
+    // is bound by shared-memory bandwidth (FLUB_CLUSTER_MAX_CELLS overrides)
+    int64_t max_cells = 32768;
+    const char *mc = getenv("FLUB_CLUSTER_MAX_CELLS");
+    if (mc && atoll(mc) > 0) max_cells = atoll(mc);
+    for (int C : {16, 8}) {
+        for (int l = 0; l < mg->levels; l++) {
+            const Dims D{mg->nx >> l, mg->ny >> l, mg->nz >> l};
+            if (D.n() > max_cells) continue;
+            ClusterParams P;
+            const size_t b = cluster_layout(mg, l, C, &P);
+            if (b == 0 || b > (size_t)max_smem) break;
+            if (cudaFuncSetAttribute(k_cluster_vcycle, cudaFuncAttributeNonPortableClusterSizeAllowed, 1) !=
+                    cudaSuccess ||
+                cudaFuncSetAttribute(k_cluster_vcycle, cudaFuncAttributeMaxDynamicSharedMemorySize, max_smem) !=
+                    cudaSuccess) {
+                cudaGetLastError();
+                break;
+            }
+            cudaLaunchConfig_t cfg;
+            cudaLaunchAttribute attr[2];
+            cluster_launch_config(C, b, nullptr, &cfg, attr);
+            cfg.numAttrs = 1;  // the cluster dimension only
+            int nclusters = 0;
+            if (cudaOccupancyMaxActiveClusters(&nclusters, k_cluster_vcycle, &cfg) != cudaSuccess || nclusters < 1) {
+                cudaGetLastError();
+                break;
+            }
+            mg->cl_start = l;
+            mg->cl_size = C;
+            mg->cl_smem = b;
+            return FLUB_OK;
+        }
     }
     return FLUB_OK;
 }
@@ -239,7 +351,8 @@ static int sweep(const LaunchCtx &c, const Level &L, int phase, int mode, int sk
 // multigrid/mgpcg.py:296-349 apply_preconditioner; level 0 uses (r0, z0).
 // z0_clean: z0 holds 0 on every non-fluid cell (true for the handle's own z).
 static int enqueue_vcycle(flub_mg *mg, const LaunchCtx &c, const float *r0, float *z0, bool z0_clean) {
-    const int Lm = mg->levels, lt = mg->tail_start;
+    const bool use_cl = mg->cl_start < mg->levels;
+    const int Lm = mg->levels, lt = use_cl ? mg->cl_start : mg->tail_start;
     const int sk = mg->skip_ok ? 1 : 0;
     auto SK = [&](int l) { return (l == 0 && !z0_clean) ? 0 : sk; };
     auto R = [&](int l) -> const float * { return l == 0 ? r0 : mg->lv[l].r; };
@@ -257,7 +370,22 @@ static int enqueue_vcycle(flub_mg *mg, const LaunchCtx &c, const float *r0, floa
         FLUB_TRY(launch_pdl(k_restrict, dim3(blocks_for(C.D.n(), 256, 1 << 20)), dim3(256), 0, c.s, R(l), ZP(l),
                             L.code, C.r, C.code, C.D, c.kc));
     }
-    if (lt < Lm) {
+    if (use_cl) {
+        ClusterParams P;
+        cluster_layout(mg, lt, mg->cl_size, &P);
+        P.r_top = R(lt);
+        P.z_top = ZF(lt);
+        cudaLaunchConfig_t cfg;
+        cudaLaunchAttribute attr[2];
+        cluster_launch_config(mg->cl_size, mg->cl_smem, c.s, &cfg, attr);
+        const cudaError_t e = cudaLaunchKernelEx(&cfg, k_cluster_vcycle, (const ClusterParams)P, c.kc);
+        if (e != cudaSuccess) {
+            set_last_error("cluster V-cycle launch: %s", cudaGetErrorString(e));
+            cudaGetLastError();
+            return FLUB_ERR_CUDA;
+        }
+        count_launches(1);
+    } else if (lt < Lm) {
         TailParams P;
         tail_layout(mg, lt, &P);
         P.r_top = R(lt);
@@ -512,6 +640,7 @@ int flub_mg_create(int nx, int ny, int nz, int levels, int precision, void *work
     mg->host_loop = hl && hl[0] == '1';
     mg->skip_ok = true;  // the workspace is zeroed below and set_tags re-zeroes the z buffers
     choose_tail(mg);
+    choose_cluster(mg);
     if (set_tail_smem_limit() != FLUB_OK) {
         flub_mg_destroy(mg);
         return FLUB_ERR_CUDA;
@@ -768,6 +897,7 @@ extern "C" int flub_vcycle_noalloc(const int32_t *tag, const float *r, float *z,
     FLUB_TRY(noalloc_scratch_address(&base));
     noalloc_layout(&mg, (char *)base);
     choose_tail(&mg);
+    choose_cluster(&mg);
     FLUB_TRY(set_tail_smem_limit());
     cudaStream_t s = as_stream(stream);
     // every scratch element is written before it is read: the codes by these two

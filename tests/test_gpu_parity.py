@@ -151,6 +151,21 @@ def test_vcycle_bit_exact(scene):
     assert np.array_equal(host(z), z_o)
 
 
+@pytest.mark.parametrize("name", ["dam64", "rand32b", "box32"])
+def test_vcycle_fallback_paths_bit_exact(name, monkeypatch):
+    """The coarse levels run in one thread-block cluster when the GPU allows it;
+    the fallback (global sweeps + one-block tail kernel) must give the same bits."""
+    scene = SCENES[name]()
+    tag_o, r0, mg = _setup(scene)
+    z_cluster = host(mg.apply_preconditioner(dev(r0)))
+    monkeypatch.setenv("FLUB_NO_CLUSTER", "1")
+    tag_o, r0, mg2 = _setup(scene)
+    z_plain = host(mg2.apply_preconditioner(dev(r0)))
+    z_o = O.vcycle(r0, O.tag_levels(tag_o, scene.levels), np.float32)
+    assert np.array_equal(z_cluster, z_o)
+    assert np.array_equal(z_plain, z_o)
+
+
 def test_solve_matches_oracle(scene):
     tag_o, r0, mg = _setup(scene)
     info = mg.solve(200, 1e-12, 0.0, 1e-12, smoother="phases")
@@ -349,7 +364,8 @@ def test_kernel_counter_advances():
     tag_o, r0, mg = _setup(s)
     k0 = mg.kernels_executed()
     info = mg.solve(200, 1e-12, 0.0, 1e-12, smoother="phases")
-    assert mg.kernels_executed() > k0 + 10 * info["iterations"]
+    # at least the V-cycle and the CG kernels of every iteration
+    assert mg.kernels_executed() >= k0 + 4 * info["iterations"]
 
 
 def test_reference_call_sequence():
