@@ -20,6 +20,7 @@
 #pragma once
 
 #include <cooperative_groups.h>
+#include <cuda_fp16.h>
 
 #include "mg_kernels.cuh"
 
@@ -45,6 +46,8 @@ struct ClusterParams {
     ClusterLevel lv[kClusterMaxLevels];
     const float *r_top;  // residual of the first cluster level (global)
     float *z_top;        // its final correction (global)
+    const __half *r_top_h;  // FP16 instead of r_top / z_top when not NULL (mixed precision)
+    __half *z_top_h;
 };
 
 struct ClusterCtx {
@@ -235,8 +238,11 @@ __global__ void __launch_bounds__(kClusterThreads, 1) k_cluster_vcycle(const Clu
             float *rs = cl_r(x, L);
             const int lg_pl = L.lg_ny + L.lg_nz;
             const int n = L.P << lg_pl;
-            const float *src = P.r_top + ((int)x.rank * L.P << lg_pl);
-            for (int q = threadIdx.x; q < n; q += blockDim.x) rs[q] = __ldg(src + q);
+            const int base = (int)x.rank * L.P << lg_pl;
+            if (P.r_top_h)
+                for (int q = threadIdx.x; q < n; q += blockDim.x) rs[q] = __half2float(P.r_top_h[base + q]);
+            else
+                for (int q = threadIdx.x; q < n; q += blockDim.x) rs[q] = __ldg(P.r_top + base + q);
         }
     }
     x.cl.sync();
@@ -271,7 +277,10 @@ __global__ void __launch_bounds__(kClusterThreads, 1) k_cluster_vcycle(const Clu
         const int lg_pl = L.lg_ny + L.lg_nz;
         const int n = L.P << lg_pl;
         const int base = (int)x.rank * L.P << lg_pl;
-        for (int q = threadIdx.x; q < n; q += blockDim.x) P.z_top[base + q] = zs[(1 << lg_pl) + q];
+        if (P.z_top_h)
+            for (int q = threadIdx.x; q < n; q += blockDim.x) P.z_top_h[base + q] = __float2half_rn(zs[(1 << lg_pl) + q]);
+        else
+            for (int q = threadIdx.x; q < n; q += blockDim.x) P.z_top[base + q] = zs[(1 << lg_pl) + q];
     }
 }
 

@@ -19,6 +19,7 @@
 #include "mg_kernels.cuh"
 #include "cg8.cuh"
 #include "cluster.cuh"
+#include "mixed.cuh"
 #include "smooth8.cuh"
 #include "tail.cuh"
 
@@ -38,6 +39,9 @@ struct Level {
     float *r;
     float *z;
     float *z2;
+    // mixed precision: FP16 copies at scale 8^-l (level 0: rh is the FP16 copy
+    // of the CG residual, zh is unused, z is the FP32 CG vector)
+    __half *rh, *zh, *z2h;
 };
 
 struct LaunchCtx {
@@ -58,6 +62,7 @@ struct flub_mg {
     int device;
     flub::Level lv[flub::kMaxLevels];
     float *x, *p, *Ap;
+    float *r_old;  // mixed precision: the residual of the previous iteration (flexible CG)
     flub::MgState *st;
     double *partials;
     double *hist;
@@ -107,7 +112,14 @@ static size_t carve(flub_mg *mg, char *base) {
         L.r = (float *)take(sizeof(float) * nl);
         L.z = (float *)take(sizeof(float) * nl);
         L.z2 = (float *)take(sizeof(float) * nl);
+        L.rh = L.zh = L.z2h = nullptr;
+        if (mg->precision == FLUB_PRECISION_MIXED) {
+            L.rh = (__half *)take(sizeof(__half) * nl);
+            L.zh = l ? (__half *)take(sizeof(__half) * nl) : nullptr;
+            L.z2h = (__half *)take(sizeof(__half) * nl);
+        }
     }
+    mg->r_old = mg->precision == FLUB_PRECISION_MIXED ? (float *)take(sizeof(float) * n) : nullptr;
     return off;
 }
 
@@ -283,10 +295,10 @@ static inline unsigned red_blocks(int64_t n) { return blocks_for(n, kRedThreads,
 
 // ---------------------------------------------------------------- enqueue helpers
 
-#define FLUB_TRY(x)            \
-    do {                       \
-        int _s = (x);          \
-        if (_s) return _s;     \
+#define FLUB_TRY(...)              \
+    do {                           \
+        int _s = (__VA_ARGS__);    \
+        if (_s) return _s;         \
     } while (0)
 
 // Kernel launch with programmatic stream serialisation (the kernel's entry
@@ -319,22 +331,30 @@ enum SweepMode { kSweepInPlace = 0, kSweepFromZero = 1, kSweepProlong = 2 };
 //   kSweepInPlace   zout = sweep(zout)
 //   kSweepFromZero  zout = sweep(0)
 //   kSweepProlong   zout = sweep(zin + P zc)   (mgpcg.py:113-116 fused in)
+// Storage-generic form of the vectorised sweep (nz % 8 == 0): TO/TI/TR/TC are
+// the types of zout, zin, r and the coarse correction zc (float or __half);
+// zc is multiplied by zc_scale on load.
+template <typename TO, typename TI, typename TR, typename TC>
+static int sweep8(const LaunchCtx &c, const Level &L, int phase, int mode, int skip, const TR *r, const TI *zin,
+                  TO *zout, const TC *zc, float zc_scale) {
+    const Dims D = L.D;
+    const int nz8 = D.nz >> 3;
+    const int bx = nz8 < 32 ? nz8 : 32, by = 256 / bx;
+    const dim3 blk(bx, by), grd((nz8 + bx - 1) / bx, (D.ny + by - 1) / by, D.nx);
+    if (mode == kSweepFromZero)
+        return launch_pdl(k_smooth8<true, false, TO, TO, TR, TC>, grd, blk, 0, c.s, zout, (const TO *)zout,
+                          (const TC *)nullptr, 1.0f, r, (const uint8_t *)L.code, D, phase, skip, c.kc);
+    if (mode == kSweepProlong)
+        return launch_pdl(k_smooth8<false, true, TO, TI, TR, TC>, grd, blk, 0, c.s, zout, zin, zc, zc_scale, r,
+                          (const uint8_t *)L.code, D, phase, skip, c.kc);
+    return launch_pdl(k_smooth8<false, false, TO, TO, TR, TC>, grd, blk, 0, c.s, zout, (const TO *)zout,
+                      (const TC *)nullptr, 1.0f, r, (const uint8_t *)L.code, D, phase, skip, c.kc);
+}
+
 static int sweep(const LaunchCtx &c, const Level &L, int phase, int mode, int skip, const float *r,
                  const float *zin, float *zout, const float *zc) {
     const Dims D = L.D;
-    if (D.nz % 8 == 0) {
-        const int nz8 = D.nz >> 3;
-        const int bx = nz8 < 32 ? nz8 : 32, by = 256 / bx;
-        const dim3 blk(bx, by), grd((nz8 + bx - 1) / bx, (D.ny + by - 1) / by, D.nx);
-        if (mode == kSweepFromZero)
-            return launch_pdl(k_smooth8<true, false>, grd, blk, 0, c.s, zout, (const float *)zout,
-                              (const float *)nullptr, r, (const uint8_t *)L.code, D, phase, skip, c.kc);
-        if (mode == kSweepProlong)
-            return launch_pdl(k_smooth8<false, true>, grd, blk, 0, c.s, zout, zin, zc, r, (const uint8_t *)L.code, D,
-                              phase, skip, c.kc);
-        return launch_pdl(k_smooth8<false, false>, grd, blk, 0, c.s, zout, (const float *)zout,
-                          (const float *)nullptr, r, (const uint8_t *)L.code, D, phase, skip, c.kc);
-    }
+    if (D.nz % 8 == 0) return sweep8<float, float, float, float>(c, L, phase, mode, skip, r, zin, zout, zc, 1.0f);
     // scalar path for levels whose nz is not a multiple of 8
     if (mode == kSweepProlong)
         FLUB_TRY(launch_pdl(k_prolong, dim3(blocks_for(D.n(), 256, 1 << 20)), dim3(256), 0, c.s, zout, zin, zc, D,
@@ -371,7 +391,7 @@ static int enqueue_vcycle(flub_mg *mg, const LaunchCtx &c, const float *r0, floa
                             L.code, C.r, C.code, C.D, c.kc));
     }
     if (use_cl) {
-        ClusterParams P;
+        ClusterParams P = {};
         cluster_layout(mg, lt, mg->cl_size, &P);
         P.r_top = R(lt);
         P.z_top = ZF(lt);
@@ -386,7 +406,7 @@ static int enqueue_vcycle(flub_mg *mg, const LaunchCtx &c, const float *r0, floa
         }
         count_launches(1);
     } else if (lt < Lm) {
-        TailParams P;
+        TailParams P = {};
         tail_layout(mg, lt, &P);
         P.r_top = R(lt);
         P.z_top = ZF(lt);
@@ -415,6 +435,112 @@ static int enqueue_vcycle(flub_mg *mg, const LaunchCtx &c, const float *r0, floa
     return FLUB_OK;
 }
 
+// Cluster or one-block kernel for the coarse levels from lt down, with FP16
+// (mixed precision) or FP32 top-level residual/correction.
+static int launch_coarse(flub_mg *mg, const LaunchCtx &c, int lt, const float *r_top, float *z_top,
+                         const __half *r_top_h, __half *z_top_h) {
+    if (mg->cl_start < mg->levels) {
+        ClusterParams P = {};
+        cluster_layout(mg, lt, mg->cl_size, &P);
+        P.r_top = r_top;
+        P.z_top = z_top;
+        P.r_top_h = r_top_h;
+        P.z_top_h = z_top_h;
+        cudaLaunchConfig_t cfg;
+        cudaLaunchAttribute attr[2];
+        cluster_launch_config(mg->cl_size, mg->cl_smem, c.s, &cfg, attr);
+        const cudaError_t e = cudaLaunchKernelEx(&cfg, k_cluster_vcycle, (const ClusterParams)P, c.kc);
+        if (e != cudaSuccess) {
+            set_last_error("cluster V-cycle launch: %s", cudaGetErrorString(e));
+            cudaGetLastError();
+            return FLUB_ERR_CUDA;
+        }
+        count_launches(1);
+        return FLUB_OK;
+    }
+    TailParams P = {};
+    tail_layout(mg, lt, &P);
+    P.r_top = r_top;
+    P.z_top = z_top;
+    P.r_top_h = r_top_h;
+    P.z_top_h = z_top_h;
+    return launch_pdl(k_tail_vcycle, dim3(1), dim3(kTailThreads), mg->tail_smem, c.s, P, c.kc);
+}
+
+// Mixed-precision V-cycle: the levels in global memory are FP16 at scale 8^-l
+// (mixed.cuh); the level-0 residual is read from its FP16 copy lv[0].rh, the
+// result z0 is FP32.  Same schedule as enqueue_vcycle.
+static int enqueue_vcycle_mixed(flub_mg *mg, const LaunchCtx &c, float *z0, bool z0_clean) {
+    const bool use_cl = mg->cl_start < mg->levels;
+    const int Lm = mg->levels, lt = use_cl ? mg->cl_start : mg->tail_start;
+    const int sk = mg->skip_ok ? 1 : 0;
+    const int sk0 = z0_clean ? sk : 0;
+    const int lg = lt < Lm - 1 ? lt : Lm - 1;
+    for (int l = 0; l < lg; l++) {
+        const Level &L = mg->lv[l];
+        const int iters = 6 << l;
+        for (int it = 0; it < iters; it++) {
+            FLUB_TRY(sweep8<__half, __half, __half, __half>(c, L, 0, it == 0 ? kSweepFromZero : kSweepInPlace, sk,
+                                                            L.rh, L.z2h, L.z2h, nullptr, 1.0f));
+            FLUB_TRY(sweep8<__half, __half, __half, __half>(c, L, 1, kSweepInPlace, sk, L.rh, L.z2h, L.z2h, nullptr,
+                                                            1.0f));
+        }
+        const Level &C = mg->lv[l + 1];
+        FLUB_TRY(launch_pdl(k_restrict_t<__half, __half, __half>, dim3(blocks_for(C.D.n(), 256, 1 << 20)), dim3(256),
+                            0, c.s, (const __half *)L.rh, (const __half *)L.z2h, (const uint8_t *)L.code, C.rh,
+                            (const uint8_t *)C.code, C.D, 0.125f, c.kc));
+    }
+    if (lt < Lm) {
+        if (lt == 0)
+            FLUB_TRY(launch_coarse(mg, c, 0, nullptr, z0, mg->lv[0].rh, nullptr));
+        else
+            FLUB_TRY(launch_coarse(mg, c, lt, nullptr, nullptr, mg->lv[lt].rh, mg->lv[lt].zh));
+    } else {
+        const int b = Lm - 1;
+        const Level &L = mg->lv[b];
+        for (int q = 0; q < 6; q++) {
+            // bottom: 3 x (0, 1) from zero, then 3 x (1, 0)
+            const int ph0 = q < 3 ? 0 : 1, ph1 = 1 - ph0;
+            const int m0 = q == 0 ? kSweepFromZero : kSweepInPlace;
+            if (b == 0) {
+                FLUB_TRY(sweep8<float, float, __half, float>(c, L, ph0, m0, sk0, L.rh, z0, z0, nullptr, 1.0f));
+                FLUB_TRY(sweep8<float, float, __half, float>(c, L, ph1, kSweepInPlace, sk0, L.rh, z0, z0, nullptr,
+                                                             1.0f));
+            } else {
+                FLUB_TRY(sweep8<__half, __half, __half, __half>(c, L, ph0, m0, sk, L.rh, L.zh, L.zh, nullptr, 1.0f));
+                FLUB_TRY(sweep8<__half, __half, __half, __half>(c, L, ph1, kSweepInPlace, sk, L.rh, L.zh, L.zh,
+                                                                nullptr, 1.0f));
+            }
+        }
+    }
+    for (int l = lg - 1; l >= 0; l--) {
+        const Level &L = mg->lv[l];
+        const __half *zc = mg->lv[l + 1].zh;
+        const int iters = 6 << l;
+        for (int it = 0; it < iters; it++) {
+            if (l == 0) {
+                if (it == 0)
+                    FLUB_TRY(sweep8<float, __half, __half, __half>(c, L, 1, kSweepProlong, sk0, L.rh, L.z2h, z0, zc,
+                                                                   8.0f));
+                else
+                    FLUB_TRY(sweep8<float, float, __half, float>(c, L, 1, kSweepInPlace, sk0, L.rh, z0, z0, nullptr,
+                                                                 1.0f));
+                FLUB_TRY(sweep8<float, float, __half, float>(c, L, 0, kSweepInPlace, sk0, L.rh, z0, z0, nullptr, 1.0f));
+            } else {
+                if (it == 0)
+                    FLUB_TRY(sweep8<__half, __half, __half, __half>(c, L, 1, kSweepProlong, sk, L.rh, L.z2h, L.zh, zc,
+                                                                    8.0f));
+                else
+                    FLUB_TRY(sweep8<__half, __half, __half, __half>(c, L, 1, kSweepInPlace, sk, L.rh, L.zh, L.zh,
+                                                                    nullptr, 1.0f));
+                FLUB_TRY(sweep8<__half, __half, __half, __half>(c, L, 0, kSweepInPlace, sk, L.rh, L.zh, L.zh, nullptr,
+                                                                1.0f));
+            }
+        }
+    }
+    return FLUB_OK;
+}
+
 static int enqueue_mean_removal(flub_mg *mg, const LaunchCtx &c, int guard) {
     const unsigned b = red_blocks(mg->n);
     FLUB_TRY(launch_pdl(k_fluid_mean, dim3(b), dim3(kRedThreads), 0, c.s, mg->st, mg->lv[0].r, mg->lv[0].code, mg->n, mg->partials, guard, c.kc));
@@ -422,7 +548,53 @@ static int enqueue_mean_removal(flub_mg *mg, const LaunchCtx &c, int guard) {
     return FLUB_OK;
 }
 
+// ---- mixed precision: same loop, FP16 V-cycle, flexible beta
+static int enqueue_prologue_mixed(flub_mg *mg, const LaunchCtx &c, int smoother) {
+    const Level &L0 = mg->lv[0];
+    const unsigned bg = red_blocks(mg->n / 8 + 1);
+    if (smoother == FLUB_SMOOTHER_FRACTION) FLUB_TRY(enqueue_mean_removal(mg, c, 0));
+    FLUB_TRY(launch_pdl(k8_dot_rr0, dim3(bg), dim3(kRedThreads), 0, c.s, mg->st, L0.r, L0.code, mg->n, mg->partials,
+                        c.kc));
+    FLUB_TRY(launch_pdl(k_residual_x0, dim3(blocks_for(mg->n, 256)), dim3(256), 0, c.s, mg->st, L0.r, mg->x, L0.code,
+                        L0.D, c.kc));
+    if (smoother == FLUB_SMOOTHER_FRACTION) FLUB_TRY(enqueue_mean_removal(mg, c, 2));
+    FLUB_TRY(launch_pdl(k8_to_half, dim3(blocks_for(mg->n / 8, 256)), dim3(256), 0, c.s, (const float *)L0.r, L0.rh,
+                        mg->n, c.kc));
+    FLUB_TRY(enqueue_vcycle_mixed(mg, c, L0.z, true));
+    return launch_pdl(k8_dot_zr<true>, dim3(bg), dim3(kRedThreads), 0, c.s, mg->st, L0.z, L0.r, mg->p, L0.code,
+                      mg->n, mg->partials, c.kc);
+}
+
+static int enqueue_first_half_mixed(flub_mg *mg, const LaunchCtx &c, int smoother) {
+    const Level &L0 = mg->lv[0];
+    const unsigned b = red_blocks(mg->n), bg = red_blocks(mg->n / 8 + 1);
+    FLUB_TRY(launch_pdl(k8_matvec_pap, dim3(bg), dim3(kRedThreads), 0, c.s, mg->st, mg->p, mg->Ap, L0.code, L0.D,
+                        mg->partials, c.kc));
+    if (smoother == FLUB_SMOOTHER_FRACTION) {
+        FLUB_CHECK_CUDA(cudaMemcpyAsync(mg->r_old, L0.r, sizeof(float) * mg->n, cudaMemcpyDeviceToDevice, c.s));
+        FLUB_TRY(launch_pdl(k_update_r, dim3(b), dim3(kRedThreads), 0, c.s, mg->st, L0.r, mg->Ap, mg->n, c.kc));
+        FLUB_TRY(enqueue_mean_removal(mg, c, 1));
+        FLUB_TRY(launch_pdl(k8_to_half, dim3(blocks_for(mg->n / 8, 256)), dim3(256), 0, c.s, (const float *)L0.r,
+                            L0.rh, mg->n, c.kc));
+        return launch_pdl(k8_update_r_rr<false>, dim3(bg), dim3(kRedThreads), 0, c.s, mg->st, L0.r, mg->Ap, L0.code,
+                          mg->n, mg->partials, mg->hist, c.h, c.set_cond, c.kc);
+    }
+    return launch_pdl(k8_update_r_rr_mixed, dim3(bg), dim3(kRedThreads), 0, c.s, mg->st, L0.r, mg->r_old, L0.rh,
+                      mg->Ap, L0.code, mg->n, mg->partials, mg->hist, c.h, c.set_cond, c.kc);
+}
+
+static int enqueue_second_half_mixed(flub_mg *mg, const LaunchCtx &c) {
+    const Level &L0 = mg->lv[0];
+    const unsigned bg = red_blocks(mg->n / 8 + 1);
+    FLUB_TRY(enqueue_vcycle_mixed(mg, c, L0.z, true));
+    FLUB_TRY(launch_pdl(k8_dot_zr_flex, dim3(bg), dim3(kRedThreads), 0, c.s, mg->st, L0.z, L0.r, mg->r_old, L0.code,
+                        mg->n, mg->partials, c.kc));
+    return launch_pdl(k8_update_xp, dim3(blocks_for(mg->n / 8, 256)), dim3(256), 0, c.s, mg->st, mg->x, mg->p, L0.z,
+                      L0.code, mg->n, c.kc);
+}
+
 static int enqueue_prologue(flub_mg *mg, const LaunchCtx &c, int smoother) {
+    if (mg->precision == FLUB_PRECISION_MIXED) return enqueue_prologue_mixed(mg, c, smoother);
     const unsigned b = red_blocks(mg->n);
     const Level &L0 = mg->lv[0];
     const bool v8 = (L0.D.nz % 8) == 0;  // group-of-8 kernels; the scalar ones otherwise
@@ -446,6 +618,7 @@ static int enqueue_prologue(flub_mg *mg, const LaunchCtx &c, int smoother) {
 
 // Ap, alpha, r update, r.r, convergence test, loop condition.
 static int enqueue_first_half(flub_mg *mg, const LaunchCtx &c, int smoother) {
+    if (mg->precision == FLUB_PRECISION_MIXED) return enqueue_first_half_mixed(mg, c, smoother);
     const unsigned b = red_blocks(mg->n);
     const Level &L0 = mg->lv[0];
     const bool v8 = (L0.D.nz % 8) == 0;
@@ -474,6 +647,7 @@ static int enqueue_first_half(flub_mg *mg, const LaunchCtx &c, int smoother) {
 
 // z = M r, beta, x += alpha p, p = z + beta p, it += 1.
 static int enqueue_second_half(flub_mg *mg, const LaunchCtx &c) {
+    if (mg->precision == FLUB_PRECISION_MIXED) return enqueue_second_half_mixed(mg, c);
     const unsigned b = red_blocks(mg->n);
     const Level &L0 = mg->lv[0];
     FLUB_TRY(enqueue_vcycle(mg, c, L0.r, L0.z, true));
@@ -602,7 +776,6 @@ int flub_mg_create(int nx, int ny, int nz, int levels, int precision, void *work
     FLUB_REQUIRE(out != nullptr, "flub_mg_create: out is NULL");
     *out = nullptr;
     FLUB_TRY(validate_shape(nx, ny, nz, levels, precision));
-    FLUB_REQUIRE(precision == FLUB_PRECISION_FP32, "precision %d not available in this build", precision);
     flub_mg *mg = new flub_mg;
     memset(mg, 0, sizeof(*mg));
     mg->nx = nx; mg->ny = ny; mg->nz = nz; mg->levels = levels; mg->precision = precision;
@@ -641,6 +814,18 @@ int flub_mg_create(int nx, int ny, int nz, int levels, int precision, void *work
     mg->skip_ok = true;  // the workspace is zeroed below and set_tags re-zeroes the z buffers
     choose_tail(mg);
     choose_cluster(mg);
+    if (precision == FLUB_PRECISION_MIXED) {
+        // the FP16 sweeps work on rows of 8 cells: every level left to the global
+        // kernels needs nz % 8 == 0
+        const int lt = mg->cl_start < mg->levels ? mg->cl_start : mg->tail_start;
+        const int last_global = lt < mg->levels ? lt - 1 : mg->levels - 1;
+        for (int l = 0; l <= last_global; l++)
+            if (mg->lv[l].D.nz % 8 != 0) {
+                flub_mg_destroy(mg);
+                set_last_error("mixed precision needs nz %% 8 == 0 on level %d (nz = %d)", l, nz >> l);
+                return FLUB_ERR_UNSUPPORTED;
+            }
+    }
     if (set_tail_smem_limit() != FLUB_OK) {
         flub_mg_destroy(mg);
         return FLUB_ERR_CUDA;
@@ -682,6 +867,8 @@ int flub_mg_set_tags(flub_mg *mg, const int32_t *tag, void *stream) {
         const size_t b = sizeof(float) * (size_t)mg->lv[l].D.n();
         FLUB_CHECK_CUDA(cudaMemsetAsync(mg->lv[l].z, 0, b, s));
         FLUB_CHECK_CUDA(cudaMemsetAsync(mg->lv[l].z2, 0, b, s));
+        if (mg->lv[l].zh) FLUB_CHECK_CUDA(cudaMemsetAsync(mg->lv[l].zh, 0, b / 2, s));
+        if (mg->lv[l].z2h) FLUB_CHECK_CUDA(cudaMemsetAsync(mg->lv[l].z2h, 0, b / 2, s));
     }
     FLUB_CHECK_CUDA(cudaMemsetAsync(mg->p, 0, sizeof(float) * (size_t)mg->n, s));
     FLUB_CHECK_CUDA(cudaMemsetAsync(mg->Ap, 0, sizeof(float) * (size_t)mg->n, s));
@@ -782,6 +969,11 @@ int flub_mg_get_x(flub_mg *mg, float *out, float scale, void *stream) {
 int flub_mg_apply_preconditioner(flub_mg *mg, const float *r, float *z, void *stream) {
     FLUB_REQUIRE(mg && r && z, "flub_mg_apply_preconditioner: NULL argument");
     LaunchCtx c{as_stream(stream), nullptr, 0, 0};
+    if (mg->precision == FLUB_PRECISION_MIXED) {
+        FLUB_TRY(launch_pdl(k8_to_half, dim3(blocks_for(mg->n / 8, 256)), dim3(256), 0, c.s, r, mg->lv[0].rh, mg->n,
+                            c.kc));
+        return enqueue_vcycle_mixed(mg, c, z, false);
+    }
     return enqueue_vcycle(mg, c, r, z, false);
 }
 

@@ -7,6 +7,7 @@
 #pragma once
 
 #include "mg_kernels.cuh"
+#include "store.cuh"
 
 namespace flub {
 
@@ -43,13 +44,20 @@ __device__ __forceinline__ uint8_t code_at(uint2 c, int m) {
     return (uint8_t)(((m < 4 ? c.x : c.y) >> (8 * (m & 3))) & 0xffu);
 }
 
-// z_eff[m] += zc[parent] for the 8 cells of a row whose coarse row starts at pc
-// (4 coarse values: cell m has parent m / 2).
-__device__ __forceinline__ void add_coarse_row8(Row8 &o, const float *__restrict__ pc) {
-    const float4 c = __ldg(reinterpret_cast<const float4 *>(pc));
-    const float cv[4] = {c.x, c.y, c.z, c.w};
+// z_eff[m] += scale * zc[parent] for the 8 cells of a row whose coarse row
+// starts at pc (4 coarse values: cell m has parent m / 2).  scale is 1 for FP32
+// levels and 8 between FP16 levels stored at 8^-l (exact powers of two).
+template <typename TC>
+__device__ __forceinline__ void add_coarse_row8(Row8 &o, const TC *__restrict__ pc, float scale) {
+    float cv[4];
+    St<TC>::ld4_ro(pc, cv);
 #pragma unroll
-    for (int m = 0; m < 8; m++) o.v[m] = __fadd_rn(o.v[m], cv[m >> 1]);
+    for (int m = 0; m < 8; m++) o.v[m] = __fadd_rn(o.v[m], __fmul_rn(cv[m >> 1], scale));
+}
+
+template <typename TC>
+__device__ __forceinline__ float coarse_at(const TC *__restrict__ p, float scale) {
+    return __fmul_rn(St<TC>::ld_ro(p), scale);
 }
 
 // One half-sweep over 8 cells per thread.
@@ -58,16 +66,19 @@ __device__ __forceinline__ void add_coarse_row8(Row8 &o, const float *__restrict
 //   kProlong:  the sweep reads zin + zc[I/2] (multigrid/mgpcg.py:113-116 fused
 //              into the first post-smoothing sweep) and writes every cell to
 //              zout != zin; otherwise zout == zin (in place).
+// TO/TI/TR/TC: storage of zout, zin, r and the coarse zc (float, or __half in
+// the mixed-precision V-cycle); arithmetic is FP32 throughout.
 // Every non-fluid cell is written as 0 (its value is never read by a fluid
 // cell's update, and the reference's sweeps leave it 0 by the end of the
 // V-cycle), so a buffer that starts at 0 keeps z = 0 off the fluid.  With
 // skip_inactive set the caller asserts that invariant for zout, and a thread
 // whose 8 cells hold no fluid cell returns without touching z or r.
 // Grid: x over k groups of 8, y over j, z over i.  Requires nz % 8 == 0.
-template <bool kFromZero, bool kProlong>
-__global__ void __launch_bounds__(256, 4) k_smooth8(float *zout, const float *zin, const float *__restrict__ zc,
-                                                    const float *__restrict__ r, const uint8_t *__restrict__ code,
-                                                    Dims D, int phase, int skip_inactive, unsigned long long *kc) {
+template <bool kFromZero, bool kProlong, typename TO, typename TI, typename TR, typename TC>
+__global__ void __launch_bounds__(256, 4) k_smooth8(TO *zout, const TI *zin, const TC *__restrict__ zc,
+                                                    float zc_scale, const TR *__restrict__ r,
+                                                    const uint8_t *__restrict__ code, Dims D, int phase,
+                                                    int skip_inactive, unsigned long long *kc) {
     count_kernel(kc);
     const int nz8 = D.nz >> 3;
     const int kg = blockIdx.x * blockDim.x + threadIdx.x;
@@ -93,30 +104,30 @@ __global__ void __launch_bounds__(256, 4) k_smooth8(float *zout, const float *zi
     const uint8_t ckp = hkp ? __ldg(code + c0 + 8) : (uint8_t)0;
 
     Row8 rr;
-    load_row8(r + c0, rr);
+    St<TR>::ld8_ro(r + c0, rr.v);
     Row8 zc0, zip, zim, zjp, zjm;
     float zkm = 0.0f, zkp = 0.0f;
     if (kFromZero) {
         zero_row8(zc0);
     } else {
-        load_row8_rw(zin + c0, zc0);
-        if (hip) load_row8_rw(zin + c0 + si, zip); else zero_row8(zip);
-        if (him) load_row8_rw(zin + c0 - si, zim); else zero_row8(zim);
-        if (hjp) load_row8_rw(zin + c0 + sj, zjp); else zero_row8(zjp);
-        if (hjm) load_row8_rw(zin + c0 - sj, zjm); else zero_row8(zjm);
-        if (hkm) zkm = zin[c0 - 1];
-        if (hkp) zkp = zin[c0 + 8];
+        St<TI>::ld8(zin + c0, zc0.v);
+        if (hip) St<TI>::ld8(zin + c0 + si, zip.v); else zero_row8(zip);
+        if (him) St<TI>::ld8(zin + c0 - si, zim.v); else zero_row8(zim);
+        if (hjp) St<TI>::ld8(zin + c0 + sj, zjp.v); else zero_row8(zjp);
+        if (hjm) St<TI>::ld8(zin + c0 - sj, zjm.v); else zero_row8(zjm);
+        if (hkm) zkm = St<TI>::ld(zin + c0 - 1);
+        if (hkp) zkp = St<TI>::ld(zin + c0 + 8);
         if (kProlong) {
             const int cy = D.ny >> 1, cz = D.nz >> 1;
             const int ci = i >> 1, cj = j >> 1, ck = k0 >> 1;
             const int cb = (ci * cy + cj) * cz + ck;
-            add_coarse_row8(zc0, zc + cb);
-            if (hip) add_coarse_row8(zip, zc + (((i + 1) >> 1) * cy + cj) * cz + ck);
-            if (him) add_coarse_row8(zim, zc + (((i - 1) >> 1) * cy + cj) * cz + ck);
-            if (hjp) add_coarse_row8(zjp, zc + (ci * cy + ((j + 1) >> 1)) * cz + ck);
-            if (hjm) add_coarse_row8(zjm, zc + (ci * cy + ((j - 1) >> 1)) * cz + ck);
-            if (hkm) zkm = __fadd_rn(zkm, __ldg(zc + cb - 1));
-            if (hkp) zkp = __fadd_rn(zkp, __ldg(zc + cb + 4));
+            add_coarse_row8(zc0, zc + cb, zc_scale);
+            if (hip) add_coarse_row8(zip, zc + (((i + 1) >> 1) * cy + cj) * cz + ck, zc_scale);
+            if (him) add_coarse_row8(zim, zc + (((i - 1) >> 1) * cy + cj) * cz + ck, zc_scale);
+            if (hjp) add_coarse_row8(zjp, zc + (ci * cy + ((j + 1) >> 1)) * cz + ck, zc_scale);
+            if (hjm) add_coarse_row8(zjm, zc + (ci * cy + ((j - 1) >> 1)) * cz + ck, zc_scale);
+            if (hkm) zkm = __fadd_rn(zkm, coarse_at(zc + cb - 1, zc_scale));
+            if (hkp) zkp = __fadd_rn(zkp, coarse_at(zc + cb + 4, zc_scale));
         }
     }
 
@@ -158,9 +169,7 @@ __global__ void __launch_bounds__(256, 4) k_smooth8(float *zout, const float *zi
         }
         out[m] = zn;
     }
-    float4 *o = reinterpret_cast<float4 *>(zout + c0);
-    o[0] = make_float4(out[0], out[1], out[2], out[3]);
-    o[1] = make_float4(out[4], out[5], out[6], out[7]);
+    St<TO>::st8(zout + c0, out);
 }
 
 }  // namespace flub

@@ -9,6 +9,8 @@
 // kernels, cell by cell, so the result is bit-identical.
 #pragma once
 
+#include <cuda_fp16.h>
+
 #include "mg_kernels.cuh"
 
 namespace flub {
@@ -29,6 +31,8 @@ struct TailParams {
     TailLevel lv[kTailMaxLevels];
     const float *r_top;  // restricted residual of the first tail level (global)
     float *z_top;        // its correction (global)
+    const __half *r_top_h;  // FP16 instead of r_top / z_top when not NULL (mixed precision)
+    __half *z_top_h;
 };
 
 // ---------------------------------------------------------------- lean smoothing
@@ -186,7 +190,10 @@ __global__ void __launch_bounds__(kTailThreads) k_tail_vcycle(const TailParams P
         const Dims D = P.lv[0].D;
         const int n = D.nx * D.ny * D.nz;
         float *r = R(0);
-        for (int q = threadIdx.x; q < n; q += blockDim.x) r[q] = P.r_top[q];
+        if (P.r_top_h)
+            for (int q = threadIdx.x; q < n; q += blockDim.x) r[q] = __half2float(P.r_top_h[q]);
+        else
+            for (int q = threadIdx.x; q < n; q += blockDim.x) r[q] = P.r_top[q];
     }
     __syncthreads();
     const int nb = P.nt - 1;
@@ -227,7 +234,10 @@ __global__ void __launch_bounds__(kTailThreads) k_tail_vcycle(const TailParams P
         const Dims D = P.lv[0].D;
         const int n = D.nx * D.ny * D.nz;
         const float *z = Z(0);
-        for (int q = threadIdx.x; q < n; q += blockDim.x) P.z_top[q] = z[q];
+        if (P.z_top_h)
+            for (int q = threadIdx.x; q < n; q += blockDim.x) P.z_top_h[q] = __float2half_rn(z[q]);
+        else
+            for (int q = threadIdx.x; q < n; q += blockDim.x) P.z_top[q] = z[q];
     }
 }
 
