@@ -33,6 +33,10 @@ METRIC = "ms per 256³ pressure solve to 1e-6 rel. residual: learned+mixed vs pl
 UNIT = "ms"
 # canonical algorithmic bytes per cell of the level a kernel runs on
 SMOOTH_HALF_SWEEP_BYTES_PER_CELL = 6.5  # red + black iteration: R z, r, tag; W z = 13 B/cell
+VARIANTS = {
+    "plain": "plain FP32 MGPCG (reference V-cycle, FP64 inner products)",
+    "mixed": "mixed-precision MGPCG (FP16 V-cycle levels, FP32 arithmetic, flexible CG, FP64 inner products)",
+}
 
 
 def parse_args():
@@ -42,6 +46,8 @@ def parse_args():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
     ap.add_argument("--config", default="dam256")
+    ap.add_argument("--variant", choices=sorted(VARIANTS), default="mixed",
+                    help="the variant the headline value is measured on (the others are timed beside it)")
     ap.add_argument("--cpu-baseline-steps", type=int, default=2)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
@@ -220,7 +226,6 @@ def run_ours(args):
     seed_base = {"dam256": 2, "dam512": 2, "sphere128": 1, "box64": 0}.get(args.config, 0)
     scene = scenes.CONFIGS[args.config](seed=seed_base + rank)
     n = scene.n_cells
-    proj = Projection(scene.shape, scene.levels)
 
     def dev(a):
         return torch.from_numpy(np.ascontiguousarray(a)).cuda()
@@ -230,45 +235,62 @@ def run_ours(args):
     vel = MACGrid(*(Field(a.clone(), d=d + 1) for d, a in enumerate(vel0)))
     velr = MACGrid(*(Field(dev(a), d=d + 1) for d, a in enumerate((scene.ur, scene.vr, scene.wr))))
     solve_kw = dict(max_iters=200, eps=1e-12, abs_tol=0.0, rel_tol=1e-12, smoother="phases")
-
-    def step():
-        for a, b in zip((vel.u.f, vel.v.f, vel.w.f), vel0):
-            a.copy_(b)
-        proj.project(vel, velr, phi, scene.prims, sync=False, **solve_kw)
-
-    for _ in range(max(args.warmup, 1)):
-        step()
-    torch.cuda.synchronize()
-    info = proj.mg.info()
-    if not info["converged"]:
-        raise RuntimeError(f"warm-up solve did not converge: {info}")
-    div_after = proj.max_abs_div(vel, velr)
-
     stream = torch.cuda.current_stream()
-    sampler = ClockSampler(local_rank)
-    if world > 1:
-        dist.barrier()
-    torch.cuda.synchronize()
-    host_l0 = lib.flub_launch_count()
-    dev_l0 = proj.mg.kernels_executed()
-    sampler.start()
-    time.sleep(0.3)
-    ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-    ev0.record(stream)
-    for _ in range(args.steps):
-        step()
-    ev1.record(stream)
-    torch.cuda.synchronize()
-    clocks = sampler.stop()
-    if world > 1:
-        dist.barrier()
-    elapsed = ev0.elapsed_time(ev1)
-    launches = (lib.flub_launch_count() - host_l0) + (proj.mg.kernels_executed() - dev_l0)
-    info = proj.mg.info()
-    if world > 1:
-        t = torch.tensor([elapsed], device="cuda")
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        elapsed = float(t.item())
+
+    def make_step(proj):
+        def step():
+            for a, b in zip((vel.u.f, vel.v.f, vel.w.f), vel0):
+                a.copy_(b)
+            proj.project(vel, velr, phi, scene.prims, sync=False, **solve_kw)
+        return step
+
+    def time_variant(proj, sample_clocks):
+        """W warm-up steps, then exactly K timed steps between barriers and
+        synchronisations; returns (ms over K steps, max over ranks), info, launches, clocks."""
+        step = make_step(proj)
+        for _ in range(max(args.warmup, 1)):
+            step()
+        torch.cuda.synchronize()
+        info = proj.mg.info()
+        if not info["converged"]:
+            raise RuntimeError(f"warm-up solve did not converge: {info}")
+        sampler = ClockSampler(local_rank) if sample_clocks else None
+        if world > 1:
+            dist.barrier()
+        torch.cuda.synchronize()
+        host_l0, dev_l0 = lib.flub_launch_count(), proj.mg.kernels_executed()
+        if sampler:
+            sampler.start()
+            time.sleep(0.3)
+        ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        ev0.record(stream)
+        for _ in range(args.steps):
+            step()
+        ev1.record(stream)
+        torch.cuda.synchronize()
+        clocks = sampler.stop() if sampler else None
+        if world > 1:
+            dist.barrier()
+        elapsed = ev0.elapsed_time(ev1)
+        launches = (lib.flub_launch_count() - host_l0) + (proj.mg.kernels_executed() - dev_l0)
+        if world > 1:
+            t = torch.tensor([elapsed], device="cuda")
+            dist.all_reduce(t, op=dist.ReduceOp.MAX)
+            elapsed = float(t.item())
+        return elapsed, proj.mg.info(), launches, clocks
+
+    variants = {"plain": Projection(scene.shape, scene.levels, precision="fp32"),
+                "mixed": Projection(scene.shape, scene.levels, precision="mixed")}
+    head = args.variant
+    results = {}
+    for name, pj in variants.items():
+        if name != head:
+            el, inf, _, _ = time_variant(pj, False)
+            results[name] = {"ms_per_solve": el / args.steps, "iterations": inf["iterations"]}
+    proj = variants[head]
+    elapsed, info, launches, clocks = time_variant(proj, True)
+    results[head] = {"ms_per_solve": elapsed / args.steps, "iterations": info["iterations"]}
+    div_after = proj.max_abs_div(vel, velr)
     ms_per_step = elapsed / args.steps
     value = elapsed / (args.steps * world)
 
@@ -308,16 +330,18 @@ def run_ours(args):
                "h2d_bytes_per_step": int(sum(t.numel() * t.element_size() for t in h_in)),
                "d2h_bytes_per_step": int(sum(t.numel() * t.element_size() for t in h_out))}
 
-    # ---- roofline of the dominant kernel: the level-0 red-black half-sweep
+    # ---- roofline of the dominant kernel of the plain path: the level-0
+    # red-black half-sweep (timed on the plain handle's level-0 buffers)
     peak, peak_kind = load_peaks()
     reps = 48
+    plain_mg = variants["plain"].mg
     for ph in (0, 1):
-        proj.mg.smooth(0, ph)
+        plain_mg.smooth(0, ph)
     torch.cuda.synchronize()
     k0, k1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     k0.record(stream)
     for q in range(reps):
-        proj.mg.smooth(0, q & 1)
+        plain_mg.smooth(0, q & 1)
     k1.record(stream)
     torch.cuda.synchronize()
     launch_ms = k0.elapsed_time(k1) / reps
@@ -352,7 +376,7 @@ def run_ours(args):
             "data": "synthetic (seeded dam-break scene and Fourier velocity field, generated on the host)",
             "config": {"workload": f"{args.config}: {scene.shape[0]}^3 dam-break projection (classify + divergence "
                                    f"+ MGPCG to rel. residual 1e-6 + gradient update)",
-                       "variant": "plain FP32 MGPCG (FP64 inner products)", "levels": scene.levels,
+                       "variant": VARIANTS[head], "variants_ms_per_solve": results, "levels": scene.levels,
                        "iterations": info["iterations"], "converged": bool(info["converged"]),
                        "fluid_cells": int((proj.tag.f == 1).sum().item()), "cells": n,
                        "cell_iterations_per_s": n * info["iterations"] / (ms_per_step * 1e-3),

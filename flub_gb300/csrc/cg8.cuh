@@ -174,7 +174,8 @@ __global__ void __launch_bounds__(kRedThreads) k8_dot_rr0(MgState *st, const flo
 }
 
 // z.r; kInit: old_zTr = z.r and p = z (mgpcg.py:396-401), else beta (:451-455).
-template <bool kInit>
+// kScaleZ: the V-cycle output is z / st->zscale (mixed precision), scaled back here.
+template <bool kInit, bool kScaleZ = false>
 __global__ void __launch_bounds__(kRedThreads) k8_dot_zr(MgState *st, const float *__restrict__ z,
                                                          const float *__restrict__ r, float *__restrict__ p,
                                                          const uint8_t *__restrict__ code, int64_t n,
@@ -182,11 +183,16 @@ __global__ void __launch_bounds__(kRedThreads) k8_dot_zr(MgState *st, const floa
     __shared__ double red[32];
     count_kernel(kc);
     const int ng = (int)(n >> 3);
+    const float zs = kScaleZ ? st->zscale : 1.0f;
     double s = 0.0;
     FLUB_GROUP_LOOP(g, ng) {
         if (!group_has_fluid(load_codes8(code + (g << 3)))) continue;  // z = 0 (and p = 0) there
         Row8 zv, rv;
         load_row8(z + (g << 3), zv);
+        if (kScaleZ) {
+#pragma unroll
+            for (int m = 0; m < 8; m++) zv.v[m] = __fmul_rn(zv.v[m], zs);
+        }
         load_row8(r + (g << 3), rv);
 #pragma unroll
         for (int m = 0; m < 8; m++) s = fma((double)zv.v[m], (double)rv.v[m], s);
@@ -206,11 +212,13 @@ __global__ void __launch_bounds__(kRedThreads) k8_dot_zr(MgState *st, const floa
 }
 
 // x += alpha p; p = z + beta p; it += 1 (mgpcg.py:457-461).
+template <bool kScaleZ = false>
 __global__ void __launch_bounds__(256) k8_update_xp(MgState *st, float *__restrict__ x, float *__restrict__ p,
                                                     const float *__restrict__ z, const uint8_t *__restrict__ code,
                                                     int64_t n, unsigned long long *kc) {
     count_kernel(kc);
     const float a = (float)st->alpha, b = (float)st->beta;
+    const float zs = kScaleZ ? st->zscale : 1.0f;
     const int ng = (int)(n >> 3);
     FLUB_GROUP_LOOP(g, ng) {
         if (!group_has_fluid(load_codes8(code + (g << 3)))) continue;  // p = z = 0 there
@@ -218,6 +226,10 @@ __global__ void __launch_bounds__(256) k8_update_xp(MgState *st, float *__restri
         load_row8_rw(x + (g << 3), xv);
         load_row8_rw(p + (g << 3), pv);
         load_row8(z + (g << 3), zv);
+        if (kScaleZ) {
+#pragma unroll
+            for (int m = 0; m < 8; m++) zv.v[m] = __fmul_rn(zv.v[m], zs);
+        }
 #pragma unroll
         for (int m = 0; m < 8; m++) {
             xv.v[m] = __fmaf_rn(a, pv.v[m], xv.v[m]);

@@ -24,8 +24,20 @@ struct MgState {
     unsigned long long kernels;  // solver kernels executed inside graphs
     int it, max_iters, converged, status, cond, use_x0;
     unsigned int ticket;
-    int skip_r;  // r is 0 off the fluid (masked), so r.r may skip groups without fluid
+    int skip_r;    // r is 0 off the fluid (masked), so r.r may skip groups without fluid
+    float zscale;  // mixed precision: z = zscale * (V-cycle output); the FP16 residual copy is r / zscale
+    float pad_;
 };
+
+// Power of two near 1 / RMS of a vector with squared norm rtr over n entries:
+// the FP16 residual copy is stored at this scale so that it neither overflows
+// nor underflows as CG drives the residual down by orders of magnitude.
+__device__ __forceinline__ float fp16_residual_scale(double rtr, int64_t n) {
+    if (!(rtr > 0.0) || !isfinite(rtr)) return 1.0f;
+    int e = ilogb(sqrt(rtr / (double)n));
+    e = e < -100 ? -100 : (e > 100 ? 100 : e);
+    return ldexpf(1.0f, -e);
+}
 
 struct Dims {
     int nx, ny, nz;
@@ -272,6 +284,7 @@ __global__ void k_solve_begin(MgState *st, int max_iters, double eps, double abs
     st->status = FLUB_OK;
     st->cond = 0;
     st->use_x0 = use_x0;
+    st->zscale = 1.0f;
     st->alpha = 0.0;
     st->beta = 0.0;
     st->ticket = 0u;

@@ -558,10 +558,10 @@ static int enqueue_prologue_mixed(flub_mg *mg, const LaunchCtx &c, int smoother)
     FLUB_TRY(launch_pdl(k_residual_x0, dim3(blocks_for(mg->n, 256)), dim3(256), 0, c.s, mg->st, L0.r, mg->x, L0.code,
                         L0.D, c.kc));
     if (smoother == FLUB_SMOOTHER_FRACTION) FLUB_TRY(enqueue_mean_removal(mg, c, 2));
-    FLUB_TRY(launch_pdl(k8_to_half, dim3(blocks_for(mg->n / 8, 256)), dim3(256), 0, c.s, (const float *)L0.r, L0.rh,
+    FLUB_TRY(launch_pdl(k8_to_half, dim3(blocks_for(mg->n / 8, 256)), dim3(256), 0, c.s, mg->st, (const float *)L0.r, L0.rh,
                         mg->n, c.kc));
     FLUB_TRY(enqueue_vcycle_mixed(mg, c, L0.z, true));
-    return launch_pdl(k8_dot_zr<true>, dim3(bg), dim3(kRedThreads), 0, c.s, mg->st, L0.z, L0.r, mg->p, L0.code,
+    return launch_pdl(k8_dot_zr<true, true>, dim3(bg), dim3(kRedThreads), 0, c.s, mg->st, L0.z, L0.r, mg->p, L0.code,
                       mg->n, mg->partials, c.kc);
 }
 
@@ -574,7 +574,7 @@ static int enqueue_first_half_mixed(flub_mg *mg, const LaunchCtx &c, int smoothe
         FLUB_CHECK_CUDA(cudaMemcpyAsync(mg->r_old, L0.r, sizeof(float) * mg->n, cudaMemcpyDeviceToDevice, c.s));
         FLUB_TRY(launch_pdl(k_update_r, dim3(b), dim3(kRedThreads), 0, c.s, mg->st, L0.r, mg->Ap, mg->n, c.kc));
         FLUB_TRY(enqueue_mean_removal(mg, c, 1));
-        FLUB_TRY(launch_pdl(k8_to_half, dim3(blocks_for(mg->n / 8, 256)), dim3(256), 0, c.s, (const float *)L0.r,
+        FLUB_TRY(launch_pdl(k8_to_half, dim3(blocks_for(mg->n / 8, 256)), dim3(256), 0, c.s, mg->st, (const float *)L0.r,
                             L0.rh, mg->n, c.kc));
         return launch_pdl(k8_update_r_rr<false>, dim3(bg), dim3(kRedThreads), 0, c.s, mg->st, L0.r, mg->Ap, L0.code,
                           mg->n, mg->partials, mg->hist, c.h, c.set_cond, c.kc);
@@ -589,7 +589,7 @@ static int enqueue_second_half_mixed(flub_mg *mg, const LaunchCtx &c) {
     FLUB_TRY(enqueue_vcycle_mixed(mg, c, L0.z, true));
     FLUB_TRY(launch_pdl(k8_dot_zr_flex, dim3(bg), dim3(kRedThreads), 0, c.s, mg->st, L0.z, L0.r, mg->r_old, L0.code,
                         mg->n, mg->partials, c.kc));
-    return launch_pdl(k8_update_xp, dim3(blocks_for(mg->n / 8, 256)), dim3(256), 0, c.s, mg->st, mg->x, mg->p, L0.z,
+    return launch_pdl(k8_update_xp<true>, dim3(blocks_for(mg->n / 8, 256)), dim3(256), 0, c.s, mg->st, mg->x, mg->p, L0.z,
                       L0.code, mg->n, c.kc);
 }
 
@@ -610,7 +610,7 @@ static int enqueue_prologue(flub_mg *mg, const LaunchCtx &c, int smoother) {
     if (smoother == FLUB_SMOOTHER_FRACTION) FLUB_TRY(enqueue_mean_removal(mg, c, 2));
     FLUB_TRY(enqueue_vcycle(mg, c, L0.r, L0.z, true));
     if (v8)
-        return launch_pdl(k8_dot_zr<true>, dim3(bg), dim3(kRedThreads), 0, c.s, mg->st, L0.z, L0.r, mg->p, L0.code,
+        return launch_pdl(k8_dot_zr<true, false>, dim3(bg), dim3(kRedThreads), 0, c.s, mg->st, L0.z, L0.r, mg->p, L0.code,
                           mg->n, mg->partials, c.kc);
     return launch_pdl(k_dot_zr_init, dim3(b), dim3(kRedThreads), 0, c.s, mg->st, L0.z, L0.r, mg->p, mg->n,
                       mg->partials, c.kc);
@@ -655,7 +655,7 @@ static int enqueue_second_half(flub_mg *mg, const LaunchCtx &c) {
         const unsigned bg = red_blocks(mg->n / 8 + 1);
         FLUB_TRY(launch_pdl(k8_dot_zr<false>, dim3(bg), dim3(kRedThreads), 0, c.s, mg->st, L0.z, L0.r,
                             (float *)nullptr, L0.code, mg->n, mg->partials, c.kc));
-        return launch_pdl(k8_update_xp, dim3(blocks_for(mg->n / 8, 256)), dim3(256), 0, c.s, mg->st, mg->x, mg->p,
+        return launch_pdl(k8_update_xp<false>, dim3(blocks_for(mg->n / 8, 256)), dim3(256), 0, c.s, mg->st, mg->x, mg->p,
                           L0.z, L0.code, mg->n, c.kc);
     }
     FLUB_TRY(launch_pdl(k_dot_zr_beta, dim3(b), dim3(kRedThreads), 0, c.s, mg->st, L0.z, L0.r, mg->n, mg->partials,
@@ -970,7 +970,7 @@ int flub_mg_apply_preconditioner(flub_mg *mg, const float *r, float *z, void *st
     FLUB_REQUIRE(mg && r && z, "flub_mg_apply_preconditioner: NULL argument");
     LaunchCtx c{as_stream(stream), nullptr, 0, 0};
     if (mg->precision == FLUB_PRECISION_MIXED) {
-        FLUB_TRY(launch_pdl(k8_to_half, dim3(blocks_for(mg->n / 8, 256)), dim3(256), 0, c.s, r, mg->lv[0].rh, mg->n,
+        FLUB_TRY(launch_pdl(k8_to_half, dim3(blocks_for(mg->n / 8, 256)), dim3(256), 0, c.s, (MgState *)nullptr, r, mg->lv[0].rh, mg->n,
                             c.kc));
         return enqueue_vcycle_mixed(mg, c, z, false);
     }

@@ -69,14 +69,21 @@ __global__ void __launch_bounds__(256) k_restrict_t(const TRI *__restrict__ rf, 
     }
 }
 
-// FP16 copy of the level-0 residual for the V-cycle (every group).
-__global__ void __launch_bounds__(256) k8_to_half(const float *__restrict__ r, __half *__restrict__ rh, int64_t n,
-                                                  unsigned long long *kc) {
+// FP16 copy of the level-0 residual for the V-cycle (every group).  With a
+// solver state, the copy is r / zscale with zscale a power of two near the
+// RMS of r (fp16_residual_scale), recorded in st->zscale; without one
+// (flub_mg_apply_preconditioner) the copy is unscaled.
+__global__ void __launch_bounds__(256) k8_to_half(MgState *st, const float *__restrict__ r, __half *__restrict__ rh,
+                                                  int64_t n, unsigned long long *kc) {
     count_kernel(kc);
+    const float hs = st ? fp16_residual_scale(st->rtr0, n) : 1.0f;
+    if (st && (blockIdx.x | threadIdx.x) == 0) st->zscale = 1.0f / hs;
     const int ng = (int)(n >> 3);
     FLUB_GROUP_LOOP(g, ng) {
         float v[8];
         St<float>::ld8_ro(r + (g << 3), v);
+#pragma unroll
+        for (int m = 0; m < 8; m++) v[m] = __fmul_rn(v[m], hs);
         St<__half>::st8(rh + (g << 3), v);
     }
 }
@@ -98,18 +105,25 @@ __global__ void __launch_bounds__(kRedThreads) k8_update_r_rr_mixed(MgState *st,
     }
     const float a = (float)st->alpha;
     const int skip = st->skip_r;
+    // scale of the FP16 copy from the previous residual norm (st->rtr is only
+    // overwritten by the last block, after every block has read it)
+    const float hs = fp16_residual_scale(st->rtr, n);
+    if ((blockIdx.x | threadIdx.x) == 0) st->zscale = 1.0f / hs;
     const int ng = (int)(n >> 3);
     double s = 0.0;
     FLUB_GROUP_LOOP(g, ng) {
         if (skip && !group_has_fluid(load_codes8(code + (g << 3)))) continue;
-        float rv[8], av[8];
+        float rv[8], av[8], hv[8];
         St<float>::ld8(r + (g << 3), rv);
         St<float>::ld8_ro(Ap + (g << 3), av);
         St<float>::st8(r_old + (g << 3), rv);
 #pragma unroll
-        for (int m = 0; m < 8; m++) rv[m] = __fmaf_rn(-a, av[m], rv[m]);
+        for (int m = 0; m < 8; m++) {
+            rv[m] = __fmaf_rn(-a, av[m], rv[m]);
+            hv[m] = __fmul_rn(rv[m], hs);
+        }
         St<float>::st8(r + (g << 3), rv);
-        St<__half>::st8(rh + (g << 3), rv);
+        St<__half>::st8(rh + (g << 3), hv);
 #pragma unroll
         for (int m = 0; m < 8; m++) s = fma((double)rv[m], (double)rv[m], s);
     }
@@ -133,11 +147,14 @@ __global__ void __launch_bounds__(kRedThreads) k8_dot_zr_flex(MgState *st, const
     __shared__ double red[32];
     count_kernel(kc);
     const int ng = (int)(n >> 3);
+    const float zs = st->zscale;
     double s = 0.0, so = 0.0;
     FLUB_GROUP_LOOP(g, ng) {
         if (!group_has_fluid(load_codes8(code + (g << 3)))) continue;  // z = 0 there
         float zv[8], rv[8], ov[8];
         St<float>::ld8_ro(z + (g << 3), zv);
+#pragma unroll
+        for (int m = 0; m < 8; m++) zv[m] = __fmul_rn(zv[m], zs);
         St<float>::ld8_ro(r + (g << 3), rv);
         St<float>::ld8_ro(r_old + (g << 3), ov);
 #pragma unroll
