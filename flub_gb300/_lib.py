@@ -73,6 +73,20 @@ SIGNATURES = {
     "flub_vcycle_noalloc": (_i32, [_vp, _vp, _vp, _i32, _i32, _i32, _i32, _vp]),
     "flub_launch_count": (_i64, []),
     "flub_reset_launch_count": (None, []),
+    "flub_conv3d_bf16": (_i32, [_vp, _i32, _vp, _vp, _i32, _vp, _vp, _vp, _i32, _i32, _i32, _i32, _i32, _i32, _vp]),
+    "flub_conv3d_wgrad": (_i32, [_vp, _i32, _vp, _i32, _vp, _vp, _i32, _i32, _i32, _i32, _vp]),
+    "flub_conv_error": (_i32, [ctypes.POINTER(_i32), _i32]),
+    "flub_unet_input": (_i32, [_vp, _vp, _i32, _i64, _vp, _vp, _vp]),
+    "flub_pool2_bf16": (_i32, [_vp, _vp, _i32, _i32, _i32, _i32, _i32, _vp]),
+    "flub_pool2_bwd_bf16": (_i32, [_vp, _vp, _i32, _i32, _i32, _i32, _i32, _i32, _vp]),
+    "flub_up2_bf16": (_i32, [_vp, _vp, _i32, _i32, _i32, _i32, _i32, _vp]),
+    "flub_up2_bwd_bf16": (_i32, [_vp, _vp, _i32, _i32, _i32, _i32, _i32, _vp]),
+    "flub_relu_bwd_bf16": (_i32, [_vp, _vp, _vp, _i64, _vp]),
+    "flub_head_fwd": (_i32, [_vp, _vp, _vp, _vp, _i64, _vp]),
+    "flub_head_bwd": (_i32, [_vp, _vp, _vp, _vp, _vp, _vp, _i64, _vp]),
+    "flub_unet_loss": (_i32, [_vp, _vp, _vp, _vp, _i64, _i32, _f64, _vp, _vp, _vp]),
+    "flub_unet_output": (_i32, [_vp, _vp, _vp, _i64, _i32, _f32, _vp, _vp]),
+    "flub_adam": (_i32, [_vp, _vp, _vp, _vp, _i64, _f32, _f32, _f32, _f32, _i32, _vp, _vp, _i32, _i32, _vp]),
 }
 
 

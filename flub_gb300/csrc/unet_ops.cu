@@ -1,0 +1,441 @@
+// U-Net pieces around the tcgen05 convolution (unet_conv.cu): input assembly,
+// 2x pooling / upsampling and their gradients, ReLU gradient, the 1x1x1 output
+// head, the masked MSE loss, the convolution weight gradient, and Adam.
+//
+// No reference counterpart: the learned warm start is an addition to the
+// projection (the reference always starts CG from x = 0).  Activations are
+// channels-last BF16 [B][X][Y][Z][C]; parameters, gradients and optimiser
+// state are FP32.
+#include <cuda_bf16.h>
+
+#include "common.cuh"
+
+namespace flub {
+
+#define GRID_LOOP(i, n) for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < (n); i += (int64_t)gridDim.x * blockDim.x)
+
+__device__ __forceinline__ float bf(const __nv_bfloat16 v) { return __bfloat162float(v); }
+
+// Per-sample 1 / RMS of the right-hand side over fluid cells (1 if none).
+__global__ void __launch_bounds__(256) k_unet_rms(const float *__restrict__ div, const int32_t *__restrict__ tag,
+                                                  int64_t ncell, float *__restrict__ inv_scale) {
+    __shared__ double red[32], cnt_red[32];
+    const int b = blockIdx.x;
+    double s = 0.0, c = 0.0;
+    for (int64_t q = threadIdx.x; q < ncell; q += blockDim.x) {
+        const int64_t v = b * ncell + q;
+        if (tag[v] == 1) {
+            const double d = div[v];
+            s += d * d;
+            c += 1.0;
+        }
+    }
+    s = block_sum(s, red);
+    c = block_sum(c, cnt_red);
+    if (threadIdx.x == 0) inv_scale[b] = (c > 0.0 && s > 0.0) ? (float)(1.0 / sqrt(s / c)) : 1.0f;
+}
+
+// Network input, 16 channels: div / rms, fluid mask, solid mask, 13 zeros.
+__global__ void __launch_bounds__(256) k_unet_input(const float *__restrict__ div, const int32_t *__restrict__ tag,
+                                                    const float *__restrict__ inv_scale, int64_t ncell, int64_t n,
+                                                    __nv_bfloat16 *__restrict__ out) {
+    GRID_LOOP(v, n) {
+        const int b = (int)(v / ncell);
+        const int t = tag[v];
+        __align__(16) __nv_bfloat16 ch[16];
+#pragma unroll
+        for (int c = 0; c < 16; c++) ch[c] = __float2bfloat16_rn(0.0f);
+        ch[0] = __float2bfloat16_rn(t == 1 ? div[v] * inv_scale[b] : 0.0f);
+        ch[1] = __float2bfloat16_rn(t == 1 ? 1.0f : 0.0f);
+        ch[2] = __float2bfloat16_rn(t == 2 ? 1.0f : 0.0f);
+        uint4 *dst = reinterpret_cast<uint4 *>(out + v * 16);
+        dst[0] = reinterpret_cast<const uint4 *>(ch)[0];
+        dst[1] = reinterpret_cast<const uint4 *>(ch)[1];
+    }
+}
+
+// 2x average pool (fine -> coarse), C channels.
+__global__ void __launch_bounds__(256) k_pool2(const __nv_bfloat16 *__restrict__ x, __nv_bfloat16 *__restrict__ y,
+                                               int B, int NX, int NY, int NZ, int C) {
+    const int cx = NX / 2, cy = NY / 2, cz = NZ / 2;
+    const int64_t n = (int64_t)B * cx * cy * cz * C;
+    GRID_LOOP(q, n) {
+        const int c = (int)(q % C);
+        int64_t v = q / C;
+        const int k = (int)(v % cz); v /= cz;
+        const int j = (int)(v % cy); v /= cy;
+        const int i = (int)(v % cx);
+        const int b = (int)(v / cx);
+        float s = 0.0f;
+        for (int d = 0; d < 8; d++) {
+            const int64_t f = ((((int64_t)b * NX + 2 * i + (d >> 2)) * NY + 2 * j + ((d >> 1) & 1)) * NZ + 2 * k + (d & 1));
+            s += bf(x[f * C + c]);
+        }
+        y[q] = __float2bfloat16_rn(s * 0.125f);
+    }
+}
+
+// Gradient of the pool: dx (+)= dy / 8.
+__global__ void __launch_bounds__(256) k_pool2_bwd(const __nv_bfloat16 *__restrict__ dy, __nv_bfloat16 *dx, int B,
+                                                   int NX, int NY, int NZ, int C, int accumulate) {
+    const int64_t n = (int64_t)B * NX * NY * NZ * C;
+    GRID_LOOP(q, n) {
+        const int c = (int)(q % C);
+        int64_t v = q / C;
+        const int k = (int)(v % NZ); v /= NZ;
+        const int j = (int)(v % NY); v /= NY;
+        const int i = (int)(v % NX);
+        const int b = (int)(v / NX);
+        const int64_t cv = (((int64_t)b * (NX / 2) + i / 2) * (NY / 2) + j / 2) * (NZ / 2) + k / 2;
+        float g = bf(dy[cv * C + c]) * 0.125f;
+        if (accumulate) g += bf(dx[q]);
+        dx[q] = __float2bfloat16_rn(g);
+    }
+}
+
+// Nearest upsample (coarse -> fine).
+__global__ void __launch_bounds__(256) k_up2(const __nv_bfloat16 *__restrict__ x, __nv_bfloat16 *__restrict__ y, int B,
+                                             int NX, int NY, int NZ, int C) {
+    const int64_t n = (int64_t)B * NX * NY * NZ * C;
+    GRID_LOOP(q, n) {
+        const int c = (int)(q % C);
+        int64_t v = q / C;
+        const int k = (int)(v % NZ); v /= NZ;
+        const int j = (int)(v % NY); v /= NY;
+        const int i = (int)(v % NX);
+        const int b = (int)(v / NX);
+        const int64_t cv = (((int64_t)b * (NX / 2) + i / 2) * (NY / 2) + j / 2) * (NZ / 2) + k / 2;
+        y[q] = x[cv * C + c];
+    }
+}
+
+// Gradient of the upsample: dx_coarse = sum of the 8 fine gradients.
+__global__ void __launch_bounds__(256) k_up2_bwd(const __nv_bfloat16 *__restrict__ dy, __nv_bfloat16 *__restrict__ dx,
+                                                 int B, int NX, int NY, int NZ, int C) {
+    const int cx = NX / 2, cy = NY / 2, cz = NZ / 2;
+    const int64_t n = (int64_t)B * cx * cy * cz * C;
+    GRID_LOOP(q, n) {
+        const int c = (int)(q % C);
+        int64_t v = q / C;
+        const int k = (int)(v % cz); v /= cz;
+        const int j = (int)(v % cy); v /= cy;
+        const int i = (int)(v % cx);
+        const int b = (int)(v / cx);
+        float s = 0.0f;
+        for (int d = 0; d < 8; d++) {
+            const int64_t f = ((((int64_t)b * NX + 2 * i + (d >> 2)) * NY + 2 * j + ((d >> 1) & 1)) * NZ + 2 * k + (d & 1));
+            s += bf(dy[f * C + c]);
+        }
+        dx[q] = __float2bfloat16_rn(s);
+    }
+}
+
+// dx = dy where the ReLU output y > 0, else 0 (dx may alias dy).
+__global__ void __launch_bounds__(256) k_relu_bwd(const __nv_bfloat16 *dy, const __nv_bfloat16 *__restrict__ y,
+                                                  __nv_bfloat16 *dx, int64_t n) {
+    GRID_LOOP(q, n) dx[q] = bf(y[q]) > 0.0f ? dy[q] : __float2bfloat16_rn(0.0f);
+}
+
+// 1x1x1 head: out[v] = sum_c w[c] x[v][c] + b, 16 channels, FP32 out.
+__global__ void __launch_bounds__(256) k_head_fwd(const __nv_bfloat16 *__restrict__ x, const float *__restrict__ w,
+                                                  const float *__restrict__ bias, float *__restrict__ out, int64_t n) {
+    GRID_LOOP(v, n) {
+        float s = bias[0];
+#pragma unroll
+        for (int c = 0; c < 16; c++) s = fmaf(w[c], bf(x[v * 16 + c]), s);
+        out[v] = s;
+    }
+}
+
+// Head gradients: dx[v][c] = dout[v] w[c]; dw[c] += sum_v dout[v] x[v][c]; db += sum dout.
+__global__ void __launch_bounds__(256) k_head_bwd(const __nv_bfloat16 *__restrict__ x, const float *__restrict__ w,
+                                                  const float *__restrict__ dout, __nv_bfloat16 *__restrict__ dx,
+                                                  float *__restrict__ dw, float *__restrict__ db, int64_t n) {
+    __shared__ double red[32];
+    float acc[17];
+#pragma unroll
+    for (int c = 0; c < 17; c++) acc[c] = 0.0f;
+    GRID_LOOP(v, n) {
+        const float g = dout[v];
+#pragma unroll
+        for (int c = 0; c < 16; c++) {
+            acc[c] = fmaf(g, bf(x[v * 16 + c]), acc[c]);
+            dx[v * 16 + c] = __float2bfloat16_rn(g * w[c]);
+        }
+        acc[16] += g;
+    }
+    for (int c = 0; c < 17; c++) {
+        const double t = block_sum((double)acc[c], red);
+        if (threadIdx.x == 0) atomicAdd(c < 16 ? dw + c : db, (float)t);
+    }
+}
+
+// Masked MSE on fluid cells in normalised units: target = x * inv_scale[b].
+// loss (FP64 sum, mean over fluid cells of the batch) and dpred.
+__global__ void __launch_bounds__(256) k_unet_loss(const float *__restrict__ pred, const float *__restrict__ x,
+                                                   const int32_t *__restrict__ tag, const float *__restrict__ inv_scale,
+                                                   int64_t ncell, int64_t n, double inv_count,
+                                                   float *__restrict__ dpred, double *__restrict__ loss) {
+    __shared__ double red[32];
+    double s = 0.0;
+    GRID_LOOP(v, n) {
+        float g = 0.0f;
+        if (tag[v] == 1) {
+            const float d = pred[v] - x[v] * inv_scale[v / ncell];
+            s += (double)d * d;
+            g = (float)(2.0 * inv_count) * d;
+        }
+        dpred[v] = g;
+    }
+    s = block_sum(s, red);
+    if (threadIdx.x == 0) atomicAdd(loss, s * inv_count);
+}
+
+// Network output (normalised) -> pressure guess: x0 = out / inv_scale * gain on
+// fluid cells, 0 elsewhere.
+__global__ void __launch_bounds__(256) k_unet_output(const float *__restrict__ out, const int32_t *__restrict__ tag,
+                                                     const float *__restrict__ inv_scale, int64_t ncell, int64_t n,
+                                                     float gain, float *__restrict__ x0) {
+    GRID_LOOP(v, n) x0[v] = tag[v] == 1 ? out[v] / inv_scale[v / ncell] * gain : 0.0f;
+}
+
+// Weight gradient of a 3x3x3 convolution (CUDA cores):
+//   dW[tap][co][ci] += sum_v dY[v][co] X[v + tap][ci],  dB[co] += sum_v dY[v][co]
+// Block = (chunk set, tap).  Each block walks chunks of 64 voxels, stages dY
+// and the tap-shifted X (zero outside the volume) in shared memory, and each
+// thread accumulates a 4 x 4 tile of (co, ci) over its share of the voxels.
+constexpr int kWgChunk = 64;
+
+__global__ void __launch_bounds__(256) k_conv_wgrad(const __nv_bfloat16 *__restrict__ x, int cin,
+                                                    const __nv_bfloat16 *__restrict__ dy, int cout, float *dw,
+                                                    float *db, int B, int NX, int NY, int NZ) {
+    __shared__ float sm[2 * kWgChunk * 64];
+    float *sy = sm, *sx = sm + kWgChunk * 64;
+    const int tap = blockIdx.y;
+    const int dx_ = tap / 9 - 1, dy_ = (tap / 3) % 3 - 1, dz_ = tap % 3 - 1;
+    const int64_t nvox = (int64_t)B * NX * NY * NZ;
+    const int64_t nchunk = (nvox + kWgChunk - 1) / kWgChunk;
+    const int tco = cout / 4, tci = cin / 4, ntile = tco * tci;
+    const int vsplit = 256 / ntile;  // ntile in {16, 32, 64, 128, 256}
+    const int tile = threadIdx.x % ntile, vpart = threadIdx.x / ntile;
+    const int co0 = (tile / tci) * 4, ci0 = (tile % tci) * 4;
+    float acc[4][4];
+    float accb[4];
+#pragma unroll
+    for (int a = 0; a < 4; a++) {
+        accb[a] = 0.0f;
+#pragma unroll
+        for (int c = 0; c < 4; c++) acc[a][c] = 0.0f;
+    }
+    for (int64_t ch = blockIdx.x; ch < nchunk; ch += gridDim.x) {
+        const int64_t v0 = ch * kWgChunk;
+        for (int q = threadIdx.x; q < kWgChunk * cout; q += blockDim.x) {
+            const int64_t v = v0 + q / cout;
+            sy[q] = v < nvox ? bf(dy[v * cout + q % cout]) : 0.0f;
+        }
+        for (int q = threadIdx.x; q < kWgChunk * cin; q += blockDim.x) {
+            const int64_t v = v0 + q / cin;
+            float val = 0.0f;
+            if (v < nvox) {
+                int64_t t = v;
+                const int k = (int)(t % NZ); t /= NZ;
+                const int j = (int)(t % NY); t /= NY;
+                const int i = (int)(t % NX);
+                const int b = (int)(t / NX);
+                const int ii = i + dx_, jj = j + dy_, kk = k + dz_;
+                if (ii >= 0 && ii < NX && jj >= 0 && jj < NY && kk >= 0 && kk < NZ)
+                    val = bf(x[((((int64_t)b * NX + ii) * NY + jj) * NZ + kk) * cin + q % cin]);
+            }
+            sx[q] = val;
+        }
+        __syncthreads();
+        for (int m = vpart; m < kWgChunk; m += vsplit) {
+            float yv[4], xv[4];
+#pragma unroll
+            for (int a = 0; a < 4; a++) yv[a] = sy[m * cout + co0 + a];
+#pragma unroll
+            for (int c = 0; c < 4; c++) xv[c] = sx[m * cin + ci0 + c];
+#pragma unroll
+            for (int a = 0; a < 4; a++) {
+                accb[a] += yv[a];
+#pragma unroll
+                for (int c = 0; c < 4; c++) acc[a][c] = fmaf(yv[a], xv[c], acc[a][c]);
+            }
+        }
+        __syncthreads();
+    }
+    // combine the vsplit partial tiles in shared memory, then one atomic per entry
+    float *red = sm;  // reuse: ntile * 20 floats (16 weights + 4 bias) <= 2 * kWgChunk * 64
+    const int per = 20;
+    for (int part = 0; part < vsplit; part++) {
+        if (vpart == part) {
+#pragma unroll
+            for (int a = 0; a < 4; a++) {
+#pragma unroll
+                for (int c = 0; c < 4; c++) {
+                    float *dst = &red[tile * per + a * 4 + c];
+                    *dst = part == 0 ? acc[a][c] : *dst + acc[a][c];
+                }
+                float *dst = &red[tile * per + 16 + a];
+                *dst = part == 0 ? accb[a] : *dst + accb[a];
+            }
+        }
+        __syncthreads();
+    }
+    if (vpart == 0) {
+#pragma unroll
+        for (int a = 0; a < 4; a++) {
+#pragma unroll
+            for (int c = 0; c < 4; c++)
+                atomicAdd(&dw[((int64_t)tap * cout + co0 + a) * cin + ci0 + c], red[tile * per + a * 4 + c]);
+            if (db && tap == 13 && ci0 == 0) atomicAdd(&db[co0 + a], red[tile * per + 16 + a]);
+        }
+    }
+}
+
+// Adam (decoupled weight decay off) on FP32 masters; optionally writes the BF16
+// weights [27][cout][cin] and the flipped, transposed BF16 copy
+// [27][cin][cout] (tap 26 - t) used by the data gradient.
+__global__ void __launch_bounds__(256) k_adam(float *__restrict__ p, const float *__restrict__ g, float *__restrict__ m,
+                                              float *__restrict__ v, int64_t n, float lr, float b1, float b2,
+                                              float eps, float c1, float c2, __nv_bfloat16 *__restrict__ w16,
+                                              __nv_bfloat16 *__restrict__ w16t, int cout, int cin) {
+    GRID_LOOP(q, n) {
+        const float gq = g[q];
+        const float mq = b1 * m[q] + (1.0f - b1) * gq;
+        const float vq = b2 * v[q] + (1.0f - b2) * gq * gq;
+        m[q] = mq;
+        v[q] = vq;
+        const float pq = p[q] - lr * (mq * c1) / (sqrtf(vq * c2) + eps);
+        p[q] = pq;
+        if (w16) {
+            const int64_t tap = q / ((int64_t)cout * cin);
+            const int co = (int)((q / cin) % cout), ci = (int)(q % cin);
+            w16[q] = __float2bfloat16_rn(pq);
+            w16t[((26 - tap) * cin + ci) * cout + co] = __float2bfloat16_rn(pq);
+        }
+    }
+}
+
+}  // namespace flub
+
+using namespace flub;
+
+static inline unsigned nb(int64_t n) { return blocks_for(n, 256, 152 * 16); }
+
+extern "C" {
+
+int flub_unet_input(const float *div, const int32_t *tag, int B, int64_t ncell, float *inv_scale, void *out,
+                    void *stream) {
+    FLUB_REQUIRE(div && tag && inv_scale && out && B > 0 && ncell > 0, "flub_unet_input: bad arguments");
+    cudaStream_t s = as_stream(stream);
+    k_unet_rms<<<B, 256, 0, s>>>(div, tag, ncell, inv_scale);
+    FLUB_CHECK_LAUNCH();
+    const int64_t n = (int64_t)B * ncell;
+    k_unet_input<<<nb(n), 256, 0, s>>>(div, tag, inv_scale, ncell, n, static_cast<__nv_bfloat16 *>(out));
+    FLUB_CHECK_LAUNCH();
+    return FLUB_OK;
+}
+
+int flub_pool2_bf16(const void *x, void *y, int B, int NX, int NY, int NZ, int C, void *stream) {
+    FLUB_REQUIRE(x && y && NX % 2 == 0 && NY % 2 == 0 && NZ % 2 == 0, "flub_pool2_bf16: bad arguments");
+    k_pool2<<<nb((int64_t)B * NX * NY * NZ * C / 8), 256, 0, as_stream(stream)>>>(
+        static_cast<const __nv_bfloat16 *>(x), static_cast<__nv_bfloat16 *>(y), B, NX, NY, NZ, C);
+    FLUB_CHECK_LAUNCH();
+    return FLUB_OK;
+}
+
+int flub_pool2_bwd_bf16(const void *dy, void *dx, int B, int NX, int NY, int NZ, int C, int accumulate, void *stream) {
+    FLUB_REQUIRE(dy && dx, "flub_pool2_bwd_bf16: bad arguments");
+    k_pool2_bwd<<<nb((int64_t)B * NX * NY * NZ * C), 256, 0, as_stream(stream)>>>(
+        static_cast<const __nv_bfloat16 *>(dy), static_cast<__nv_bfloat16 *>(dx), B, NX, NY, NZ, C, accumulate);
+    FLUB_CHECK_LAUNCH();
+    return FLUB_OK;
+}
+
+int flub_up2_bf16(const void *x, void *y, int B, int NX, int NY, int NZ, int C, void *stream) {
+    FLUB_REQUIRE(x && y, "flub_up2_bf16: bad arguments");
+    k_up2<<<nb((int64_t)B * NX * NY * NZ * C), 256, 0, as_stream(stream)>>>(
+        static_cast<const __nv_bfloat16 *>(x), static_cast<__nv_bfloat16 *>(y), B, NX, NY, NZ, C);
+    FLUB_CHECK_LAUNCH();
+    return FLUB_OK;
+}
+
+int flub_up2_bwd_bf16(const void *dy, void *dx, int B, int NX, int NY, int NZ, int C, void *stream) {
+    FLUB_REQUIRE(dy && dx, "flub_up2_bwd_bf16: bad arguments");
+    k_up2_bwd<<<nb((int64_t)B * NX * NY * NZ * C / 8), 256, 0, as_stream(stream)>>>(
+        static_cast<const __nv_bfloat16 *>(dy), static_cast<__nv_bfloat16 *>(dx), B, NX, NY, NZ, C);
+    FLUB_CHECK_LAUNCH();
+    return FLUB_OK;
+}
+
+int flub_relu_bwd_bf16(const void *dy, const void *y, void *dx, int64_t n, void *stream) {
+    FLUB_REQUIRE(dy && y && dx, "flub_relu_bwd_bf16: bad arguments");
+    k_relu_bwd<<<nb(n), 256, 0, as_stream(stream)>>>(static_cast<const __nv_bfloat16 *>(dy),
+                                                     static_cast<const __nv_bfloat16 *>(y),
+                                                     static_cast<__nv_bfloat16 *>(dx), n);
+    FLUB_CHECK_LAUNCH();
+    return FLUB_OK;
+}
+
+int flub_head_fwd(const void *x, const float *w, const float *b, float *out, int64_t n, void *stream) {
+    FLUB_REQUIRE(x && w && b && out, "flub_head_fwd: bad arguments");
+    k_head_fwd<<<nb(n), 256, 0, as_stream(stream)>>>(static_cast<const __nv_bfloat16 *>(x), w, b, out, n);
+    FLUB_CHECK_LAUNCH();
+    return FLUB_OK;
+}
+
+int flub_head_bwd(const void *x, const float *w, const float *dout, void *dx, float *dw, float *db, int64_t n,
+                  void *stream) {
+    FLUB_REQUIRE(x && w && dout && dx && dw && db, "flub_head_bwd: bad arguments");
+    k_head_bwd<<<blocks_for(n, 256, 152 * 4), 256, 0, as_stream(stream)>>>(
+        static_cast<const __nv_bfloat16 *>(x), w, dout, static_cast<__nv_bfloat16 *>(dx), dw, db, n);
+    FLUB_CHECK_LAUNCH();
+    return FLUB_OK;
+}
+
+int flub_unet_loss(const float *pred, const float *x, const int32_t *tag, const float *inv_scale, int64_t ncell,
+                   int B, double inv_count, float *dpred, double *loss, void *stream) {
+    FLUB_REQUIRE(pred && x && tag && inv_scale && dpred && loss, "flub_unet_loss: bad arguments");
+    const int64_t n = (int64_t)B * ncell;
+    k_unet_loss<<<nb(n), 256, 0, as_stream(stream)>>>(pred, x, tag, inv_scale, ncell, n, inv_count, dpred, loss);
+    FLUB_CHECK_LAUNCH();
+    return FLUB_OK;
+}
+
+int flub_unet_output(const float *out, const int32_t *tag, const float *inv_scale, int64_t ncell, int B, float gain,
+                     float *x0, void *stream) {
+    FLUB_REQUIRE(out && tag && inv_scale && x0, "flub_unet_output: bad arguments");
+    const int64_t n = (int64_t)B * ncell;
+    k_unet_output<<<nb(n), 256, 0, as_stream(stream)>>>(out, tag, inv_scale, ncell, n, gain, x0);
+    FLUB_CHECK_LAUNCH();
+    return FLUB_OK;
+}
+
+int flub_conv3d_wgrad(const void *x, int cin, const void *dy, int cout, float *dw, float *db, int B, int NX, int NY,
+                      int NZ, void *stream) {
+    auto okc = [](int c) { return c == 16 || c == 32 || c == 64; };
+    FLUB_REQUIRE(x && dy && dw && okc(cin) && okc(cout), "flub_conv3d_wgrad: bad arguments");
+    const int64_t nvox = (int64_t)B * NX * NY * NZ;
+    const int64_t nchunk = (nvox + kWgChunk - 1) / kWgChunk;
+    const unsigned gx = (unsigned)(nchunk < 128 ? nchunk : 128);
+    k_conv_wgrad<<<dim3(gx, 27), 256, 0, as_stream(stream)>>>(static_cast<const __nv_bfloat16 *>(x), cin,
+                                                              static_cast<const __nv_bfloat16 *>(dy), cout, dw, db,
+                                                              B, NX, NY, NZ);
+    FLUB_CHECK_LAUNCH();
+    return FLUB_OK;
+}
+
+int flub_adam(float *p, const float *g, float *m, float *v, int64_t n, float lr, float b1, float b2, float eps,
+              int step, void *w16, void *w16t, int cout, int cin, void *stream) {
+    FLUB_REQUIRE(p && g && m && v && n > 0 && step > 0, "flub_adam: bad arguments");
+    FLUB_REQUIRE(!w16 || ((int64_t)27 * cout * cin == n && w16t), "flub_adam: weight shape mismatch");
+    const float c1 = 1.0f / (1.0f - powf(b1, (float)step)), c2 = 1.0f / (1.0f - powf(b2, (float)step));
+    k_adam<<<nb(n), 256, 0, as_stream(stream)>>>(p, g, m, v, n, lr, b1, b2, eps, c1, c2,
+                                                 static_cast<__nv_bfloat16 *>(w16), static_cast<__nv_bfloat16 *>(w16t),
+                                                 cout, cin);
+    FLUB_CHECK_LAUNCH();
+    return FLUB_OK;
+}
+
+}  // extern "C"

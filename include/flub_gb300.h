@@ -230,6 +230,74 @@ int flub_mg_kernels_executed(flub_mg *mg, void *stream, int64_t *out);
 int64_t flub_launch_count(void);
 void flub_reset_launch_count(void);
 
+/* ------------------------------------------------------------------------
+ * Learned warm start: a small 3D U-Net whose output is CG's initial guess
+ * (flub_mg_set_x0).  No counterpart in the reference (it always starts CG
+ * from x = 0); these entry points exist for the network's forward pass,
+ * backward pass and optimiser, which run on the GPU.
+ *
+ * Activations are channels-last BF16 [B][X][Y][Z][C] (C = 16, 32 or 64);
+ * convolution weights are BF16 [27][Cout][Cin] with tap index
+ * (dx+1)*9 + (dy+1)*3 + (dz+1); parameters, gradients and optimiser state are
+ * FP32.  Activation and weight pointers must be 16-byte aligned.
+ * ---------------------------------------------------------------------- */
+
+/* y = [relu](conv3x3x3(x0, w0) + conv3x3x3(x1, w1) + bias), zero padding.
+ * x1 / w1 optional (NULL, cin1 = 0): a second source accumulated into the same
+ * output (a decoder's skip connection, so the concatenation is never formed).
+ * bias may be NULL.  tcgen05 implicit GEMM with FP32 accumulation.  Shape
+ * rules: NZ divides 128 or is a multiple of 128; NY a multiple of 128 / NZ
+ * (when NZ < 128).  The data gradient is the same call on dy with the
+ * flipped, transposed weights that flub_adam writes. */
+int flub_conv3d_bf16(const void *x0, int cin0, const void *w0, const void *x1, int cin1, const void *w1,
+                     const float *bias, void *y, int cout, int B, int NX, int NY, int NZ, int relu, void *stream);
+/* Weight and bias gradients of one source of flub_conv3d_bf16, accumulated:
+ * dw[27][cout][cin] += sum_v dy[v][co] x[v + tap][ci]; db[cout] += sum dy
+ * (db may be NULL, e.g. for the second source of a two-source convolution). */
+int flub_conv3d_wgrad(const void *x, int cin, const void *dy, int cout, float *dw, float *db, int B, int NX, int NY,
+                      int NZ, void *stream);
+/* Non-zero in *out if a convolution kernel gave up on a bounded wait since the
+ * last reset (its output is then incomplete).  Synchronises. */
+int flub_conv_error(int *out, int reset);
+
+/* Network input (16 channels): div / rms(div over fluid), fluid mask, solid
+ * mask, zeros; tag is the reference's (0 air, 1 fluid, 2 solid) per sample of
+ * ncell cells.  inv_scale[b] = 1 / rms (1 without fluid). */
+int flub_unet_input(const float *div, const int32_t *tag, int B, int64_t ncell, float *inv_scale, void *out,
+                    void *stream);
+/* 2x average pool and its gradient (dx = dy / 8, optionally added to dx);
+ * NX, NY, NZ are the fine extents. */
+int flub_pool2_bf16(const void *x, void *y, int B, int NX, int NY, int NZ, int C, void *stream);
+int flub_pool2_bwd_bf16(const void *dy, void *dx, int B, int NX, int NY, int NZ, int C, int accumulate, void *stream);
+/* Nearest 2x upsample and its gradient (sum over the 8 fine cells); NX, NY,
+ * NZ are the fine extents. */
+int flub_up2_bf16(const void *x, void *y, int B, int NX, int NY, int NZ, int C, void *stream);
+int flub_up2_bwd_bf16(const void *dy, void *dx, int B, int NX, int NY, int NZ, int C, void *stream);
+/* dx = dy where y > 0 else 0 (dx may alias dy). */
+int flub_relu_bwd_bf16(const void *dy, const void *y, void *dx, int64_t n, void *stream);
+/* 1x1x1 output head over 16 channels: out = x . w + b (FP32), and its
+ * gradients (dx written, dw / db accumulated). */
+int flub_head_fwd(const void *x, const float *w, const float *b, float *out, int64_t n, void *stream);
+int flub_head_bwd(const void *x, const float *w, const float *dout, void *dx, float *dw, float *db, int64_t n,
+                  void *stream);
+/* Masked MSE against the normalised target x * inv_scale[b]:
+ * *loss += inv_count * sum over fluid cells of (pred - x * inv_scale)^2, with
+ * inv_count normally 1 / (fluid cells of the batch); dpred = d loss / d pred
+ * (0 off fluid). */
+int flub_unet_loss(const float *pred, const float *x, const int32_t *tag, const float *inv_scale, int64_t ncell,
+                   int B, double inv_count, float *dpred, double *loss, void *stream);
+/* Pressure guess from the network output: x0 = out / inv_scale * gain on
+ * fluid cells, 0 elsewhere. */
+int flub_unet_output(const float *out, const int32_t *tag, const float *inv_scale, int64_t ncell, int B, float gain,
+                     float *x0, void *stream);
+/* One Adam step (bias-corrected, step >= 1) on FP32 parameters p with
+ * gradient g and moments m, v.  For a convolution weight (w16 non-NULL,
+ * n = 27 * cout * cin) also writes its BF16 copy [27][cout][cin] and the
+ * flipped, transposed copy w16t [27][cin][cout] (tap 26 - t) for the data
+ * gradient. */
+int flub_adam(float *p, const float *g, float *m, float *v, int64_t n, float lr, float b1, float b2, float eps,
+              int step, void *w16, void *w16t, int cout, int cin, void *stream);
+
 #ifdef __cplusplus
 }
 #endif
