@@ -22,7 +22,7 @@ class FlubError(RuntimeError):
 class SolveInfo(ctypes.Structure):
     _fields_ = [("iterations", ctypes.c_int), ("converged", ctypes.c_int), ("status", ctypes.c_int),
                 ("reserved", ctypes.c_int), ("rtr0", ctypes.c_double), ("rtr", ctypes.c_double),
-                ("tol", ctypes.c_double)]
+                ("tol", ctypes.c_double), ("x0_scale", ctypes.c_double)]
 
     def as_dict(self):
         return {f: getattr(self, f) for f, _ in self._fields_ if f != "reserved"}
@@ -70,6 +70,11 @@ SIGNATURES = {
     "flub_mg_matvec": (_i32, [_vp, _vp, _vp, _vp]),
     "flub_mg_kernels_executed": (_i32, [_vp, _vp, ctypes.POINTER(_i64)]),
     "flub_mg_smooth": (_i32, [_vp, _i32, _i32, _vp]),
+    "flub_mg_set_x0_scaled": (_i32, [_vp, _vp, _vp]),
+    "flub_mg_level_shape": (_i32, [_vp, _i32, ctypes.POINTER(_i32), ctypes.POINTER(_i32), ctypes.POINTER(_i32)]),
+    "flub_mg_level_tags": (_i32, [_vp, _i32, _vp, _vp]),
+    "flub_mg_restrict_vector": (_i32, [_vp, _i32, _vp, _vp, _vp]),
+    "flub_mg_prolong_vector": (_i32, [_vp, _i32, _vp, _vp, _vp]),
     "flub_vcycle_noalloc": (_i32, [_vp, _vp, _vp, _i32, _i32, _i32, _i32, _vp]),
     "flub_launch_count": (_i64, []),
     "flub_reset_launch_count": (None, []),
@@ -84,7 +89,7 @@ SIGNATURES = {
     "flub_relu_bwd_bf16": (_i32, [_vp, _vp, _vp, _i64, _vp]),
     "flub_head_fwd": (_i32, [_vp, _vp, _vp, _vp, _i64, _vp]),
     "flub_head_bwd": (_i32, [_vp, _vp, _vp, _vp, _vp, _vp, _i64, _vp]),
-    "flub_unet_loss": (_i32, [_vp, _vp, _vp, _vp, _i64, _i32, _f64, _vp, _vp, _vp]),
+    "flub_unet_loss": (_i32, [_vp, _vp, _vp, _vp, _i64, _i32, _f64, _vp, _vp, _vp, _vp]),
     "flub_unet_output": (_i32, [_vp, _vp, _vp, _i64, _i32, _f32, _vp, _vp]),
     "flub_adam": (_i32, [_vp, _vp, _vp, _vp, _i64, _f32, _f32, _f32, _f32, _i32, _vp, _vp, _i32, _i32, _vp]),
 }

@@ -21,6 +21,7 @@ constexpr int kHistory = 4096;
 struct MgState {
     double rtr0, tol, rtr, zr_old, pap, alpha, beta, eps, abs_tol, rel_tol;
     double mean;                 // zero_centered mean (FP64 sum / count)
+    double x0_scale;             // scale applied to the initial guess (0: no guess)
     unsigned long long kernels;  // solver kernels executed inside graphs
     int it, max_iters, converged, status, cond, use_x0;
     unsigned int ticket;
@@ -284,6 +285,7 @@ __global__ void k_solve_begin(MgState *st, int max_iters, double eps, double abs
     st->status = FLUB_OK;
     st->cond = 0;
     st->use_x0 = use_x0;
+    if (!use_x0) st->x0_scale = 0.0;
     st->zscale = 1.0f;
     st->alpha = 0.0;
     st->beta = 0.0;

@@ -753,7 +753,119 @@ static int read_info(flub_mg *mg, cudaStream_t s, flub_solve_info *info) {
     info->rtr0 = h.rtr0;
     info->rtr = h.rtr;
     info->tol = h.tol;
+    info->x0_scale = h.x0_scale;
     return FLUB_OK;
+}
+
+// ---------------------------------------------------------------- warm-start support (no reference counterpart)
+
+__global__ void k_set_x0_scale(MgState *st, double v) { st->x0_scale = v; }
+
+// gamma = (d . b) / (d . L d) over fluid cells: the multiple of d closest to
+// the solution of L x = b in the energy norm.  Two FP64 sums, combined in a
+// fixed order by the last block.
+__global__ void __launch_bounds__(kRedThreads) k_x0_gamma(MgState *st, const float *__restrict__ d,
+                                                          const float *__restrict__ b,
+                                                          const uint8_t *__restrict__ code, Dims D,
+                                                          double *partials) {
+    __shared__ double red[32];
+    const int64_t n = D.n();
+    double s_ld = 0.0, s_b = 0.0;
+    for (int64_t c = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; c < n; c += (int64_t)gridDim.x * blockDim.x) {
+        if (code[c] != kCodeFluid) continue;
+        int i, j, k, dd;
+        unflatten(c, D, i, j, k);
+        const float dc = d[c];
+        const float ld = lap_at(d, code, i, j, k, D, c, dc, dd);
+        s_ld = fma((double)dc, (double)ld, s_ld);
+        s_b = fma((double)dc, (double)b[c], s_b);
+    }
+    const double bb = block_sum(s_b, red);
+    __syncthreads();
+    if (threadIdx.x == 0) partials[kMaxRedBlocks + blockIdx.x] = bb;
+    double total;
+    if (finish_partials(s_ld, partials, &st->ticket, red, &total)) {
+        __syncthreads();
+        double t2 = 0.0;
+        for (unsigned q = threadIdx.x; q < gridDim.x; q += blockDim.x) t2 += __ldcg(&partials[kMaxRedBlocks + q]);
+        t2 = block_sum(t2, red);
+        if (threadIdx.x == 0) {
+            const double g = t2 / total;
+            st->x0_scale = (total != 0.0 && isfinite(g)) ? g : 0.0;
+        }
+    }
+}
+
+// x = x0_scale * d on fluid cells, 0 elsewhere.
+__global__ void __launch_bounds__(256) k_x0_apply(const MgState *__restrict__ st, const float *__restrict__ d,
+                                                  const uint8_t *__restrict__ code, float *__restrict__ x, int64_t n) {
+    const float g = (float)st->x0_scale;
+    for (int64_t c = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; c < n; c += (int64_t)gridDim.x * blockDim.x)
+        x[c] = code[c] == kCodeFluid ? __fmul_rn(g, d[c]) : 0.0f;
+}
+
+__global__ void __launch_bounds__(256) k_decode_codes(const uint8_t *__restrict__ code, int32_t *__restrict__ tag,
+                                                      int64_t n) {
+    for (int64_t c = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; c < n; c += (int64_t)gridDim.x * blockDim.x)
+        tag[c] = decode_tag(code[c]);
+}
+
+// Coarse vector = sum of its 8 children (the V-cycle's restriction of a
+// residual with z = 0), 0 at coarse cells that are not fluid.
+__global__ void __launch_bounds__(256) k_restrict_vec(const float *__restrict__ f, const uint8_t *__restrict__ cc,
+                                                      float *__restrict__ out, Dims C) {
+    const int64_t n = C.n();
+    const int64_t fy = 2 * (int64_t)C.ny, fz = 2 * (int64_t)C.nz;
+    for (int64_t q = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; q < n; q += (int64_t)gridDim.x * blockDim.x) {
+        if (cc[q] != kCodeFluid) {
+            out[q] = 0.0f;
+            continue;
+        }
+        int I, J, K;
+        unflatten(q, C, I, J, K);
+        float s = 0.0f;
+        for (int m = 0; m < 8; m++) {
+            const int64_t c = ((2 * (int64_t)I + (m >> 2)) * fy + 2 * J + ((m >> 1) & 1)) * fz + 2 * K + (m & 1);
+            s = __fadd_rn(s, f[c]);
+        }
+        out[q] = s;
+    }
+}
+
+// Cell-centred trilinear interpolation from the coarse level to the fine
+// level at fine fluid cells (0 elsewhere).  Fine cell 2I + e sits a quarter
+// coarse cell from coarse cell I towards I - 1 (e = 0) or I + 1 (e = 1):
+// weights 3/4 and 1/4 per axis.  Coarse fluid cells contribute their value,
+// air cells 0 (Dirichlet), solid and out-of-domain cells are left out and
+// the remaining weights renormalised.
+__global__ void __launch_bounds__(256) k_prolong_trilinear(const float *__restrict__ xc,
+                                                           const uint8_t *__restrict__ cc, Dims C,
+                                                           const uint8_t *__restrict__ cf, float *__restrict__ xf,
+                                                           Dims F) {
+    const int64_t n = F.n();
+    for (int64_t c = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; c < n; c += (int64_t)gridDim.x * blockDim.x) {
+        if (cf[c] != kCodeFluid) {
+            xf[c] = 0.0f;
+            continue;
+        }
+        int i, j, k;
+        unflatten(c, F, i, j, k);
+        const int I = i >> 1, J = j >> 1, K = k >> 1;
+        const int oi = (i & 1) ? 1 : -1, oj = (j & 1) ? 1 : -1, ok = (k & 1) ? 1 : -1;
+        float s = 0.0f, w = 0.0f;
+        for (int m = 0; m < 8; m++) {
+            const int a = (m >> 2) ? oi : 0, bq = ((m >> 1) & 1) ? oj : 0, e = (m & 1) ? ok : 0;
+            const int ii = I + a, jj = J + bq, kk = K + e;
+            if (ii < 0 || ii >= C.nx || jj < 0 || jj >= C.ny || kk < 0 || kk >= C.nz) continue;
+            const int64_t q = ((int64_t)ii * C.ny + jj) * C.nz + kk;
+            const uint8_t code = cc[q];
+            if (code == kCodeSolid) continue;
+            const float wt = (a ? 0.25f : 0.75f) * (bq ? 0.25f : 0.75f) * (e ? 0.25f : 0.75f);
+            w += wt;
+            if (code == kCodeFluid) s = fmaf(wt, xc[q], s);
+        }
+        xf[c] = w > 0.0f ? s / w : 0.0f;
+    }
 }
 
 }  // namespace flub
@@ -895,6 +1007,8 @@ int flub_mg_mask_interior(flub_mg *mg, void *stream) {
 int flub_mg_set_x0(flub_mg *mg, const float *x0, void *stream) {
     FLUB_REQUIRE(mg && x0, "flub_mg_set_x0: NULL argument");
     FLUB_CHECK_CUDA(cudaMemcpyAsync(mg->x, x0, sizeof(float) * mg->n, cudaMemcpyDeviceToDevice, as_stream(stream)));
+    k_set_x0_scale<<<1, 1, 0, as_stream(stream)>>>(mg->st, 1.0);
+    FLUB_CHECK_LAUNCH();
     mg->use_x0 = true;
     return FLUB_OK;
 }
@@ -953,6 +1067,59 @@ int flub_mg_residual_history(flub_mg *mg, void *stream, double *out, int max_n, 
         FLUB_CHECK_CUDA(cudaMemcpy(out, mg->hist, sizeof(double) * n, cudaMemcpyDeviceToHost));
     }
     *n_out = n;
+    return FLUB_OK;
+}
+
+int flub_mg_set_x0_scaled(flub_mg *mg, const float *d, void *stream) {
+    FLUB_REQUIRE(mg && d, "flub_mg_set_x0_scaled: NULL argument");
+    FLUB_REQUIRE(d != mg->x, "flub_mg_set_x0_scaled: d must not be the solution vector itself");
+    cudaStream_t s = as_stream(stream);
+    const Level &L0 = mg->lv[0];
+    k_x0_gamma<<<red_blocks(mg->n), kRedThreads, 0, s>>>(mg->st, d, L0.r, L0.code, L0.D, mg->partials);
+    FLUB_CHECK_LAUNCH();
+    k_x0_apply<<<blocks_for(mg->n, 256), 256, 0, s>>>(mg->st, d, L0.code, mg->x, mg->n);
+    FLUB_CHECK_LAUNCH();
+    mg->use_x0 = true;
+    return FLUB_OK;
+}
+
+int flub_mg_level_shape(flub_mg *mg, int level, int *nx, int *ny, int *nz) {
+    FLUB_REQUIRE(mg && nx && ny && nz, "flub_mg_level_shape: NULL argument");
+    FLUB_REQUIRE(level >= 0 && level < mg->levels, "flub_mg_level_shape: level %d outside [0, %d)", level,
+                 mg->levels);
+    *nx = mg->lv[level].D.nx;
+    *ny = mg->lv[level].D.ny;
+    *nz = mg->lv[level].D.nz;
+    return FLUB_OK;
+}
+
+int flub_mg_level_tags(flub_mg *mg, int level, int32_t *tag, void *stream) {
+    FLUB_REQUIRE(mg && tag, "flub_mg_level_tags: NULL argument");
+    FLUB_REQUIRE(level >= 0 && level < mg->levels, "flub_mg_level_tags: level %d outside [0, %d)", level, mg->levels);
+    const Level &L = mg->lv[level];
+    k_decode_codes<<<blocks_for(L.D.n(), 256), 256, 0, as_stream(stream)>>>(L.code, tag, L.D.n());
+    FLUB_CHECK_LAUNCH();
+    return FLUB_OK;
+}
+
+int flub_mg_restrict_vector(flub_mg *mg, int level, const float *fine, float *coarse, void *stream) {
+    FLUB_REQUIRE(mg && fine && coarse, "flub_mg_restrict_vector: NULL argument");
+    FLUB_REQUIRE(level >= 1 && level < mg->levels, "flub_mg_restrict_vector: level %d outside [1, %d)", level,
+                 mg->levels);
+    const Level &L = mg->lv[level];
+    k_restrict_vec<<<blocks_for(L.D.n(), 256), 256, 0, as_stream(stream)>>>(fine, L.code, coarse, L.D);
+    FLUB_CHECK_LAUNCH();
+    return FLUB_OK;
+}
+
+int flub_mg_prolong_vector(flub_mg *mg, int level, const float *coarse, float *fine, void *stream) {
+    FLUB_REQUIRE(mg && fine && coarse, "flub_mg_prolong_vector: NULL argument");
+    FLUB_REQUIRE(level >= 1 && level < mg->levels, "flub_mg_prolong_vector: level %d outside [1, %d)", level,
+                 mg->levels);
+    const Level &C = mg->lv[level], &F = mg->lv[level - 1];
+    k_prolong_trilinear<<<blocks_for(F.D.n(), 256), 256, 0, as_stream(stream)>>>(coarse, C.code, C.D, F.code, fine,
+                                                                                 F.D);
+    FLUB_CHECK_LAUNCH();
     return FLUB_OK;
 }
 

@@ -239,6 +239,184 @@ __global__ void __launch_bounds__(kConvThreads, 1)
     if (warp == 0) asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(kCols));
 }
 
+// ---------------------------------------------------------------- weight gradient
+//
+//   dW[tap][co][ci] = sum over voxels v of X[v + off(tap)][ci] * dY[v][co]
+// as a tcgen05 GEMM with the voxels as K:
+//   D[m = (slot, ci)][co] += A[m][v] * B[co][v]
+// A holds G = 128 / Cin tap-shifted input tiles side by side (a "tap group":
+// M = 128 rows = G taps x Cin channels), B the output-gradient tile.  Both are
+// the channels-last tiles TMA already writes for the forward pass, read as
+// MN-major operands: the channel dimension is contiguous, one swizzle atom
+// wide, and the tap tiles of a group are consecutive atoms along M (leading
+// byte offset = one tile).  A persistent CTA walks its share of the
+// 128-voxel tiles, keeps one FP32 accumulator per tap group in TMEM for its
+// whole life, and adds it to dW with one atomic per entry at the end.
+// Groups that do not fit in TMEM (512 columns) are split over blockIdx.y.
+
+constexpr int kWgStages = 4;
+constexpr int kWgA = 32768;  // G tap tiles of 128 voxels x Cin BF16
+constexpr int kWgB = 16384;  // dY tile, 128 voxels x Cout <= 64
+constexpr int kWgStage = kWgA + kWgB;
+constexpr int kWgSmem = kWgStages * kWgStage + 1024 + 256;
+constexpr uint32_t kDoneWaitLimit = 1u << 26;
+
+// MN-major shared-memory descriptor: swizzle width = one row (the channel
+// extent), lbo = stride between atoms along M/N, sbo = 8 rows along K.
+__device__ __forceinline__ uint64_t sw_desc_mn(uint32_t saddr, int row_bytes, uint32_t lbo) {
+    const uint64_t layout = row_bytes == 128 ? 2ull : (row_bytes == 64 ? 4ull : 6ull);
+    uint64_t d = 0;
+    d |= (uint64_t)((saddr & 0x3FFFFu) >> 4);
+    d |= (uint64_t)((lbo >> 4) & 0x3FFFu) << 16;
+    d |= (uint64_t)(((8u * row_bytes) >> 4) & 0x3FFFu) << 32;
+    d |= (uint64_t)1 << 46;
+    d |= layout << 61;
+    return d;
+}
+
+__device__ __forceinline__ bool mbar_wait_long(uint32_t bar, uint32_t parity) {
+    for (uint32_t i = 0; i < kDoneWaitLimit; i++) {
+        uint32_t ok;
+        asm volatile(
+            "{\n\t.reg .pred p;\n\t"
+            "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+            "selp.u32 %0, 1, 0, p;\n\t}"
+            : "=r"(ok)
+            : "r"(bar), "r"(parity)
+            : "memory");
+        if (ok) return true;
+    }
+    return false;
+}
+
+template <int CIN, int COUT>
+__global__ void __launch_bounds__(kConvThreads, 1)
+    k_conv3d_wgrad_tc(const __grid_constant__ CUtensorMap mx, const __grid_constant__ CUtensorMap mdy, const ConvGeom g,
+                      int groups_per_slice, int tmem_cols, float *__restrict__ dw) {
+    constexpr int G = 128 / CIN;                 // taps per group
+    constexpr int NG = (27 + G - 1) / G;         // groups
+    constexpr int TILE_A = 128 * CIN * 2;        // one tap tile
+    constexpr int TILE_B = 128 * COUT * 2;
+    extern __shared__ unsigned char conv_smem_raw[];
+    unsigned char *smem = reinterpret_cast<unsigned char *>(
+        (reinterpret_cast<uintptr_t>(conv_smem_raw) + 1023) & ~static_cast<uintptr_t>(1023));
+    uint64_t *full = reinterpret_cast<uint64_t *>(smem + kWgStages * kWgStage);
+    uint64_t *empty = full + kWgStages;
+    uint64_t *done = empty + kWgStages;
+    uint32_t *tmem_slot = reinterpret_cast<uint32_t *>(done + 1);
+    __shared__ int fail;
+
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int tz = g.NZ / g.nzb, ty = g.NY / g.nyb;
+    const int ntiles = g.B * g.NX * ty * tz;
+    const int my_tiles = blockIdx.x < (unsigned)ntiles ? (ntiles - 1 - (int)blockIdx.x) / (int)gridDim.x + 1 : 0;
+    const int gbeg = blockIdx.y * groups_per_slice;
+    const int gend = min(NG, gbeg + groups_per_slice);
+    const int ng = gend - gbeg;
+    const int T = my_tiles * ng;
+
+    if (threadIdx.x == 0) {
+        fail = 0;
+        for (int s = 0; s < kWgStages; s++) {
+            asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_u32(&full[s])));
+            asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_u32(&empty[s])));
+        }
+        asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_u32(done)));
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+        asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+    }
+    if (warp == 0) {
+        asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(tmem_slot)),
+                     "r"(tmem_cols));
+        asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;");
+    }
+    asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+    __syncthreads();
+    asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+    const uint32_t tmem = *tmem_slot;
+
+    if (threadIdx.x == 0) {
+        for (int it = 0; it < T; it++) {
+            const int s = it % kWgStages, u = it / kWgStages;
+            if (u > 0 && !mbar_wait(smem_u32(&empty[s]), (u - 1) & 1)) {
+                fail = 1;
+                break;
+            }
+            int t = (int)blockIdx.x + (it / ng) * (int)gridDim.x;
+            const int grp = gbeg + it % ng;
+            const int z0 = (t % tz) * g.nzb;
+            t /= tz;
+            const int y0 = (t % ty) * g.nyb;
+            t /= ty;
+            const int x = t % g.NX, b = t / g.NX;
+            const int taps = min(G, 27 - grp * G);
+            const uint32_t bytes = (uint32_t)(taps * TILE_A + TILE_B);
+            const uint32_t fb = smem_u32(&full[s]);
+            asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(fb), "r"(bytes) : "memory");
+            const uint32_t a = smem_u32(smem + s * kWgStage);
+            for (int q = 0; q < taps; q++) {
+                const int tap = grp * G + q;
+                const int dx = tap / 9 - 1, dy = (tap / 3) % 3 - 1, dz = tap % 3 - 1;
+                tma_load_5d(a + q * TILE_A, &mx, 0, z0 + dz, y0 + dy, x + dx, b, fb);
+            }
+            tma_load_5d(a + kWgA, &mdy, 0, z0, y0, x, b, fb);
+        }
+    } else if (threadIdx.x == 32) {
+        const uint32_t idesc = mma_idesc(COUT) | (1u << 15) | (1u << 16);  // A and B MN-major
+        for (int it = 0; it < T; it++) {
+            const int s = it % kWgStages, u = it / kWgStages;
+            if (!mbar_wait(smem_u32(&full[s]), u & 1)) {
+                fail = 1;
+                break;
+            }
+            asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+            const int j = it % ng;
+            const uint32_t a = smem_u32(smem + s * kWgStage), bb = a + kWgA;
+#pragma unroll
+            for (int kk = 0; kk < 8; kk++) {  // 16 voxel rows per MMA
+                const uint64_t ad = sw_desc_mn(a + kk * 16 * CIN * 2, CIN * 2, TILE_A);
+                const uint64_t bd = sw_desc_mn(bb + kk * 16 * COUT * 2, COUT * 2, TILE_B);
+                const uint32_t acc = (it >= ng || kk > 0) ? 1u : 0u;
+                asm volatile(
+                    "{\n\t.reg .pred p;\n\tsetp.ne.b32 p, %4, 0;\n\t"
+                    "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n\t}" ::"r"(tmem + (uint32_t)(j * COUT)),
+                    "l"(ad), "l"(bd), "r"(idesc), "r"(acc));
+            }
+            asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(
+                smem_u32(&empty[s]))
+                         : "memory");
+        }
+        asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(
+            smem_u32(done))
+                     : "memory");
+    }
+    __syncwarp();
+    const bool got = __all_sync(0xffffffffu, mbar_wait_long(smem_u32(done), 0) ? 1 : 0) != 0;
+    if (!got) fail = 1;
+    asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+    __syncthreads();  // every thread sees a failure of the producer or the MMA issuer
+    if (got && !fail && my_tiles > 0) {
+        const int m = warp * 32 + lane;
+        const int slot = m / CIN, ci = m % CIN;
+        for (int j = 0; j < ng; j++) {
+            const int tap = (gbeg + j) * G + slot;
+#pragma unroll
+            for (int c = 0; c < COUT; c += 16) {
+                float v[16];
+                tmem_ld16(tmem + ((uint32_t)(warp * 32) << 16) + (uint32_t)(j * COUT + c), v);
+                if (tap < 27) {
+#pragma unroll
+                    for (int e = 0; e < 16; e++) atomicAdd(&dw[((int64_t)tap * COUT + c + e) * CIN + ci], v[e]);
+                }
+            }
+        }
+    }
+    asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+    __syncthreads();
+    if (fail && threadIdx.x == 0) atomicExch(&g_conv_error, 1);
+    if (warp == 0) asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(tmem_cols));
+}
+
 // ---------------------------------------------------------------- host side
 
 static PFN_cuTensorMapEncodeTiled_v12000 g_encode = nullptr;
@@ -356,6 +534,67 @@ extern "C" int flub_conv3d_bf16(const void *x0, int cin0, const void *w0, const 
     case 32: return launch_conv<32>(mx0, mw0, mx1, mw1, g, bias, yo, s);
     default: return launch_conv<64>(mx0, mw0, mx1, mw1, g, bias, yo, s);
     }
+}
+
+namespace flub {
+int launch_bias_grad(const void *dy, int cout, int64_t nvox, float *db, cudaStream_t s);
+
+template <int CIN, int COUT>
+static int launch_wgrad(const CUtensorMap &mx, const CUtensorMap &mdy, const ConvGeom &g, float *dw, cudaStream_t s) {
+    static bool attr_set = false;
+    if (!attr_set) {
+        FLUB_CHECK_CUDA(
+            cudaFuncSetAttribute(k_conv3d_wgrad_tc<CIN, COUT>, cudaFuncAttributeMaxDynamicSharedMemorySize, kWgSmem));
+        attr_set = true;
+    }
+    constexpr int G = 128 / CIN, NG = (27 + G - 1) / G;
+    const int per = NG * COUT <= 512 ? NG : 512 / COUT;
+    const int slices = (NG + per - 1) / per;
+    int cols = 32;
+    while (cols < per * COUT) cols <<= 1;
+    int dev = 0, sms = kNumSMs;
+    FLUB_CHECK_CUDA(cudaGetDevice(&dev));
+    FLUB_CHECK_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
+    const int64_t ntiles = (int64_t)g.B * g.NX * (g.NY / g.nyb) * (g.NZ / g.nzb);
+    const unsigned gx = (unsigned)(ntiles < sms ? ntiles : sms);
+    k_conv3d_wgrad_tc<CIN, COUT><<<dim3(gx, slices), kConvThreads, kWgSmem, s>>>(mx, mdy, g, per, cols, dw);
+    FLUB_CHECK_LAUNCH();
+    return FLUB_OK;
+}
+}  // namespace flub
+
+extern "C" int flub_conv3d_wgrad(const void *x, int cin, const void *dy, int cout, float *dw, float *db, int B, int NX,
+                                 int NY, int NZ, void *stream) {
+    auto okc = [](int c) { return c == 16 || c == 32 || c == 64; };
+    FLUB_REQUIRE(x && dy && dw, "flub_conv3d_wgrad: NULL argument");
+    FLUB_REQUIRE(okc(cin) && okc(cout), "flub_conv3d_wgrad: channels must be 16, 32 or 64 (cin=%d cout=%d)", cin, cout);
+    FLUB_REQUIRE(B > 0 && NX > 0 && NY > 0 && NZ > 0, "flub_conv3d_wgrad: bad shape");
+    FLUB_REQUIRE(aligned16(x) && aligned16(dy), "flub_conv3d_wgrad: pointers must be 16-byte aligned");
+    ConvGeom g;
+    g.B = B; g.NX = NX; g.NY = NY; g.NZ = NZ;
+    g.nzb = NZ < 128 ? NZ : 128;
+    FLUB_REQUIRE(128 % g.nzb == 0 && NZ % g.nzb == 0, "flub_conv3d_wgrad: NZ=%d must divide 128 or be a multiple of 128",
+                 NZ);
+    g.nyb = 128 / g.nzb;
+    FLUB_REQUIRE(NY % g.nyb == 0, "flub_conv3d_wgrad: NY=%d must be a multiple of %d", NY, g.nyb);
+    g.cout = cout;
+    g.cin0 = cin;
+    g.cin1 = 0;
+    g.relu = 0;
+    int st = get_encode();
+    if (st) return st;
+    CUtensorMap mx, mdy;
+    if ((st = make_act_map(&mx, x, cin, g)) || (st = make_act_map(&mdy, dy, cout, g))) return st;
+    cudaStream_t s = as_stream(stream);
+#define FLUB_WG(CI, CO) \
+    if (cin == CI && cout == CO) st = launch_wgrad<CI, CO>(mx, mdy, g, dw, s);
+    FLUB_WG(16, 16) FLUB_WG(16, 32) FLUB_WG(16, 64)
+    FLUB_WG(32, 16) FLUB_WG(32, 32) FLUB_WG(32, 64)
+    FLUB_WG(64, 16) FLUB_WG(64, 32) FLUB_WG(64, 64)
+#undef FLUB_WG
+    if (st) return st;
+    if (db) return launch_bias_grad(dy, cout, (int64_t)B * NX * NY * NZ, db, s);
+    return FLUB_OK;
 }
 
 extern "C" int flub_conv_error(int *out, int reset) {

@@ -170,25 +170,48 @@ __global__ void __launch_bounds__(256) k_head_bwd(const __nv_bfloat16 *__restric
     }
 }
 
+// Per-sample squared norm of the normalised target over fluid cells.
+__global__ void __launch_bounds__(256) k_target_norm(const float *__restrict__ x, const int32_t *__restrict__ tag,
+                                                     const float *__restrict__ inv_scale, int64_t ncell,
+                                                     double *__restrict__ norm) {
+    __shared__ double red[32];
+    const int b = blockIdx.x;
+    const float sc = inv_scale[b];
+    double s = 0.0;
+    for (int64_t q = threadIdx.x; q < ncell; q += blockDim.x) {
+        const int64_t v = b * ncell + q;
+        if (tag[v] == 1) {
+            const double t = (double)(x[v] * sc);
+            s += t * t;
+        }
+    }
+    s = block_sum(s, red);
+    if (threadIdx.x == 0) norm[b] = s;
+}
+
 // Masked MSE on fluid cells in normalised units: target = x * inv_scale[b].
-// loss (FP64 sum, mean over fluid cells of the batch) and dpred.
+// Weight per cell: inv_count, or 1 / (B * |target_b|^2) with per-sample norms
+// (relative error averaged over the batch).  loss (FP64) and dpred.
 __global__ void __launch_bounds__(256) k_unet_loss(const float *__restrict__ pred, const float *__restrict__ x,
                                                    const int32_t *__restrict__ tag, const float *__restrict__ inv_scale,
-                                                   int64_t ncell, int64_t n, double inv_count,
-                                                   float *__restrict__ dpred, double *__restrict__ loss) {
+                                                   const double *__restrict__ norm, int B, int64_t ncell, int64_t n,
+                                                   double inv_count, float *__restrict__ dpred,
+                                                   double *__restrict__ loss) {
     __shared__ double red[32];
     double s = 0.0;
     GRID_LOOP(v, n) {
         float g = 0.0f;
         if (tag[v] == 1) {
-            const float d = pred[v] - x[v] * inv_scale[v / ncell];
-            s += (double)d * d;
-            g = (float)(2.0 * inv_count) * d;
+            const int64_t b = v / ncell;
+            const double w = norm ? (norm[b] > 0.0 ? 1.0 / (B * norm[b]) : 0.0) : inv_count;
+            const float d = pred[v] - x[v] * inv_scale[b];
+            s += w * ((double)d * d);
+            g = (float)(2.0 * w) * d;
         }
         dpred[v] = g;
     }
     s = block_sum(s, red);
-    if (threadIdx.x == 0) atomicAdd(loss, s * inv_count);
+    if (threadIdx.x == 0) atomicAdd(loss, s);
 }
 
 // Network output (normalised) -> pressure guess: x0 = out / inv_scale * gain on
@@ -199,98 +222,41 @@ __global__ void __launch_bounds__(256) k_unet_output(const float *__restrict__ o
     GRID_LOOP(v, n) x0[v] = tag[v] == 1 ? out[v] / inv_scale[v / ncell] * gain : 0.0f;
 }
 
-// Weight gradient of a 3x3x3 convolution (CUDA cores):
-//   dW[tap][co][ci] += sum_v dY[v][co] X[v + tap][ci],  dB[co] += sum_v dY[v][co]
-// Block = (chunk set, tap).  Each block walks chunks of 64 voxels, stages dY
-// and the tap-shifted X (zero outside the volume) in shared memory, and each
-// thread accumulates a 4 x 4 tile of (co, ci) over its share of the voxels.
-constexpr int kWgChunk = 64;
+// Bias gradient db[co] += sum_v dy[v][co]: each thread owns one 8-channel
+// chunk (16 bytes) of the voxel rows it visits; per-block sums in shared
+// memory, one global atomic per channel and block.
+__global__ void __launch_bounds__(256) k_bias_grad(const uint4 *__restrict__ dy, int nch, int64_t nq,
+                                                   float *__restrict__ db) {
+    __shared__ float sb[64];
+    if (threadIdx.x < 64) sb[threadIdx.x] = 0.0f;
+    __syncthreads();
+    float acc[8];
+#pragma unroll
+    for (int e = 0; e < 8; e++) acc[e] = 0.0f;
+    // blockDim and the grid stride are multiples of nch: q % nch is fixed per thread
+    GRID_LOOP(q, nq) {
+        const uint4 u = dy[q];
+        const __nv_bfloat162 *h = reinterpret_cast<const __nv_bfloat162 *>(&u);
+#pragma unroll
+        for (int e = 0; e < 4; e++) {
+            const float2 f = __bfloat1622float2(h[e]);
+            acc[2 * e] += f.x;
+            acc[2 * e + 1] += f.y;
+        }
+    }
+    const int j = threadIdx.x % nch;
+#pragma unroll
+    for (int e = 0; e < 8; e++) atomicAdd(&sb[j * 8 + e], acc[e]);
+    __syncthreads();
+    if (threadIdx.x < nch * 8) atomicAdd(&db[threadIdx.x], sb[threadIdx.x]);
+}
 
-__global__ void __launch_bounds__(256) k_conv_wgrad(const __nv_bfloat16 *__restrict__ x, int cin,
-                                                    const __nv_bfloat16 *__restrict__ dy, int cout, float *dw,
-                                                    float *db, int B, int NX, int NY, int NZ) {
-    __shared__ float sm[2 * kWgChunk * 64];
-    float *sy = sm, *sx = sm + kWgChunk * 64;
-    const int tap = blockIdx.y;
-    const int dx_ = tap / 9 - 1, dy_ = (tap / 3) % 3 - 1, dz_ = tap % 3 - 1;
-    const int64_t nvox = (int64_t)B * NX * NY * NZ;
-    const int64_t nchunk = (nvox + kWgChunk - 1) / kWgChunk;
-    const int tco = cout / 4, tci = cin / 4, ntile = tco * tci;
-    const int vsplit = 256 / ntile;  // ntile in {16, 32, 64, 128, 256}
-    const int tile = threadIdx.x % ntile, vpart = threadIdx.x / ntile;
-    const int co0 = (tile / tci) * 4, ci0 = (tile % tci) * 4;
-    float acc[4][4];
-    float accb[4];
-#pragma unroll
-    for (int a = 0; a < 4; a++) {
-        accb[a] = 0.0f;
-#pragma unroll
-        for (int c = 0; c < 4; c++) acc[a][c] = 0.0f;
-    }
-    for (int64_t ch = blockIdx.x; ch < nchunk; ch += gridDim.x) {
-        const int64_t v0 = ch * kWgChunk;
-        for (int q = threadIdx.x; q < kWgChunk * cout; q += blockDim.x) {
-            const int64_t v = v0 + q / cout;
-            sy[q] = v < nvox ? bf(dy[v * cout + q % cout]) : 0.0f;
-        }
-        for (int q = threadIdx.x; q < kWgChunk * cin; q += blockDim.x) {
-            const int64_t v = v0 + q / cin;
-            float val = 0.0f;
-            if (v < nvox) {
-                int64_t t = v;
-                const int k = (int)(t % NZ); t /= NZ;
-                const int j = (int)(t % NY); t /= NY;
-                const int i = (int)(t % NX);
-                const int b = (int)(t / NX);
-                const int ii = i + dx_, jj = j + dy_, kk = k + dz_;
-                if (ii >= 0 && ii < NX && jj >= 0 && jj < NY && kk >= 0 && kk < NZ)
-                    val = bf(x[((((int64_t)b * NX + ii) * NY + jj) * NZ + kk) * cin + q % cin]);
-            }
-            sx[q] = val;
-        }
-        __syncthreads();
-        for (int m = vpart; m < kWgChunk; m += vsplit) {
-            float yv[4], xv[4];
-#pragma unroll
-            for (int a = 0; a < 4; a++) yv[a] = sy[m * cout + co0 + a];
-#pragma unroll
-            for (int c = 0; c < 4; c++) xv[c] = sx[m * cin + ci0 + c];
-#pragma unroll
-            for (int a = 0; a < 4; a++) {
-                accb[a] += yv[a];
-#pragma unroll
-                for (int c = 0; c < 4; c++) acc[a][c] = fmaf(yv[a], xv[c], acc[a][c]);
-            }
-        }
-        __syncthreads();
-    }
-    // combine the vsplit partial tiles in shared memory, then one atomic per entry
-    float *red = sm;  // reuse: ntile * 20 floats (16 weights + 4 bias) <= 2 * kWgChunk * 64
-    const int per = 20;
-    for (int part = 0; part < vsplit; part++) {
-        if (vpart == part) {
-#pragma unroll
-            for (int a = 0; a < 4; a++) {
-#pragma unroll
-                for (int c = 0; c < 4; c++) {
-                    float *dst = &red[tile * per + a * 4 + c];
-                    *dst = part == 0 ? acc[a][c] : *dst + acc[a][c];
-                }
-                float *dst = &red[tile * per + 16 + a];
-                *dst = part == 0 ? accb[a] : *dst + accb[a];
-            }
-        }
-        __syncthreads();
-    }
-    if (vpart == 0) {
-#pragma unroll
-        for (int a = 0; a < 4; a++) {
-#pragma unroll
-            for (int c = 0; c < 4; c++)
-                atomicAdd(&dw[((int64_t)tap * cout + co0 + a) * cin + ci0 + c], red[tile * per + a * 4 + c]);
-            if (db && tap == 13 && ci0 == 0) atomicAdd(&db[co0 + a], red[tile * per + 16 + a]);
-        }
-    }
+int launch_bias_grad(const void *dy, int cout, int64_t nvox, float *db, cudaStream_t s) {
+    const int nch = cout / 8;
+    const int64_t nq = nvox * nch;
+    k_bias_grad<<<blocks_for(nq, 256, 152 * 8), 256, 0, s>>>(static_cast<const uint4 *>(dy), nch, nq, db);
+    FLUB_CHECK_LAUNCH();
+    return FLUB_OK;
 }
 
 // Adam (decoupled weight decay off) on FP32 masters; optionally writes the BF16
@@ -395,10 +361,15 @@ int flub_head_bwd(const void *x, const float *w, const float *dout, void *dx, fl
 }
 
 int flub_unet_loss(const float *pred, const float *x, const int32_t *tag, const float *inv_scale, int64_t ncell,
-                   int B, double inv_count, float *dpred, double *loss, void *stream) {
-    FLUB_REQUIRE(pred && x && tag && inv_scale && dpred && loss, "flub_unet_loss: bad arguments");
+                   int B, double inv_count, double *sample_norm, float *dpred, double *loss, void *stream) {
+    FLUB_REQUIRE(pred && x && tag && inv_scale && dpred && loss && B > 0, "flub_unet_loss: bad arguments");
     const int64_t n = (int64_t)B * ncell;
-    k_unet_loss<<<nb(n), 256, 0, as_stream(stream)>>>(pred, x, tag, inv_scale, ncell, n, inv_count, dpred, loss);
+    cudaStream_t s = as_stream(stream);
+    if (sample_norm) {
+        k_target_norm<<<B, 256, 0, s>>>(x, tag, inv_scale, ncell, sample_norm);
+        FLUB_CHECK_LAUNCH();
+    }
+    k_unet_loss<<<nb(n), 256, 0, s>>>(pred, x, tag, inv_scale, sample_norm, B, ncell, n, inv_count, dpred, loss);
     FLUB_CHECK_LAUNCH();
     return FLUB_OK;
 }
@@ -408,20 +379,6 @@ int flub_unet_output(const float *out, const int32_t *tag, const float *inv_scal
     FLUB_REQUIRE(out && tag && inv_scale && x0, "flub_unet_output: bad arguments");
     const int64_t n = (int64_t)B * ncell;
     k_unet_output<<<nb(n), 256, 0, as_stream(stream)>>>(out, tag, inv_scale, ncell, n, gain, x0);
-    FLUB_CHECK_LAUNCH();
-    return FLUB_OK;
-}
-
-int flub_conv3d_wgrad(const void *x, int cin, const void *dy, int cout, float *dw, float *db, int B, int NX, int NY,
-                      int NZ, void *stream) {
-    auto okc = [](int c) { return c == 16 || c == 32 || c == 64; };
-    FLUB_REQUIRE(x && dy && dw && okc(cin) && okc(cout), "flub_conv3d_wgrad: bad arguments");
-    const int64_t nvox = (int64_t)B * NX * NY * NZ;
-    const int64_t nchunk = (nvox + kWgChunk - 1) / kWgChunk;
-    const unsigned gx = (unsigned)(nchunk < 128 ? nchunk : 128);
-    k_conv_wgrad<<<dim3(gx, 27), 256, 0, as_stream(stream)>>>(static_cast<const __nv_bfloat16 *>(x), cin,
-                                                              static_cast<const __nv_bfloat16 *>(dy), cout, dw, db,
-                                                              B, NX, NY, NZ);
     FLUB_CHECK_LAUNCH();
     return FLUB_OK;
 }

@@ -111,6 +111,48 @@ class MGPCG:
         x0 = x0.contiguous()
         _lib.check(self._lib.flub_mg_set_x0(self._h, ctypes.c_void_p(x0.data_ptr()), _stream()), "flub_mg_set_x0")
 
+    def set_initial_guess_scaled(self, d):
+        """Warm start x0 = gamma d, gamma = (d . b) / (d . L d) computed on the
+        device (no reference counterpart; the guess is never worse than 0 in
+        the energy norm)."""
+        d = d.contiguous()
+        _lib.check(self._lib.flub_mg_set_x0_scaled(self._h, ctypes.c_void_p(d.data_ptr()), _stream()),
+                   "flub_mg_set_x0_scaled")
+
+    def level_shape(self, level):
+        nx, ny, nz = ctypes.c_int(), ctypes.c_int(), ctypes.c_int()
+        _lib.check(self._lib.flub_mg_level_shape(self._h, int(level), ctypes.byref(nx), ctypes.byref(ny),
+                                                 ctypes.byref(nz)), "flub_mg_level_shape")
+        return (nx.value, ny.value, nz.value)
+
+    def level_tags(self, level, out=None):
+        """Tags of a level of the hierarchy (0 air, 1 fluid, 2 solid)."""
+        if out is None:
+            out = torch.empty(self.level_shape(level), dtype=torch.int32, device=self.device)
+        _lib.check(self._lib.flub_mg_level_tags(self._h, int(level), ctypes.c_void_p(out.data_ptr()), _stream()),
+                   "flub_mg_level_tags")
+        return out
+
+    def restrict_vector(self, level, fine, coarse=None):
+        """Level-(l-1) vector -> level l: sum of the 8 children on coarse fluid cells."""
+        if coarse is None:
+            coarse = torch.empty(self.level_shape(level), dtype=torch.float32, device=self.device)
+        fine = fine.contiguous()
+        _lib.check(self._lib.flub_mg_restrict_vector(self._h, int(level), ctypes.c_void_p(fine.data_ptr()),
+                                                     ctypes.c_void_p(coarse.data_ptr()), _stream()),
+                   "flub_mg_restrict_vector")
+        return coarse
+
+    def prolong_vector(self, level, coarse, fine=None):
+        """Level-l vector -> level l-1 by cell-centred trilinear interpolation."""
+        if fine is None:
+            fine = torch.empty(self.level_shape(level - 1), dtype=torch.float32, device=self.device)
+        coarse = coarse.contiguous()
+        _lib.check(self._lib.flub_mg_prolong_vector(self._h, int(level), ctypes.c_void_p(coarse.data_ptr()),
+                                                    ctypes.c_void_p(fine.data_ptr()), _stream()),
+                   "flub_mg_prolong_vector")
+        return fine
+
     def solve(self, max_iters=1, eps=1e-12, abs_tol=1e-12, rel_tol=1e-12, verbose=False, smoother="default",
               x0=None, sync=True):
         """mgpcg.py:378-462.  With sync=False the solve is only enqueued on the

@@ -30,10 +30,12 @@ class Projection:
         return self.tag
 
     def project(self, vel: MACGrid, vel_rigid: MACGrid, phi=None, prims=(), tag=None, max_iters=200, eps=1e-12,
-                abs_tol=0.0, rel_tol=1e-12, smoother="phases", x0=None, sync=True):
+                abs_tol=0.0, rel_tol=1e-12, smoother="phases", x0=None, warm_start=None, sync=True):
         """Project ``vel`` in place.  Either the level set ``phi`` (+ solid
-        primitives) or ready ``tag``s must be given.  Returns the solve info
-        (sync=True) or None (the work is only enqueued)."""
+        primitives) or ready ``tag``s must be given.  ``x0`` (a pressure guess
+        in solver units) or ``warm_start`` (a learned.WarmStart) start CG from
+        a guess; the tolerance stays relative to the right-hand side.  Returns
+        the solve info (sync=True) or None (the work is only enqueued)."""
         if tag is not None:
             self.tag.f.copy_(tag.f if hasattr(tag, "f") else tag)
         else:
@@ -45,6 +47,8 @@ class Projection:
         mg.mask_interior()
         if x0 is not None:
             mg.set_initial_guess(x0)
+        elif warm_start is not None:
+            warm_start.apply(mg)
         mg.solve(max_iters, eps, abs_tol, rel_tol, smoother=smoother, sync=False)
         mg.get_x(self.p.f, self.h0)
         K.subtract_gradient(vel, vel_rigid, self.p, self.tag, p_scale=1.0 / self.h0)

@@ -171,31 +171,96 @@ def _default_levels(n):
     return levels
 
 
-def random_scene(n, seed, levels=None):
-    """Random fluid boxes, water spheres and solid boxes with a seeded Fourier
-    velocity field (training/evaluation scenes for the learned warm start)."""
+def _random_layout(seed):
+    """The random parts of a training scene: fluid boxes, water spheres and
+    solid boxes, drawn in a fixed order from one seeded generator."""
     rng = np.random.default_rng(seed + 7919)
-    shape = (n, n, n)
-    phi = np.full(shape, 1.0)
+    boxes, spheres, objs = [], [], []
     for _ in range(rng.integers(1, 3)):
         xm, ym = rng.uniform(0.2, 0.6), rng.uniform(0.2, 0.7)
-        x, y, z = _centres(shape)
         zlo, zhi = sorted(rng.uniform(0.0, 1.0, 2))
         zlo, zhi = (0.0, 1.0) if rng.random() < 0.5 else (zlo * 0.5, 0.5 + zhi * 0.5)
-        b = np.maximum(np.maximum(x - xm, y - ym), np.maximum(zlo - z, z - zhi)) + np.zeros(shape)
-        if rng.random() < 0.5:
-            b = b[::-1].copy()
-        phi = np.minimum(phi, b)
+        boxes.append((xm, ym, zlo, zhi, bool(rng.random() < 0.5)))
     for _ in range(rng.integers(0, 3)):
         c = rng.uniform(0.2, 0.8, 3)
-        phi = np.minimum(phi, _sphere_phi(shape, c, rng.uniform(0.05, 0.15)))
-    objs = []
+        spheres.append((c, rng.uniform(0.05, 0.15)))
     for _ in range(rng.integers(0, 3)):
         c = rng.uniform(0.15, 0.85, 3)
         objs.append(dict(geometry=GEOM_BOX, x=tuple(c), radius=float(rng.uniform(0.03, 0.1))))
+    return boxes, spheres, objs
+
+
+def random_scene(n, seed, levels=None):
+    """Random fluid boxes (one or two, optionally mirrored in x and cut in z),
+    up to two water spheres and up to two solid boxes, with a seeded Fourier
+    velocity field (training/evaluation scenes for the learned warm start)."""
+    shape = (n, n, n)
+    boxes, spheres, objs = _random_layout(seed)
+    x, y, z = _centres(shape)
+    phi = np.full(shape, 1.0)
+    for xm, ym, zlo, zhi, flip in boxes:
+        b = np.maximum(np.maximum(x - xm, y - ym), np.maximum(zlo - z, z - zhi)) + np.zeros(shape)
+        if flip:
+            b = b[::-1].copy()
+        phi = np.minimum(phi, b)
+    for c, r in spheres:
+        phi = np.minimum(phi, _sphere_phi(shape, c, r))
     u, v, w = fourier_faces(shape, seed)
     zeros = [np.zeros_like(a) for a in (u, v, w)]
     return Scene(f"rand{n}_{seed}", shape, levels or _default_levels(n), phi.astype(np.float32),
+                 make_prims(objs), u, v, w, *zeros, seed=seed)
+
+
+def fourier_faces_device(shape, seed, device, n_modes=16, kmax=8, noise=0.01):
+    """fourier_faces evaluated with torch on ``device`` (float64, stored FP32):
+    the same modes, amplitudes and phases; the U(-noise, noise) noise comes
+    from a torch generator on the device seeded with ``seed``."""
+    import torch
+    nx, ny, nz = shape
+    h = 1.0 / nx
+    rng = np.random.default_rng(seed)
+    ks = rng.integers(1, kmax + 1, size=(n_modes, 3))
+    amps = rng.standard_normal((n_modes, 3)) / np.sum(ks.astype(np.float64) ** 2, axis=1, keepdims=True)
+    phases = rng.uniform(0.0, 2.0 * np.pi, n_modes)
+    gen = torch.Generator(device=device).manual_seed(int(seed))
+    out = []
+    for c, fs in enumerate(face_shapes(shape)):
+        st = [0.5, 0.5, 0.5]
+        st[c] = 0.0
+        xs = [(torch.arange(fs[a], dtype=torch.float64, device=device) + st[a]) * h for a in range(3)]
+        acc = torch.zeros(fs, dtype=torch.float64, device=device)
+        for m in range(n_modes):
+            ax = 2 * np.pi * ks[m, 0] * xs[0] + phases[m]
+            ay = 2 * np.pi * ks[m, 1] * xs[1]
+            az = 2 * np.pi * ks[m, 2] * xs[2]
+            sxy = torch.sin(ax)[:, None] * torch.cos(ay)[None, :] + torch.cos(ax)[:, None] * torch.sin(ay)[None, :]
+            cxy = torch.cos(ax)[:, None] * torch.cos(ay)[None, :] - torch.sin(ax)[:, None] * torch.sin(ay)[None, :]
+            acc += amps[m, c] * (sxy[:, :, None] * torch.cos(az)[None, None, :] +
+                                 cxy[:, :, None] * torch.sin(az)[None, None, :])
+        nz_ = torch.rand(fs, generator=gen, dtype=torch.float64, device=device) * (2 * noise) - noise
+        out.append((acc + nz_).float())
+    return out
+
+
+def random_scene_device(n, seed, device, levels=None):
+    """random_scene built with torch on ``device`` (the same layout; phi and
+    faces are device tensors), for generating training sets quickly."""
+    import torch
+    shape = (n, n, n)
+    boxes, spheres, objs = _random_layout(seed)
+    c = (torch.arange(n, dtype=torch.float64, device=device) + 0.5) / n
+    x, y, z = c[:, None, None], c[None, :, None], c[None, None, :]
+    phi = torch.full(shape, 1.0, dtype=torch.float64, device=device)
+    for xm, ym, zlo, zhi, flip in boxes:
+        b = torch.maximum(torch.maximum(x - xm, y - ym), torch.maximum(zlo - z, z - zhi)).expand(shape)
+        if flip:
+            b = b.flip(0)
+        phi = torch.minimum(phi, b)
+    for cc, r in spheres:
+        phi = torch.minimum(phi, torch.sqrt((x - cc[0]) ** 2 + (y - cc[1]) ** 2 + (z - cc[2]) ** 2) - r)
+    u, v, w = fourier_faces_device(shape, seed, device)
+    zeros = [torch.zeros_like(a) for a in (u, v, w)]
+    return Scene(f"rand{n}_{seed}", shape, levels or _default_levels(n), phi.float().contiguous(),
                  make_prims(objs), u, v, w, *zeros, seed=seed)
 
 

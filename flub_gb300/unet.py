@@ -160,15 +160,18 @@ def head_bwd(x, w, dout, dw, db, dx=None):
     return dx
 
 
-def unet_loss(pred, x, tag, inv_scale, inv_count, dpred=None, loss=None):
+def unet_loss(pred, x, tag, inv_scale, inv_count=None, relative=False, dpred=None, loss=None):
+    """Masked MSE of the normalised prediction; relative=True weights each
+    sample by 1 / |target|^2 (mean relative squared error)."""
     B = pred.shape[0]
     ncell = pred[0].numel()
     if dpred is None:
         dpred = torch.empty_like(pred)
     if loss is None:
         loss = torch.zeros(1, dtype=torch.float64, device=pred.device)
-    _lib.call("flub_unet_loss", _p(pred), _p(x), _p(tag), _p(inv_scale), ncell, B, float(inv_count), _p(dpred),
-              _p(loss), _s())
+    norm = torch.empty(B, dtype=torch.float64, device=pred.device) if relative else None
+    _lib.call("flub_unet_loss", _p(pred), _p(x), _p(tag), _p(inv_scale), ncell, B,
+              float(inv_count) if inv_count is not None else 0.0, _p(norm), _p(dpred), _p(loss), _s())
     return dpred, loss
 
 
@@ -359,15 +362,18 @@ class UNet3D:
         g = relu_bwd(g, a["e0a"])
         conv_back("enc0a", a["in"], g, need_dx=False)
 
-    def loss_and_grad(self, div, tag, x):
+    def loss_and_grad(self, div, tag, x, relative=True):
         """Masked MSE of the normalised prediction against x (the converged
-        solution); accumulates gradients.  Returns the loss (device scalar)."""
+        solution), by default relative per sample (mean of
+        |pred - t|^2 / |t|^2); accumulates gradients.  Returns the loss
+        (device scalar)."""
         if div.dim() == 3:
             div, tag, x = div.unsqueeze(0), tag.unsqueeze(0), x.unsqueeze(0)
         out, inv = self.forward(div, tag, keep=True)
-        nfluid = (tag == 1).sum()
-        inv_count = 1.0 / max(int(nfluid.item()), 1)
-        dout, loss = unet_loss(out, x.contiguous(), tag.contiguous(), inv, inv_count)
+        inv_count = None
+        if not relative:
+            inv_count = 1.0 / max(int((tag == 1).sum().item()), 1)
+        dout, loss = unet_loss(out, x.contiguous(), tag.contiguous(), inv, inv_count, relative=relative)
         self.backward(dout)
         self._acts = None
         return loss

@@ -136,6 +136,8 @@ typedef struct flub_solve_info {
     double rtr0;    /* initial squared residual norm (x0 = 0 residual) */
     double rtr;     /* final squared residual norm */
     double tol;     /* the squared-norm tolerance used */
+    double x0_scale; /* scale applied to the initial guess: 0 none, 1 flub_mg_set_x0,
+                        gamma for flub_mg_set_x0_scaled */
 } flub_solve_info;
 
 /* Bytes of device workspace a handle of this shape needs. */
@@ -219,6 +221,28 @@ int flub_mg_smooth(flub_mg *mg, int level, int phase, void *stream);
 int flub_vcycle_noalloc(const int32_t *tag, const float *r, float *z, int nx, int ny, int nz, int levels,
                         void *stream);
 
+/* Warm start scaled on the device (no reference counterpart): x0 = gamma d
+ * with gamma = (d . b) / (d . L d) over fluid cells, b the current right-hand
+ * side (flub_mg_init + flub_mg_mask_interior), L the solver's operator --
+ * the multiple of d closest to the solution in the energy norm, so the guess
+ * is never worse than x0 = 0 in that norm.  Used by the next flub_mg_solve
+ * only; gamma is reported in flub_solve_info.x0_scale.  No synchronisation. */
+int flub_mg_set_x0_scaled(flub_mg *mg, const float *d, void *stream);
+
+/* Extents of level l of the hierarchy (shape >> l). */
+int flub_mg_level_shape(flub_mg *mg, int level, int *nx, int *ny, int *nz);
+/* Cell tags of level l (the reference's convention, 0 air / 1 fluid /
+ * 2 solid; levels >= 1 follow multigrid/mgpcg.py:162-174 restrict_tag), as set
+ * by the last flub_mg_set_tags. */
+int flub_mg_level_tags(flub_mg *mg, int level, int32_t *tag, void *stream);
+/* coarse (level l) = sum of the 8 children in fine (level l - 1), 0 at coarse
+ * cells that are not fluid: the V-cycle's restriction of a residual. */
+int flub_mg_restrict_vector(flub_mg *mg, int level, const float *fine, float *coarse, void *stream);
+/* fine (level l - 1) = cell-centred trilinear interpolation of coarse (level
+ * l) at fine fluid cells, 0 elsewhere; coarse air cells count as 0, solid and
+ * outside cells are left out with the weights renormalised. */
+int flub_mg_prolong_vector(flub_mg *mg, int level, const float *coarse, float *fine, void *stream);
+
 /* Solver kernels executed on the device inside solve graphs by this handle
  * since it was created (each kernel node counts once per execution).
  * Synchronises the stream. */
@@ -253,7 +277,9 @@ int flub_conv3d_bf16(const void *x0, int cin0, const void *w0, const void *x1, i
                      const float *bias, void *y, int cout, int B, int NX, int NY, int NZ, int relu, void *stream);
 /* Weight and bias gradients of one source of flub_conv3d_bf16, accumulated:
  * dw[27][cout][cin] += sum_v dy[v][co] x[v + tap][ci]; db[cout] += sum dy
- * (db may be NULL, e.g. for the second source of a two-source convolution). */
+ * (db may be NULL, e.g. for the second source of a two-source convolution).
+ * tcgen05 GEMM over the voxels; same shape rules as flub_conv3d_bf16.
+ * Accumulates with float atomics: the summation order is not fixed. */
 int flub_conv3d_wgrad(const void *x, int cin, const void *dy, int cout, float *dw, float *db, int B, int NX, int NY,
                       int NZ, void *stream);
 /* Non-zero in *out if a convolution kernel gave up on a bounded wait since the
@@ -280,12 +306,14 @@ int flub_relu_bwd_bf16(const void *dy, const void *y, void *dx, int64_t n, void 
 int flub_head_fwd(const void *x, const float *w, const float *b, float *out, int64_t n, void *stream);
 int flub_head_bwd(const void *x, const float *w, const float *dout, void *dx, float *dw, float *db, int64_t n,
                   void *stream);
-/* Masked MSE against the normalised target x * inv_scale[b]:
- * *loss += inv_count * sum over fluid cells of (pred - x * inv_scale)^2, with
- * inv_count normally 1 / (fluid cells of the batch); dpred = d loss / d pred
- * (0 off fluid). */
+/* Masked MSE against the normalised target t = x * inv_scale[b] over fluid
+ * cells: *loss += sum of w_b (pred - t)^2 and dpred = d loss / d pred (0 off
+ * fluid).  With sample_norm == NULL, w_b = inv_count (normally 1 / the
+ * batch's fluid cells); otherwise sample_norm (B doubles of device memory)
+ * receives |t_b|^2 and w_b = 1 / (B |t_b|^2): the mean relative squared
+ * error of the samples. */
 int flub_unet_loss(const float *pred, const float *x, const int32_t *tag, const float *inv_scale, int64_t ncell,
-                   int B, double inv_count, float *dpred, double *loss, void *stream);
+                   int B, double inv_count, double *sample_norm, float *dpred, double *loss, void *stream);
 /* Pressure guess from the network output: x0 = out / inv_scale * gain on
  * fluid cells, 0 elsewhere. */
 int flub_unet_output(const float *out, const int32_t *tag, const float *inv_scale, int64_t ncell, int B, float gain,

@@ -102,18 +102,27 @@ def forward(params, div, tag, bf16=True):
     return out, inv
 
 
-def loss_fn(out, x, tag, inv):
-    """Masked MSE of the normalised prediction (mean over the batch's fluid cells)."""
+def loss_fn(out, x, tag, inv, relative=False):
+    """Masked MSE of the normalised prediction: the mean over the batch's fluid
+    cells, or (relative=True) the mean over samples of |out - t|^2 / |t|^2."""
     fl = tag == 1
     B = out.shape[0]
-    d = out - x.double() * inv.view(B, 1, 1, 1)
-    return (d[fl] ** 2).sum() / max(int(fl.sum()), 1)
+    t = x.double() * inv.view(B, 1, 1, 1)
+    d = out - t
+    if not relative:
+        return (d[fl] ** 2).sum() / max(int(fl.sum()), 1)
+    total = 0.0
+    for b in range(B):
+        nb = float((t[b][fl[b]] ** 2).sum())
+        if nb > 0:
+            total = total + (d[b][fl[b]] ** 2).sum() / (B * nb)
+    return total
 
 
-def loss_and_grads(params, div, tag, x, bf16=True):
+def loss_and_grads(params, div, tag, x, bf16=True, relative=True):
     """Float64 loss and d loss / d param for every parameter."""
     leaf = {k: v.detach().clone().double().requires_grad_(True) for k, v in params.items()}
     out, inv = forward(leaf, div, tag, bf16=bf16)
-    loss = loss_fn(out, x, tag, inv)
+    loss = loss_fn(out, x, tag, inv, relative=relative)
     loss.backward()
     return float(loss.detach()), {k: v.grad.detach() for k, v in leaf.items()}, out.detach()

@@ -161,12 +161,13 @@ def test_input_loss_output():
     pred = _rand(shape, g).float()
     x = _rand(shape, g).float()
     cnt = int((tag == 1).sum())
-    dpred, loss = U.unet_loss(pred.to(_dev()), x.to(_dev()), tag.to(_dev()), inv, 1.0 / cnt)
-    pr = pred.double().requires_grad_(True)
-    lr = R.loss_fn(pr, x, tag, rinv)
-    lr.backward()
-    assert abs(float(loss) - float(lr.detach())) <= 1e-5 * float(lr.detach())
-    assert _rel(dpred, pr.grad) <= 1e-5
+    for relative in (False, True):
+        dpred, loss = U.unet_loss(pred.to(_dev()), x.to(_dev()), tag.to(_dev()), inv, 1.0 / cnt, relative=relative)
+        pr = pred.double().requires_grad_(True)
+        lr = R.loss_fn(pr, x, tag, rinv, relative=relative)
+        lr.backward()
+        assert abs(float(loss) - float(lr.detach())) <= 1e-5 * float(lr.detach())
+        assert _rel(dpred, pr.grad) <= 1e-5
     x0 = U.unet_output(pred.to(_dev()), tag.to(_dev()), inv, gain=0.5)
     ref = torch.where(tag == 1, pred.double() / rinv.view(2, 1, 1, 1) * 0.5, 0.0)
     assert _rel(x0, ref) <= 1e-6
@@ -256,3 +257,69 @@ def test_unet_training_reduces_loss():
         losses.append(float(net.loss_and_grad(d, t, xx)))
         net.adam_step(lr=1e-3)
     assert losses[-1] < 0.5 * losses[0], losses
+
+
+def test_learned_pipeline_small():
+    """Data generation by the plain solver, a few training steps, and the
+    cold/warm evaluation at 64^3: every solve converges to the same tolerance,
+    and the scaled guess never starts above the cold residual in energy."""
+    from flub_gb300 import learned
+    from flub_gb300.unet import UNet3D
+    dev = _dev()
+    data = learned.generate(6, 64, seed0=123, device=dev)
+    assert (data.iters > 0).all()
+    net = UNet3D(device=dev, seed=0)
+    losses = learned.train(net, data, epochs=4, batch=2, lr=1e-3, seed=0)
+    assert len(losses) == 12 and all(math.isfinite(l) for l in losses)
+    summary, rows = learned.evaluate(net, data, "fp32")
+    assert summary["all_converged"]
+    for r in rows:
+        assert math.isfinite(r["gamma"])
+        assert r["warm"] <= r["cold"] + 2, r
+        assert r["err_warm"] <= 1e-3 and r["err_cold"] <= 1e-3, r
+
+
+def test_warm_start_support_kernels_match_reference_formulas():
+    """Level tags, restriction, trilinear prolongation and the device-scaled
+    guess against plain float64 restatements on the CPU."""
+    from flub_gb300 import MGPCG, scenes
+    from flub_gb300 import kernels as K
+    from flub_gb300.fields import Field, MACGrid
+    from oracle import np_oracle
+    sc = scenes.random_scene(32, 7)
+    dev = _dev()
+    tag = K.classify(torch.as_tensor(sc.phi).to(dev), sc.prims, sc.h, sc.h0)
+    tagf = tag.f if hasattr(tag, "f") else tag
+    vel = MACGrid(*(Field(torch.as_tensor(a).to(dev), d=d + 1) for d, a in enumerate((sc.u, sc.v, sc.w))))
+    velr = MACGrid(*(Field(torch.as_tensor(a).to(dev), d=d + 1) for d, a in enumerate((sc.ur, sc.vr, sc.wr))))
+    div = K.divergence(vel, velr, tag, scale=-1.0 / sc.h)
+    mg = MGPCG(3, sc.shape, sc.levels, float, device=dev)
+    mg.set_tags(tag)
+    mg.init(div, -sc.h0)
+    mg.mask_interior()
+    t0 = tagf.cpu().numpy()
+    t1 = mg.level_tags(1).cpu().numpy()
+    assert np.array_equal(t1, np_oracle.tag_levels(t0, 2)[1])
+    b = mg.r0.view(sc.shape).clone()
+    bc = mg.restrict_vector(1, b).cpu().double().numpy()
+    ref = b.cpu().double().numpy().reshape(16, 2, 16, 2, 16, 2).sum((1, 3, 5))
+    ref[t1 != 1] = 0
+    assert np.allclose(bc, ref, rtol=1e-5, atol=1e-6 * np.abs(ref).max())
+    # trilinear prolongation of a linear function is exact away from walls
+    I = np.arange(16)[:, None, None] + 0 * np.arange(16)[None, :, None] + 0 * np.arange(16)[None, None, :]
+    lin = (1.0 + 0.5 * I).astype(np.float32)
+    allfluid = MGPCG(3, (32, 32, 32), 3, float, device=dev)
+    allfluid.set_tags(torch.ones((32, 32, 32), dtype=torch.int32, device=dev))
+    f = allfluid.prolong_vector(1, torch.as_tensor(lin).to(dev)).cpu().numpy()
+    i = np.arange(32)
+    exact = 1.0 + 0.5 * ((i + 0.5) / 2 - 0.5)
+    assert np.allclose(f[1:-1, 5, 5], exact[1:-1], atol=1e-6)
+    # scaled guess: gamma = (d . b) / (d . L d)
+    g = torch.Generator(device=dev).manual_seed(1)
+    d = torch.randn(sc.shape, generator=g, device=dev) * (tagf == 1)
+    mg.set_initial_guess_scaled(d)
+    info = mg.solve(200, 1e-12, 0.0, 1e-12, smoother="phases")
+    dn = d.cpu().double().numpy()
+    gamma = float((dn * b.cpu().double().numpy()).sum() / (dn * np_oracle.matvec(dn, t0)).sum())
+    assert abs(info["x0_scale"] - gamma) <= 1e-5 * abs(gamma)
+    assert info["converged"]
