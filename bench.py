@@ -36,6 +36,8 @@ SMOOTH_HALF_SWEEP_BYTES_PER_CELL = 6.5  # red + black iteration: R z, r, tag; W 
 VARIANTS = {
     "plain": "plain FP32 MGPCG (reference V-cycle, FP64 inner products)",
     "mixed": "mixed-precision MGPCG (FP16 V-cycle levels, FP32 arithmetic, flexible CG, FP64 inner products)",
+    "learned+mixed": "mixed-precision MGPCG started from the U-Net warm start (network on the 128^3 level of the "
+                     "hierarchy, trilinear prolongation, energy-optimal scale), same tolerance",
 }
 
 
@@ -46,12 +48,14 @@ def parse_args():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
     ap.add_argument("--config", default="dam256")
-    ap.add_argument("--variant", choices=sorted(VARIANTS), default="mixed",
+    ap.add_argument("--variant", choices=sorted(VARIANTS), default="learned+mixed",
                     help="the variant the headline value is measured on (the others are timed beside it)")
     ap.add_argument("--cpu-baseline-steps", type=int, default=2)
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-oracle-check", action="store_true",
+                    help="skip the FP64 host projection that checks each variant's pressure")
     ap.add_argument("--no-e2e", action="store_true")
-    ap.add_argument("--profile-kernel", choices=["smooth", "restrict", "matvec", "solve"], default=None,
+    ap.add_argument("--profile-kernel", choices=["smooth", "restrict", "matvec", "solve", "project"], default=None,
                     help="set up the 256^3 solver state and launch only this kernel 3 times (for ncu)")
     return ap.parse_args()
 
@@ -60,12 +64,25 @@ def run_profile_kernel(args):
     """Small, bounded process for an ncu capture: the solver state of the
     benchmark scene on the device (about 0.6 GB) and three launches of one kernel."""
     import torch
-    from flub_gb300 import MGPCG, scenes
+    from flub_gb300 import MGPCG, Projection, learned, scenes
     from flub_gb300 import kernels as K
     from flub_gb300.fields import Field, MACGrid
+    from flub_gb300.unet import UNet3D
 
     scene = scenes.CONFIGS[args.config]()
     dev = lambda a: torch.from_numpy(np.ascontiguousarray(a)).cuda()
+    if args.profile_kernel == "project":
+        # one whole projection of the chosen variant (every kernel launch of one step)
+        proj = Projection(scene.shape, scene.levels, precision="fp32" if args.variant == "plain" else "mixed")
+        ws = learned.WarmStart(UNet3D.load(learned.WEIGHTS)) if args.variant == "learned+mixed" else None
+        vel = MACGrid(*(Field(dev(a), d=d + 1) for d, a in enumerate((scene.u, scene.v, scene.w))))
+        velr = MACGrid(*(Field(dev(a), d=d + 1) for d, a in enumerate((scene.ur, scene.vr, scene.wr))))
+        info = proj.project(vel, velr, dev(scene.phi), scene.prims, max_iters=200, eps=1e-12, abs_tol=0.0,
+                            rel_tol=1e-12, smoother="phases", warm_start=ws)
+        torch.cuda.synchronize()
+        print(json.dumps({"profile_kernel": "project", "variant": args.variant, "iterations": info["iterations"],
+                          "ok": bool(info["converged"])}))
+        return 0
     tag = K.classify(dev(scene.phi), scene.prims, scene.h, scene.h0)
     vel = MACGrid(*(Field(dev(a), d=d + 1) for d, a in enumerate((scene.u, scene.v, scene.w))))
     velr = MACGrid(*(Field(dev(a), d=d + 1) for d, a in enumerate((scene.ur, scene.vr, scene.wr))))
@@ -79,8 +96,8 @@ def run_profile_kernel(args):
     torch.cuda.synchronize()
     torch.cuda.empty_cache()
     if args.profile_kernel == "smooth":
-        mg.apply_preconditioner()  # defined z everywhere (level hierarchy kernels run here too)
-        torch.cuda.synchronize()
+        # z is defined (set_tags clears every level's z): three level-0
+        # half-sweeps are the only smoother launches of this process
         for q in range(3):
             mg.smooth(0, q & 1)
     elif args.profile_kernel == "matvec":
@@ -219,8 +236,9 @@ def run_ours(args):
     if world > 1:
         dist.init_process_group(backend="nccl", device_id=torch.device("cuda", local_rank))
 
-    from flub_gb300 import Projection, _lib, scenes
+    from flub_gb300 import Projection, _lib, learned, scenes
     from flub_gb300.fields import Field, MACGrid
+    from flub_gb300.unet import UNet3D
 
     lib = _lib.load()
     seed_base = {"dam256": 2, "dam512": 2, "sphere128": 1, "box64": 0}.get(args.config, 0)
@@ -237,11 +255,15 @@ def run_ours(args):
     solve_kw = dict(max_iters=200, eps=1e-12, abs_tol=0.0, rel_tol=1e-12, smoother="phases")
     stream = torch.cuda.current_stream()
 
+    warm = {}
+
     def make_step(proj):
+        ws = warm.get(id(proj))
+
         def step():
             for a, b in zip((vel.u.f, vel.v.f, vel.w.f), vel0):
                 a.copy_(b)
-            proj.project(vel, velr, phi, scene.prims, sync=False, **solve_kw)
+            proj.project(vel, velr, phi, scene.prims, sync=False, warm_start=ws, **solve_kw)
         return step
 
     def time_variant(proj, sample_clocks):
@@ -282,14 +304,29 @@ def run_ours(args):
     variants = {"plain": Projection(scene.shape, scene.levels, precision="fp32"),
                 "mixed": Projection(scene.shape, scene.levels, precision="mixed")}
     head = args.variant
+    learned_info = None
+    if os.path.exists(learned.WEIGHTS):
+        variants["learned+mixed"] = Projection(scene.shape, scene.levels, precision="mixed")
+        net = UNet3D.load(learned.WEIGHTS)
+        warm[id(variants["learned+mixed"])] = learned.WarmStart(net)
+        learned_info = {"weights": os.path.relpath(learned.WEIGHTS, ROOT), "parameters": net.num_parameters(),
+                        "network_level": warm[id(variants["learned+mixed"])].choose_level(
+                            variants["learned+mixed"].mg)}
+    elif head == "learned+mixed":
+        head = "mixed"  # no trained weights in the tree: the headline is the mixed variant
     results = {}
+    pressures = {}
     for name, pj in variants.items():
         if name != head:
             el, inf, _, _ = time_variant(pj, False)
-            results[name] = {"ms_per_solve": el / args.steps, "iterations": inf["iterations"]}
+            results[name] = {"ms_per_solve": el / args.steps, "iterations": inf["iterations"],
+                             "x0_scale": inf["x0_scale"]}
+            pressures[name] = pj.p.f.detach().clone()
     proj = variants[head]
     elapsed, info, launches, clocks = time_variant(proj, True)
-    results[head] = {"ms_per_solve": elapsed / args.steps, "iterations": info["iterations"]}
+    results[head] = {"ms_per_solve": elapsed / args.steps, "iterations": info["iterations"],
+                     "x0_scale": info["x0_scale"]}
+    pressures[head] = proj.p.f.detach().clone()
     div_after = proj.max_abs_div(vel, velr)
     ms_per_step = elapsed / args.steps
     value = elapsed / (args.steps * world)
@@ -306,7 +343,7 @@ def run_ours(args):
         def step_e2e():
             for h, d in zip(h_in, d_in):
                 d.copy_(h, non_blocking=True)
-            proj.project(vel, velr, phi, scene.prims, sync=False, **solve_kw)
+            proj.project(vel, velr, phi, scene.prims, sync=False, warm_start=warm.get(id(proj)), **solve_kw)
             for h, d in zip(h_out, d_out):
                 h.copy_(d, non_blocking=True)
 
@@ -367,6 +404,15 @@ def run_ours(args):
         cpu = {"value": cpu_ms, "unit": UNIT, "cores": cores, "kind": "port",
                "sample": f"{args.cpu_baseline_steps} full {args.config} projections "
                          f"({cpu_res['iters']} CG iterations each), FP32 C restatement with OpenMP"}
+        if not args.no_oracle_check:
+            # the same projection in FP64 on the host checks every variant's pressure
+            import oracle as O
+            ref = O.project(scene, max_iters=200, rel_tol=1e-12, abs_tol=0.0, dtype=np.float64)
+            p64 = torch.from_numpy(ref["p"].astype(np.float64))
+            for name, pg in pressures.items():
+                pv = pg.double().cpu()
+                results[name]["pressure_rel_l2_vs_fp64_oracle"] = float((pv - p64).norm() / p64.norm())
+            cpu["fp64_oracle_iterations"] = int(ref["iters"])
 
     if rank == 0:
         out = {
@@ -376,7 +422,8 @@ def run_ours(args):
             "data": "synthetic (seeded dam-break scene and Fourier velocity field, generated on the host)",
             "config": {"workload": f"{args.config}: {scene.shape[0]}^3 dam-break projection (classify + divergence "
                                    f"+ MGPCG to rel. residual 1e-6 + gradient update)",
-                       "variant": VARIANTS[head], "variants_ms_per_solve": results, "levels": scene.levels,
+                       "variant": head, "variant_desc": VARIANTS[head], "variants_ms_per_solve": results,
+                       "learned": learned_info, "levels": scene.levels,
                        "iterations": info["iterations"], "converged": bool(info["converged"]),
                        "fluid_cells": int((proj.tag.f == 1).sum().item()), "cells": n,
                        "cell_iterations_per_s": n * info["iterations"] / (ms_per_step * 1e-3),

@@ -14,6 +14,7 @@ from .fields import (DEFAULT_SHAPE, Field, IntField, MACGrid, MACGridInt, field_
 from .kernels import (_tag_dirichlet, _tag_neumann, classify, divergence, divergence_tag, launch, mask_with_tag,
                       phi_prims, precompute_grid_point_phi_prims, scale_by_3d, subtract_gradient,
                       subtract_gradient_tag, tag_dirichlet, tag_neumann)
+from ._lib import FlubError
 from .mgpcg import MGPCG
 from .projection import Projection
 
@@ -21,5 +22,5 @@ __all__ = [
     "DEFAULT_SHAPE", "Field", "IntField", "MACGrid", "MACGridInt", "field_like", "field_shape", "get_uf",
     "make_field", "make_mac_grid", "_tag_dirichlet", "_tag_neumann", "classify", "divergence", "divergence_tag",
     "launch", "mask_with_tag", "phi_prims", "precompute_grid_point_phi_prims", "scale_by_3d", "subtract_gradient",
-    "subtract_gradient_tag", "tag_dirichlet", "tag_neumann", "MGPCG", "Projection",
+    "subtract_gradient_tag", "tag_dirichlet", "tag_neumann", "MGPCG", "Projection", "FlubError",
 ]

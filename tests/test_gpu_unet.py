@@ -323,3 +323,24 @@ def test_warm_start_support_kernels_match_reference_formulas():
     gamma = float((dn * b.cpu().double().numpy()).sum() / (dn * np_oracle.matvec(dn, t0)).sum())
     assert abs(info["x0_scale"] - gamma) <= 1e-5 * abs(gamma)
     assert info["converged"]
+
+
+def test_trained_network_saves_iterations():
+    """The committed network against the method without it on held-out 128^3
+    scenes (seeds outside the training range): every solve reaches the same
+    tolerance, and the warm start needs fewer CG iterations on average."""
+    import os
+    from flub_gb300 import learned
+    from flub_gb300.unet import UNet3D
+    if not os.path.exists(learned.WEIGHTS):
+        pytest.skip("no trained weights in the tree")
+    dev = _dev()
+    net = UNet3D.load(learned.WEIGHTS, device=dev)
+    data = learned.generate(6, 128, seed0=950000, device=dev)
+    summary, rows = learned.evaluate(net, data, "fp32")
+    assert summary["all_converged"]
+    assert summary["saved_mean"] >= 0.5, summary
+    for r in rows:
+        assert r["warm"] <= r["cold"], r
+        assert r["err_warm"] <= 1e-5, r
+        assert r["err_net"] < 0.5, r
