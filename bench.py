@@ -38,6 +38,20 @@ VARIANTS = {
     "mixed": "mixed-precision MGPCG (FP16 V-cycle levels, FP32 arithmetic, flexible CG, FP64 inner products)",
     "learned+mixed": "mixed-precision MGPCG started from the U-Net warm start (network on the 128^3 level of the "
                      "hierarchy, trilinear prolongation, energy-optimal scale), same tolerance",
+    "plain-v22": "FP32 MGPCG with the light V-cycle: 2+2 red-black iterations per level, 8+8 at the bottom, "
+                 "restriction scaled by 1/2 (flub_mg_set_schedule), same tolerance",
+    "mixed-v22": "mixed-precision MGPCG (FP16 V-cycle levels) with the light V-cycle, same tolerance",
+    "learned+mixed-v22": "mixed-precision MGPCG with the light V-cycle, started from the U-Net warm start, "
+                         "same tolerance",
+}
+# variant -> (precision, schedule, warm start)
+VARIANT_SETUP = {
+    "plain": ("fp32", "reference", False),
+    "mixed": ("mixed", "reference", False),
+    "learned+mixed": ("mixed", "reference", True),
+    "plain-v22": ("fp32", "v22", False),
+    "mixed-v22": ("mixed", "v22", False),
+    "learned+mixed-v22": ("mixed", "v22", True),
 }
 
 
@@ -48,7 +62,7 @@ def parse_args():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
     ap.add_argument("--config", default="dam256")
-    ap.add_argument("--variant", choices=sorted(VARIANTS), default="learned+mixed",
+    ap.add_argument("--variant", choices=sorted(VARIANTS), default="learned+mixed-v22",
                     help="the variant the headline value is measured on (the others are timed beside it)")
     ap.add_argument("--cpu-baseline-steps", type=int, default=2)
     ap.add_argument("--no-cpu-baseline", action="store_true")
@@ -73,8 +87,9 @@ def run_profile_kernel(args):
     dev = lambda a: torch.from_numpy(np.ascontiguousarray(a)).cuda()
     if args.profile_kernel == "project":
         # one whole projection of the chosen variant (every kernel launch of one step)
-        proj = Projection(scene.shape, scene.levels, precision="fp32" if args.variant == "plain" else "mixed")
-        ws = learned.WarmStart(UNet3D.load(learned.WEIGHTS)) if args.variant == "learned+mixed" else None
+        prec, sched, use_net = VARIANT_SETUP[args.variant]
+        proj = Projection(scene.shape, scene.levels, precision=prec, schedule=sched)
+        ws = learned.WarmStart(UNet3D.load(learned.WEIGHTS)) if use_net else None
         vel = MACGrid(*(Field(dev(a), d=d + 1) for d, a in enumerate((scene.u, scene.v, scene.w))))
         velr = MACGrid(*(Field(dev(a), d=d + 1) for d, a in enumerate((scene.ur, scene.vr, scene.wr))))
         info = proj.project(vel, velr, dev(scene.phi), scene.prims, max_iters=200, eps=1e-12, abs_tol=0.0,
@@ -301,19 +316,22 @@ def run_ours(args):
             elapsed = float(t.item())
         return elapsed, proj.mg.info(), launches, clocks
 
-    variants = {"plain": Projection(scene.shape, scene.levels, precision="fp32"),
-                "mixed": Projection(scene.shape, scene.levels, precision="mixed")}
     head = args.variant
+    have_net = os.path.exists(learned.WEIGHTS)
+    net = UNet3D.load(learned.WEIGHTS) if have_net else None
+    variants = {}
     learned_info = None
-    if os.path.exists(learned.WEIGHTS):
-        variants["learned+mixed"] = Projection(scene.shape, scene.levels, precision="mixed")
-        net = UNet3D.load(learned.WEIGHTS)
-        warm[id(variants["learned+mixed"])] = learned.WarmStart(net)
-        learned_info = {"weights": os.path.relpath(learned.WEIGHTS, ROOT), "parameters": net.num_parameters(),
-                        "network_level": warm[id(variants["learned+mixed"])].choose_level(
-                            variants["learned+mixed"].mg)}
-    elif head == "learned+mixed":
-        head = "mixed"  # no trained weights in the tree: the headline is the mixed variant
+    for name, (prec, sched, use_net) in VARIANT_SETUP.items():
+        if use_net and not have_net:
+            continue
+        pj = Projection(scene.shape, scene.levels, precision=prec, schedule=sched)
+        variants[name] = pj
+        if use_net:
+            warm[id(pj)] = learned.WarmStart(net)
+            learned_info = {"weights": os.path.relpath(learned.WEIGHTS, ROOT), "parameters": net.num_parameters(),
+                            "network_level": warm[id(pj)].choose_level(pj.mg)}
+    if head not in variants:
+        head = head.replace("learned+", "")  # no trained weights in the tree
     results = {}
     pressures = {}
     for name, pj in variants.items():

@@ -48,6 +48,9 @@ struct ClusterParams {
     float *z_top;        // its final correction (global)
     const __half *r_top_h;  // FP16 instead of r_top / z_top when not NULL (mixed precision)
     __half *z_top_h;
+    int nu;        // red-black iterations per side at every level (< 0: 6 << level, the reference's)
+    int nbottom;   // iterations of each of the two bottom orders (3 in the reference)
+    float rscale;  // restriction scale (1 in the reference)
 };
 
 struct ClusterCtx {
@@ -187,7 +190,7 @@ __device__ __forceinline__ void cl_restrict(const ClusterCtx &x, const ClusterPa
                         }
             }
             float *rdst = x.cl.map_shared_rank(cl_r(x, C), (unsigned)owner);
-            rdst[(lcp << (C.lg_ny + C.lg_nz)) + (J << C.lg_nz) + K] = s;
+            rdst[(lcp << (C.lg_ny + C.lg_nz)) + (J << C.lg_nz) + K] = __fmul_rn(s, P.rscale);
         }
     }
     x.cl.sync();
@@ -248,24 +251,24 @@ __global__ void __launch_bounds__(kClusterThreads, 1) k_cluster_vcycle(const Clu
     x.cl.sync();
     const int nb = P.nl - 1;
     for (int t = 0; t < nb; t++) {
-        const int iters = 6 << P.lv[t].abs_level;
+        const int iters = P.nu < 0 ? (6 << P.lv[t].abs_level) : P.nu;
         for (int it = 0; it < iters; it++) {
             cl_half(x, P, t, 0, it == 0);
             cl_half(x, P, t, 1, false);
         }
         cl_restrict(x, P, t);
     }
-    for (int it = 0; it < 3; it++) {
+    for (int it = 0; it < P.nbottom; it++) {
         cl_half(x, P, nb, 0, it == 0);
         cl_half(x, P, nb, 1, false);
     }
-    for (int it = 0; it < 3; it++) {
+    for (int it = 0; it < P.nbottom; it++) {
         cl_half(x, P, nb, 1, false);
         cl_half(x, P, nb, 0, false);
     }
     for (int t = nb - 1; t >= 0; t--) {
         cl_prolong(x, P, t);
-        const int iters = 6 << P.lv[t].abs_level;
+        const int iters = P.nu < 0 ? (6 << P.lv[t].abs_level) : P.nu;
         for (int it = 0; it < iters; it++) {
             cl_half(x, P, t, 1, false);
             cl_half(x, P, t, 0, false);

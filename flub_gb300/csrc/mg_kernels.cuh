@@ -223,7 +223,8 @@ __global__ void __launch_bounds__(256) k_smooth_half(float *__restrict__ z, cons
 // sums r + L z of its 8 children in (ii, jj, kk) order; 0 unless coarse fluid.
 __global__ void __launch_bounds__(256) k_restrict(const float *__restrict__ rf, const float *__restrict__ zf,
                                                   const uint8_t *__restrict__ cf, float *__restrict__ rc,
-                                                  const uint8_t *__restrict__ cc, Dims C, unsigned long long *kc) {
+                                                  const uint8_t *__restrict__ cc, Dims C, float scale,
+                                                  unsigned long long *kc) {
     count_kernel(kc);
     const Dims F{2 * C.nx, 2 * C.ny, 2 * C.nz};
     const int64_t n = C.n();
@@ -253,7 +254,7 @@ __global__ void __launch_bounds__(256) k_restrict(const float *__restrict__ rf, 
                     s = first ? v : __fadd_rn(s, v);
                     first = false;
                 }
-        rc[q] = s;
+        rc[q] = __fmul_rn(s, scale);  // scale 1: the reference's sum, exactly
     }
 }
 

@@ -78,11 +78,24 @@ struct flub_mg {
     int cl_start;    // first level run by the cluster kernel (== levels: none)
     int cl_size;     // blocks per cluster
     size_t cl_smem;
+    // V-cycle schedule (flub_mg_set_schedule); the reference's: -1, 3, 1
+    int sched_nu;        // red-black iterations per side at every level (< 0: 6 << level)
+    int sched_bottom;    // bottom: this many (0, 1) iterations, then as many (1, 0)
+    float sched_rscale;  // restriction scale
 };
 
 namespace flub {
 
 static inline size_t align256(size_t b) { return (b + 255) & ~(size_t)255; }
+
+static inline void reference_schedule(flub_mg *mg) {
+    mg->sched_nu = -1;
+    mg->sched_bottom = 3;
+    mg->sched_rscale = 1.0f;
+}
+
+// Red-black iterations per side at level l.
+static inline int level_iters(const flub_mg *mg, int l) { return mg->sched_nu < 0 ? (6 << l) : mg->sched_nu; }
 
 // Device address of the kernel counter inside the (device-resident) state.
 static inline unsigned long long *kernel_counter(flub_mg *mg) {
@@ -145,6 +158,9 @@ static size_t tail_layout(const flub_mg *mg, int lt, TailParams *P) {
         T.off_c = take(n);
     }
     P->nt = mg->levels - lt;
+    P->nu = mg->sched_nu;
+    P->nbottom = mg->sched_bottom;
+    P->rscale = mg->sched_rscale;
     return off;
 }
 
@@ -205,6 +221,9 @@ static size_t cluster_layout(const flub_mg *mg, int lc, int C, ClusterParams *P)
         L.off_r = take(sizeof(float) * L.P * plane);
     }
     P->nl = mg->levels - lc;
+    P->nu = mg->sched_nu;
+    P->nbottom = mg->sched_bottom;
+    P->rscale = mg->sched_rscale;
     return off;
 }
 
@@ -381,14 +400,14 @@ static int enqueue_vcycle(flub_mg *mg, const LaunchCtx &c, const float *r0, floa
     const int lg = lt < Lm - 1 ? lt : Lm - 1;  // levels 0 .. lg-1 restrict to a coarser level
     for (int l = 0; l < lg; l++) {
         const Level &L = mg->lv[l];
-        const int iters = 6 << l;
+        const int iters = level_iters(mg, l);
         for (int it = 0; it < iters; it++) {
             FLUB_TRY(sweep(c, L, 0, it == 0 ? kSweepFromZero : kSweepInPlace, sk, R(l), ZP(l), ZP(l), nullptr));
             FLUB_TRY(sweep(c, L, 1, kSweepInPlace, sk, R(l), ZP(l), ZP(l), nullptr));
         }
         const Level &C = mg->lv[l + 1];
         FLUB_TRY(launch_pdl(k_restrict, dim3(blocks_for(C.D.n(), 256, 1 << 20)), dim3(256), 0, c.s, R(l), ZP(l),
-                            L.code, C.r, C.code, C.D, c.kc));
+                            L.code, C.r, C.code, C.D, mg->sched_rscale, c.kc));
     }
     if (use_cl) {
         ClusterParams P = {};
@@ -414,18 +433,18 @@ static int enqueue_vcycle(flub_mg *mg, const LaunchCtx &c, const float *r0, floa
     } else {
         const int b = Lm - 1;
         const Level &L = mg->lv[b];
-        for (int it = 0; it < 3; it++) {
+        for (int it = 0; it < mg->sched_bottom; it++) {
             FLUB_TRY(sweep(c, L, 0, it == 0 ? kSweepFromZero : kSweepInPlace, SK(b), R(b), ZF(b), ZF(b), nullptr));
             FLUB_TRY(sweep(c, L, 1, kSweepInPlace, SK(b), R(b), ZF(b), ZF(b), nullptr));
         }
-        for (int it = 0; it < 3; it++) {
+        for (int it = 0; it < mg->sched_bottom; it++) {
             FLUB_TRY(sweep(c, L, 1, kSweepInPlace, SK(b), R(b), ZF(b), ZF(b), nullptr));
             FLUB_TRY(sweep(c, L, 0, kSweepInPlace, SK(b), R(b), ZF(b), ZF(b), nullptr));
         }
     }
     for (int l = lg - 1; l >= 0; l--) {
         const Level &L = mg->lv[l];
-        const int iters = 6 << l;
+        const int iters = level_iters(mg, l);
         for (int it = 0; it < iters; it++) {
             FLUB_TRY(sweep(c, L, 1, it == 0 ? kSweepProlong : kSweepInPlace, SK(l), R(l), ZP(l), ZF(l),
                            mg->lv[l + 1].z));
@@ -478,7 +497,7 @@ static int enqueue_vcycle_mixed(flub_mg *mg, const LaunchCtx &c, float *z0, bool
     const int lg = lt < Lm - 1 ? lt : Lm - 1;
     for (int l = 0; l < lg; l++) {
         const Level &L = mg->lv[l];
-        const int iters = 6 << l;
+        const int iters = level_iters(mg, l);
         for (int it = 0; it < iters; it++) {
             FLUB_TRY(sweep8<__half, __half, __half, __half>(c, L, 0, it == 0 ? kSweepFromZero : kSweepInPlace, sk,
                                                             L.rh, L.z2h, L.z2h, nullptr, 1.0f));
@@ -488,7 +507,7 @@ static int enqueue_vcycle_mixed(flub_mg *mg, const LaunchCtx &c, float *z0, bool
         const Level &C = mg->lv[l + 1];
         FLUB_TRY(launch_pdl(k_restrict_t<__half, __half, __half>, dim3(blocks_for(C.D.n(), 256, 1 << 20)), dim3(256),
                             0, c.s, (const __half *)L.rh, (const __half *)L.z2h, (const uint8_t *)L.code, C.rh,
-                            (const uint8_t *)C.code, C.D, 0.125f, c.kc));
+                            (const uint8_t *)C.code, C.D, 0.125f * mg->sched_rscale, c.kc));
     }
     if (lt < Lm) {
         if (lt == 0)
@@ -498,9 +517,9 @@ static int enqueue_vcycle_mixed(flub_mg *mg, const LaunchCtx &c, float *z0, bool
     } else {
         const int b = Lm - 1;
         const Level &L = mg->lv[b];
-        for (int q = 0; q < 6; q++) {
-            // bottom: 3 x (0, 1) from zero, then 3 x (1, 0)
-            const int ph0 = q < 3 ? 0 : 1, ph1 = 1 - ph0;
+        for (int q = 0; q < 2 * mg->sched_bottom; q++) {
+            // bottom: nbottom x (0, 1) from zero, then nbottom x (1, 0)
+            const int ph0 = q < mg->sched_bottom ? 0 : 1, ph1 = 1 - ph0;
             const int m0 = q == 0 ? kSweepFromZero : kSweepInPlace;
             if (b == 0) {
                 FLUB_TRY(sweep8<float, float, __half, float>(c, L, ph0, m0, sk0, L.rh, z0, z0, nullptr, 1.0f));
@@ -516,7 +535,7 @@ static int enqueue_vcycle_mixed(flub_mg *mg, const LaunchCtx &c, float *z0, bool
     for (int l = lg - 1; l >= 0; l--) {
         const Level &L = mg->lv[l];
         const __half *zc = mg->lv[l + 1].zh;
-        const int iters = 6 << l;
+        const int iters = level_iters(mg, l);
         for (int it = 0; it < iters; it++) {
             if (l == 0) {
                 if (it == 0)
@@ -878,6 +897,7 @@ size_t flub_mg_workspace_bytes(int nx, int ny, int nz, int levels, int precision
     if (validate_shape(nx, ny, nz, levels, precision)) return 0;
     flub_mg tmp;
     memset(&tmp, 0, sizeof(tmp));
+    reference_schedule(&tmp);
     tmp.nx = nx; tmp.ny = ny; tmp.nz = nz; tmp.levels = levels; tmp.precision = precision;
     tmp.n = (int64_t)nx * ny * nz;
     return carve(&tmp, nullptr);
@@ -890,6 +910,7 @@ int flub_mg_create(int nx, int ny, int nz, int levels, int precision, void *work
     FLUB_TRY(validate_shape(nx, ny, nz, levels, precision));
     flub_mg *mg = new flub_mg;
     memset(mg, 0, sizeof(*mg));
+    reference_schedule(mg);
     mg->nx = nx; mg->ny = ny; mg->nz = nz; mg->levels = levels; mg->precision = precision;
     mg->n = (int64_t)nx * ny * nz;
     const size_t need = carve(mg, nullptr);
@@ -1067,6 +1088,30 @@ int flub_mg_residual_history(flub_mg *mg, void *stream, double *out, int max_n, 
         FLUB_CHECK_CUDA(cudaMemcpy(out, mg->hist, sizeof(double) * n, cudaMemcpyDeviceToHost));
     }
     *n_out = n;
+    return FLUB_OK;
+}
+
+int flub_mg_set_schedule(flub_mg *mg, int smooth_iters, int bottom_iters, float restrict_scale) {
+    FLUB_REQUIRE(mg, "flub_mg_set_schedule: NULL handle");
+    FLUB_REQUIRE(smooth_iters == -1 || (smooth_iters >= 1 && smooth_iters <= 64),
+                 "flub_mg_set_schedule: smooth_iters must be -1 (the reference's 6 << level) or 1..64, got %d",
+                 smooth_iters);
+    FLUB_REQUIRE(bottom_iters >= 1 && bottom_iters <= 64, "flub_mg_set_schedule: bottom_iters must be 1..64, got %d",
+                 bottom_iters);
+    FLUB_REQUIRE(restrict_scale > 0.0f && restrict_scale <= 1.0f,
+                 "flub_mg_set_schedule: restrict_scale must be in (0, 1], got %g", (double)restrict_scale);
+    if (mg->sched_nu == smooth_iters && mg->sched_bottom == bottom_iters && mg->sched_rscale == restrict_scale)
+        return FLUB_OK;
+    // the captured solve graphs embed the schedule: drop them (recaptured by the next solve)
+    FLUB_CHECK_CUDA(cudaDeviceSynchronize());
+    for (int g = 0; g < 3; g++)
+        if (mg->graph[g]) {
+            cudaGraphExecDestroy(mg->graph[g]);
+            mg->graph[g] = nullptr;
+        }
+    mg->sched_nu = smooth_iters;
+    mg->sched_bottom = bottom_iters;
+    mg->sched_rscale = restrict_scale;
     return FLUB_OK;
 }
 
@@ -1248,6 +1293,7 @@ extern "C" int flub_vcycle_noalloc(const int32_t *tag, const float *r, float *z,
                  FLUB_NOALLOC_MAX_CELLS);
     flub_mg mg;  // host-side descriptor only; every level pointer points into the static array
     memset(&mg, 0, sizeof(mg));
+    reference_schedule(&mg);
     mg.nx = nx; mg.ny = ny; mg.nz = nz; mg.levels = levels; mg.n = n;
     const size_t need = noalloc_layout(&mg, nullptr);
     FLUB_REQUIRE(need <= kNoallocScratchBytes, "flub_vcycle_noalloc: hierarchy needs %zu bytes > %zu", need,

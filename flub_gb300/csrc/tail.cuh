@@ -33,6 +33,9 @@ struct TailParams {
     float *z_top;        // its correction (global)
     const __half *r_top_h;  // FP16 instead of r_top / z_top when not NULL (mixed precision)
     __half *z_top_h;
+    int nu;        // red-black iterations per side at every level (< 0: 6 << level, the reference's)
+    int nbottom;   // iterations of each of the two bottom orders (3 in the reference)
+    float rscale;  // restriction scale (1 in the reference)
 };
 
 // ---------------------------------------------------------------- lean smoothing
@@ -132,7 +135,7 @@ __device__ __forceinline__ void tail_half_lean(float *z, const TailCache &tc, co
 }
 
 __device__ __forceinline__ void tail_restrict(const float *rf, const float *zf, const uint8_t *cf, float *rc,
-                                              const uint8_t *cc, const Dims C) {
+                                              const uint8_t *cc, const Dims C, float rscale) {
     const Dims F{2 * C.nx, 2 * C.ny, 2 * C.nz};
     const int n = C.nx * C.ny * C.nz;
     for (int q = threadIdx.x; q < n; q += blockDim.x) {
@@ -160,7 +163,7 @@ __device__ __forceinline__ void tail_restrict(const float *rf, const float *zf, 
                     s = first ? v : __fadd_rn(s, v);
                     first = false;
                 }
-        rc[q] = s;
+        rc[q] = __fmul_rn(s, rscale);
     }
     __syncthreads();
 }
@@ -201,21 +204,21 @@ __global__ void __launch_bounds__(kTailThreads) k_tail_vcycle(const TailParams P
     for (int t = 0; t < nb; t++) {
         const Dims D = P.lv[t].D;
         tail_cache(tc, C(t), R(t), D);
-        const int iters = 6 << P.lv[t].abs_level;
+        const int iters = P.nu < 0 ? (6 << P.lv[t].abs_level) : P.nu;
         for (int it = 0; it < iters; it++) {
             tail_half_lean(Z(t), tc, D, 0, it == 0);
             tail_half_lean(Z(t), tc, D, 1, false);
         }
-        tail_restrict(R(t), Z(t), C(t), R(t + 1), C(t + 1), P.lv[t + 1].D);
+        tail_restrict(R(t), Z(t), C(t), R(t + 1), C(t + 1), P.lv[t + 1].D, P.rscale);
     }
     {
         const Dims D = P.lv[nb].D;
         tail_cache(tc, C(nb), R(nb), D);
-        for (int it = 0; it < 3; it++) {
+        for (int it = 0; it < P.nbottom; it++) {
             tail_half_lean(Z(nb), tc, D, 0, it == 0);
             tail_half_lean(Z(nb), tc, D, 1, false);
         }
-        for (int it = 0; it < 3; it++) {
+        for (int it = 0; it < P.nbottom; it++) {
             tail_half_lean(Z(nb), tc, D, 1, false);
             tail_half_lean(Z(nb), tc, D, 0, false);
         }
@@ -224,7 +227,7 @@ __global__ void __launch_bounds__(kTailThreads) k_tail_vcycle(const TailParams P
         const Dims D = P.lv[t].D;
         tail_prolong(Z(t), Z(t + 1), D);
         tail_cache(tc, C(t), R(t), D);
-        const int iters = 6 << P.lv[t].abs_level;
+        const int iters = P.nu < 0 ? (6 << P.lv[t].abs_level) : P.nu;
         for (int it = 0; it < iters; it++) {
             tail_half_lean(Z(t), tc, D, 1, false);
             tail_half_lean(Z(t), tc, D, 0, false);

@@ -17,7 +17,9 @@ Differences from the reference, all deliberate:
 * ``solve`` returns a dict (iterations, converged, rtr0, rtr, tol, status);
   the reference returns None and prints the iteration count (verbose=True
   prints it here, with the per-iteration residual);
-* the untagged "default" smoother (mgpcg.py:41-49, 88-92) is not provided.
+* the untagged "default" smoother (mgpcg.py:41-49, 88-92) is not provided;
+* ``schedule`` (default "reference", the reference's V-cycle) selects a
+  lighter V-cycle with the restriction scaled by 1/2 (``set_schedule``).
 """
 import ctypes
 
@@ -27,6 +29,13 @@ from . import _lib
 
 SMOOTHERS = {"phases": 1, "fraction": 2}
 PRECISIONS = {"fp32": 0, "mixed": 1}
+# V-cycle schedules: (red-black iterations per side at every level, -1 = the
+# reference's 6 << level; iterations of each bottom order; restriction scale)
+SCHEDULES = {
+    "reference": (-1, 3, 1.0),   # multigrid/mgpcg.py:296-349
+    "v22": (2, 8, 0.5),          # 2 + 2 iterations per level, 8 + 8 at the bottom, restriction / 2
+    "v33": (3, 8, 0.5),
+}
 
 
 def _stream():
@@ -34,7 +43,8 @@ def _stream():
 
 
 class MGPCG:
-    def __init__(self, dim=3, shape=(256, 256, 256), n_mg_levels=6, real=float, precision="fp32", device=None):
+    def __init__(self, dim=3, shape=(256, 256, 256), n_mg_levels=6, real=float, precision="fp32", device=None,
+                 schedule="reference"):
         if dim != 3:
             raise ValueError("only dim=3 is supported (as in the reference's kernels)")
         if real not in (float, torch.float32):
@@ -67,6 +77,9 @@ class MGPCG:
         self.r0 = self._view(lib.flub_mg_r(h), n)
         self._tag = None
         self.last_info = None
+        self.schedule = "reference"
+        if schedule != "reference":
+            self.set_schedule(schedule)
 
     def _view(self, addr, n):
         off = addr - self._ws.data_ptr()
@@ -110,6 +123,21 @@ class MGPCG:
         """Warm start for the next solve (no reference counterpart)."""
         x0 = x0.contiguous()
         _lib.check(self._lib.flub_mg_set_x0(self._h, ctypes.c_void_p(x0.data_ptr()), _stream()), "flub_mg_set_x0")
+
+    def set_schedule(self, schedule="reference", bottom_iters=None, restrict_scale=None):
+        """V-cycle schedule (no reference counterpart).  ``schedule`` is a name
+        of SCHEDULES or the red-black iterations per side at every level (-1:
+        the reference's 6 << level), with ``bottom_iters`` and
+        ``restrict_scale``.  See flub_mg_set_schedule."""
+        if isinstance(schedule, str):
+            if schedule not in SCHEDULES:
+                raise ValueError(f"schedule must be one of {list(SCHEDULES)} or an iteration count")
+            nu, nb, rs = SCHEDULES[schedule]
+        else:
+            nu, nb, rs = int(schedule), int(bottom_iters if bottom_iters is not None else 8), \
+                float(restrict_scale if restrict_scale is not None else 0.5)
+        _lib.check(self._lib.flub_mg_set_schedule(self._h, nu, nb, rs), "flub_mg_set_schedule")
+        self.schedule = schedule if isinstance(schedule, str) else (nu, nb, rs)
 
     def set_initial_guess_scaled(self, d):
         """Warm start x0 = gamma d, gamma = (d . b) / (d . L d) computed on the

@@ -14,12 +14,13 @@ from .mgpcg import MGPCG
 
 
 class Projection:
-    def __init__(self, shape, n_mg_levels, precision="fp32", device=None, h=None):
+    def __init__(self, shape, n_mg_levels, precision="fp32", device=None, h=None, schedule="reference"):
         self.shape = tuple(shape)
         self.device = torch.device(device) if device is not None else torch.device("cuda", torch.cuda.current_device())
         self.h = float(h) if h is not None else 1.0 / self.shape[0]  # const_param.py:59 h = 1 / gridx
         self.h0 = self.h
-        self.mg = MGPCG(3, self.shape, n_mg_levels, float, precision=precision, device=self.device)
+        self.mg = MGPCG(3, self.shape, n_mg_levels, float, precision=precision, device=self.device,
+                        schedule=schedule)
         mk = lambda dt: torch.empty(self.shape, dtype=dt, device=self.device)
         self.tag = IntField(mk(torch.int32))
         self.div = Field(mk(torch.float32))

@@ -221,6 +221,21 @@ int flub_mg_smooth(flub_mg *mg, int level, int phase, void *stream);
 int flub_vcycle_noalloc(const int32_t *tag, const float *r, float *z, int nx, int ny, int nz, int levels,
                         void *stream);
 
+/* V-cycle schedule of the handle's preconditioner (no reference counterpart;
+ * the default is the reference's, mgpcg.py:296-349: smooth_iters = -1, i.e.
+ * 6 << l red-black iterations per side at level l, bottom_iters = 3,
+ * restrict_scale = 1).  smooth_iters = 1..64 runs that many iterations per
+ * side at every level; bottom_iters (1..64) iterations of each bottom order;
+ * the restriction multiplies its sum of 8 children by restrict_scale (0, 1].
+ * With the unscaled 7-point operator on every level the sum of 8 children
+ * over-corrects smooth errors about twice (the coarse operator is 4x the fine
+ * one, the 8-child sum 8x): restrict_scale = 0.5 removes that, and a light
+ * schedule (e.g. 2 iterations per side, 8 at the bottom) then converges in
+ * fewer CG iterations at a fraction of the reference cycle's cost.  The solve
+ * still stops at the same tolerance.  Synchronises the device when the
+ * schedule changes (the captured solve graphs are rebuilt). */
+int flub_mg_set_schedule(flub_mg *mg, int smooth_iters, int bottom_iters, float restrict_scale);
+
 /* Warm start scaled on the device (no reference counterpart): x0 = gamma d
  * with gamma = (d . b) / (d . L d) over fluid cells, b the current right-hand
  * side (flub_mg_init + flub_mg_mask_interior), L the solver's operator --

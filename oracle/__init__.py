@@ -69,6 +69,29 @@ def _declare(L):
     L.oracle_scale.argtypes = [vp, f32, i64]
     L.oracle_subtract_gradient.argtypes = [vp, vp, vp, vp, i32, i32, i32, i32]
     L.oracle_num_threads.restype = i32
+    L.oracle_set_schedule.argtypes = [i32, i32, f64]
+    L.oracle_set_schedule.restype = None
+
+
+REFERENCE_SCHEDULE = (-1, 3, 1.0)
+
+
+class schedule:
+    """Context manager: run the oracle's V-cycle with another schedule
+    (iterations per side at every level, or -1 for the reference's 6 << l;
+    iterations of each bottom order; restriction scale), restoring the
+    reference's afterwards.  No reference counterpart."""
+
+    def __init__(self, nu=-1, bottom=3, rscale=1.0):
+        self.args = (int(nu), int(bottom), float(rscale))
+
+    def __enter__(self):
+        lib().oracle_set_schedule(*self.args)
+        return self
+
+    def __exit__(self, *exc):
+        lib().oracle_set_schedule(*REFERENCE_SCHEDULE)
+        return False
 
 
 def num_threads() -> int:

@@ -19,6 +19,22 @@
 #include <stdlib.h>
 #include <string.h>
 
+/* ---------------- V-cycle schedule ----------------
+ * No reference counterpart: the reference's counts (6 << l iterations per
+ * side at level l, 3 + 3 at the bottom, restriction = plain sum) are the
+ * defaults; oracle_set_schedule generalises them to check the library's
+ * flub_mg_set_schedule. */
+static int oracle_sched_nu = -1;
+static int oracle_sched_bottom = 3;
+static double oracle_sched_rscale = 1.0;
+#define ORACLE_ITERS(l) (oracle_sched_nu < 0 ? (6 << (l)) : oracle_sched_nu)
+
+void oracle_set_schedule(int nu, int bottom, double rscale) {
+    oracle_sched_nu = nu;
+    oracle_sched_bottom = bottom;
+    oracle_sched_rscale = rscale;
+}
+
 /* ---------------- precision-generic solver pieces ---------------- */
 #define REAL float
 #define FN(name) name##_f32

@@ -111,7 +111,7 @@ void FN(oracle_restrict)(const REAL *rf, const REAL *zf, const int32_t *tagf, RE
                             REAL v = rf[c] + FN(ndot)(zf, tagf, nx, ny, nz, i, j, k);
                             if (first) { s = v; first = 0; } else s = s + v;
                         }
-                rc[cc] = s;
+                rc[cc] = s * (REAL)oracle_sched_rscale;
             }
 }
 
@@ -129,13 +129,15 @@ void FN(oracle_prolong)(REAL *zf, const REAL *zc, int nx, int ny, int nz) {
  * "fraction"): z = M r over the level hierarchy.  rl[0]/zl[0] are the finest
  * level; rl[l], zl[l] for l >= 1 are scratch of shape dims >> l.  Smoothing
  * counts: 6 << l per side (pre_and_post_smoothing = 6), 6 at the bottom
- * (bottom_smoothing = 6, split 3 x (0,1) then 3 x (1,0)). */
+ * (bottom_smoothing = 6, split 3 x (0,1) then 3 x (1,0)).  The schedule
+ * globals (oracle_set_schedule, no reference counterpart) generalise these
+ * counts and scale the restriction; their defaults are the reference's. */
 void FN(oracle_vcycle)(REAL **rl, REAL **zl, int32_t **tagl, int levels, int nx, int ny, int nz) {
     int64_t n0 = (int64_t)nx * ny * nz;
     memset(zl[0], 0, (size_t)n0 * sizeof(REAL));
     for (int l = 0; l < levels - 1; l++) {
         int ax = nx >> l, ay = ny >> l, az = nz >> l;
-        for (int it = 0; it < (6 << l); it++) {
+        for (int it = 0; it < ORACLE_ITERS(l); it++) {
             FN(oracle_smooth)(zl[l], rl[l], tagl[l], ax, ay, az, 0);
             FN(oracle_smooth)(zl[l], rl[l], tagl[l], ax, ay, az, 1);
         }
@@ -146,11 +148,11 @@ void FN(oracle_vcycle)(REAL **rl, REAL **zl, int32_t **tagl, int levels, int nx,
     {
         int l = levels - 1;
         int ax = nx >> l, ay = ny >> l, az = nz >> l;
-        for (int it = 0; it < 3; it++) {
+        for (int it = 0; it < oracle_sched_bottom; it++) {
             FN(oracle_smooth)(zl[l], rl[l], tagl[l], ax, ay, az, 0);
             FN(oracle_smooth)(zl[l], rl[l], tagl[l], ax, ay, az, 1);
         }
-        for (int it = 0; it < 3; it++) {
+        for (int it = 0; it < oracle_sched_bottom; it++) {
             FN(oracle_smooth)(zl[l], rl[l], tagl[l], ax, ay, az, 1);
             FN(oracle_smooth)(zl[l], rl[l], tagl[l], ax, ay, az, 0);
         }
@@ -158,7 +160,7 @@ void FN(oracle_vcycle)(REAL **rl, REAL **zl, int32_t **tagl, int levels, int nx,
     for (int l = levels - 2; l >= 0; l--) {
         int ax = nx >> l, ay = ny >> l, az = nz >> l;
         FN(oracle_prolong)(zl[l], zl[l + 1], ax, ay, az);
-        for (int it = 0; it < (6 << l); it++) {
+        for (int it = 0; it < ORACLE_ITERS(l); it++) {
             FN(oracle_smooth)(zl[l], rl[l], tagl[l], ax, ay, az, 1);
             FN(oracle_smooth)(zl[l], rl[l], tagl[l], ax, ay, az, 0);
         }

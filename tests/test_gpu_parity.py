@@ -441,3 +441,48 @@ def test_mixed_precision_vcycle_close_to_fp32():
     z32 = O.vcycle(r0, O.tag_levels(tag_o, scene.levels), np.float32)
     assert np.isfinite(z16).all()
     assert np.linalg.norm(z16 - z32) <= 1e-2 * np.linalg.norm(z32)
+
+
+# ---------------------------------------------------------------- V-cycle schedules (no reference counterpart)
+
+@pytest.mark.parametrize("sched", [(2, 8, 0.5), (3, 4, 0.5), (1, 2, 1.0)])
+@pytest.mark.parametrize("name", ["dam64", "rand32b"])
+def test_vcycle_schedule_bit_exact(sched, name, monkeypatch):
+    """A lighter V-cycle schedule with the scaled restriction against the FP32
+    oracle run with the same schedule: bit-exact like the reference's, on the
+    cluster path and on the fallback path."""
+    scene = SCENES[name]()
+    tags = None
+    for no_cluster in ("0", "1"):
+        if no_cluster == "1":
+            monkeypatch.setenv("FLUB_NO_CLUSTER", "1")
+        tag_o, r0, mg = _setup(scene)
+        tags = O.tag_levels(tag_o, scene.levels)
+        mg.set_schedule(*sched)
+        z = host(mg.apply_preconditioner(dev(r0)))
+        with O.schedule(*sched):
+            z_o = O.vcycle(r0, tags, np.float32)
+        assert np.array_equal(z, z_o), no_cluster
+
+
+@pytest.mark.parametrize("precision", ["fp32", "mixed"])
+def test_light_schedule_projection_matches_fp64_oracle(precision):
+    """The "v22" schedule reaches the same tolerance in fewer CG iterations
+    than the reference schedule; the pressure agrees with the FP64 oracle."""
+    scene = scenes.dam(128, seed=2)
+    ref = O.project(scene, dtype=np.float64)
+    proj = Projection(scene.shape, scene.levels, precision=precision, schedule="v22")
+    vel, velr = mac(scene.u, scene.v, scene.w), mac(scene.ur, scene.vr, scene.wr)
+    info = proj.project(vel, velr, dev(scene.phi), scene.prims)
+    assert info["converged"]
+    assert info["iterations"] < ref["iters"], (info, ref["iters"])
+    p = host(proj.p.f)
+    err = np.linalg.norm(p - ref["p"]) / np.linalg.norm(ref["p"])
+    assert err <= PRESSURE_RTOL, err
+
+
+def test_schedule_rejects_bad_values():
+    mg = MGPCG(3, (32, 32, 32), 3, float)
+    for bad in [(0, 8, 0.5), (2, 0, 0.5), (2, 8, 0.0), (2, 8, 2.0), (65, 8, 0.5)]:
+        with pytest.raises(FlubError):
+            mg.set_schedule(*bad)
