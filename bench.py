@@ -36,9 +36,9 @@ SMOOTH_HALF_SWEEP_BYTES_PER_CELL = 6.5  # red + black iteration: R z, r, tag; W 
 VARIANTS = {
     "plain": "plain FP32 MGPCG (reference V-cycle, FP64 inner products)",
     "mixed": "mixed-precision MGPCG (FP16 V-cycle levels, FP32 arithmetic, flexible CG, FP64 inner products)",
-    "learned+mixed": "mixed-precision MGPCG started from the U-Net warm start (network on the 128^3 level of the "
+    "learned+mixed": "mixed-precision MGPCG started from the U-Net warm start (network on the 64^3 level of the "
                      "hierarchy, trilinear prolongation, energy-optimal scale), same tolerance",
-    "plain-v22": "FP32 MGPCG with the light V-cycle: 2+2 red-black iterations per level, 8+8 at the bottom, "
+    "plain-v22": "FP32 MGPCG with the light V-cycle: 2+2 red-black iterations per level, 4+4 at the bottom, "
                  "restriction scaled by 1/2 (flub_mg_set_schedule), same tolerance",
     "mixed-v22": "mixed-precision MGPCG (FP16 V-cycle levels) with the light V-cycle, same tolerance",
     "learned+mixed-v22": "mixed-precision MGPCG with the light V-cycle, started from the U-Net warm start, "

@@ -82,7 +82,7 @@ SIGNATURES = {
     "flub_conv3d_bf16": (_i32, [_vp, _i32, _vp, _vp, _i32, _vp, _vp, _vp, _i32, _i32, _i32, _i32, _i32, _i32, _vp]),
     "flub_conv3d_wgrad": (_i32, [_vp, _i32, _vp, _i32, _vp, _vp, _i32, _i32, _i32, _i32, _vp]),
     "flub_conv_error": (_i32, [ctypes.POINTER(_i32), _i32]),
-    "flub_unet_input": (_i32, [_vp, _vp, _i32, _i64, _vp, _vp, _vp]),
+    "flub_unet_input": (_i32, [_vp, _vp, _i32, _i64, _vp, _vp, _vp, _vp]),
     "flub_pool2_bf16": (_i32, [_vp, _vp, _i32, _i32, _i32, _i32, _i32, _vp]),
     "flub_pool2_bwd_bf16": (_i32, [_vp, _vp, _i32, _i32, _i32, _i32, _i32, _i32, _vp]),
     "flub_up2_bf16": (_i32, [_vp, _vp, _i32, _i32, _i32, _i32, _i32, _vp]),

@@ -75,20 +75,20 @@ __device__ __forceinline__ void lap_row8(const float *__restrict__ x, const uint
     }
 }
 
-#define FLUB_GROUP_LOOP(g, ng) for (int g = blockIdx.x * blockDim.x + threadIdx.x; g < (ng); g += gridDim.x * blockDim.x)
 
 // Ap = L p, p.Ap -> alpha (mgpcg.py:410-419); guarded like k_matvec_pap.
 __global__ void __launch_bounds__(kRedThreads) k8_matvec_pap(MgState *st, const float *__restrict__ p,
                                                              float *__restrict__ Ap, const uint8_t *__restrict__ code,
-                                                             Dims D, double *partials, unsigned long long *kc) {
+                                                             Dims D, double *partials, const int *__restrict__ act,
+                                                             const int *__restrict__ act_n, unsigned long long *kc) {
     __shared__ double red[32];
     count_kernel(kc);
     if (st->it >= st->max_iters || st->converged || st->status) return;
     const int ng = (int)(D.n() >> 3);
     double s = 0.0;
-    FLUB_GROUP_LOOP(g, ng) {
+    FLUB_ACT_LOOP(g, act, act_n, ng) {
         const uint2 cc = load_codes8(code + (g << 3));
-        if (!group_has_fluid(cc)) continue;  // Ap = 0 there already
+        if (!act && !group_has_fluid(cc)) continue;  // Ap = 0 there already
         float a[8];
         Row8 pc;
         lap_row8(p, code, D, g, cc, a, pc);
@@ -112,7 +112,8 @@ __global__ void __launch_bounds__(kRedThreads) k8_update_r_rr(MgState *st, float
                                                               const uint8_t *__restrict__ code, int64_t n,
                                                               double *partials, double *hist,
                                                               cudaGraphConditionalHandle h, int set_cond,
-                                                              unsigned long long *kc) {
+                                                              const int *__restrict__ act,
+                                                              const int *__restrict__ act_n, unsigned long long *kc) {
     __shared__ double red[32];
     count_kernel(kc);
     if (st->it >= st->max_iters || st->converged || st->status) {
@@ -121,10 +122,11 @@ __global__ void __launch_bounds__(kRedThreads) k8_update_r_rr(MgState *st, float
     }
     const float a = (float)st->alpha;
     const int skip = st->skip_r;
+    const int *ga = skip ? act : nullptr;
     const int ng = (int)(n >> 3);
     double s = 0.0;
-    FLUB_GROUP_LOOP(g, ng) {
-        if (skip && !group_has_fluid(load_codes8(code + (g << 3)))) continue;
+    FLUB_ACT_LOOP(g, ga, act_n, ng) {
+        if (skip && !ga && !group_has_fluid(load_codes8(code + (g << 3)))) continue;
         Row8 rv;
         load_row8_rw(r + (g << 3), rv);
         if (kUpdate) {
@@ -151,14 +153,16 @@ __global__ void __launch_bounds__(kRedThreads) k8_update_r_rr(MgState *st, float
 // rTr0 and the tolerance (mgpcg.py:391-393).
 __global__ void __launch_bounds__(kRedThreads) k8_dot_rr0(MgState *st, const float *__restrict__ r,
                                                           const uint8_t *__restrict__ code, int64_t n,
-                                                          double *partials, unsigned long long *kc) {
+                                                          double *partials, const int *__restrict__ act,
+                                                          const int *__restrict__ act_n, unsigned long long *kc) {
     __shared__ double red[32];
     count_kernel(kc);
     const int skip = st->skip_r;
+    const int *ga = skip ? act : nullptr;
     const int ng = (int)(n >> 3);
     double s = 0.0;
-    FLUB_GROUP_LOOP(g, ng) {
-        if (skip && !group_has_fluid(load_codes8(code + (g << 3)))) continue;
+    FLUB_ACT_LOOP(g, ga, act_n, ng) {
+        if (skip && !ga && !group_has_fluid(load_codes8(code + (g << 3)))) continue;
         Row8 rv;
         load_row8(r + (g << 3), rv);
 #pragma unroll
@@ -179,14 +183,15 @@ template <bool kInit, bool kScaleZ = false>
 __global__ void __launch_bounds__(kRedThreads) k8_dot_zr(MgState *st, const float *__restrict__ z,
                                                          const float *__restrict__ r, float *__restrict__ p,
                                                          const uint8_t *__restrict__ code, int64_t n,
-                                                         double *partials, unsigned long long *kc) {
+                                                         double *partials, const int *__restrict__ act,
+                                                         const int *__restrict__ act_n, unsigned long long *kc) {
     __shared__ double red[32];
     count_kernel(kc);
     const int ng = (int)(n >> 3);
     const float zs = kScaleZ ? st->zscale : 1.0f;
     double s = 0.0;
-    FLUB_GROUP_LOOP(g, ng) {
-        if (!group_has_fluid(load_codes8(code + (g << 3)))) continue;  // z = 0 (and p = 0) there
+    FLUB_ACT_LOOP(g, act, act_n, ng) {
+        if (!act && !group_has_fluid(load_codes8(code + (g << 3)))) continue;  // z = 0 (and p = 0) there
         Row8 zv, rv;
         load_row8(z + (g << 3), zv);
         if (kScaleZ) {
@@ -215,13 +220,14 @@ __global__ void __launch_bounds__(kRedThreads) k8_dot_zr(MgState *st, const floa
 template <bool kScaleZ = false>
 __global__ void __launch_bounds__(256) k8_update_xp(MgState *st, float *__restrict__ x, float *__restrict__ p,
                                                     const float *__restrict__ z, const uint8_t *__restrict__ code,
-                                                    int64_t n, unsigned long long *kc) {
+                                                    int64_t n, const int *__restrict__ act,
+                                                    const int *__restrict__ act_n, unsigned long long *kc) {
     count_kernel(kc);
     const float a = (float)st->alpha, b = (float)st->beta;
     const float zs = kScaleZ ? st->zscale : 1.0f;
     const int ng = (int)(n >> 3);
-    FLUB_GROUP_LOOP(g, ng) {
-        if (!group_has_fluid(load_codes8(code + (g << 3)))) continue;  // p = z = 0 there
+    FLUB_ACT_LOOP(g, act, act_n, ng) {
+        if (!act && !group_has_fluid(load_codes8(code + (g << 3)))) continue;  // p = z = 0 there
         Row8 xv, pv, zv;
         load_row8_rw(x + (g << 3), xv);
         load_row8_rw(p + (g << 3), pv);
@@ -241,16 +247,80 @@ __global__ void __launch_bounds__(256) k8_update_xp(MgState *st, float *__restri
     if ((blockIdx.x | threadIdx.x) == 0) st->it += 1;
 }
 
+// r -= L x0 when an initial guess was given (no reference counterpart); L x0
+// is 0 off the fluid, so only the active groups change.
+__global__ void __launch_bounds__(256) k8_residual_x0(MgState *st, float *__restrict__ r, const float *__restrict__ x,
+                                                      const uint8_t *__restrict__ code, Dims D,
+                                                      const int *__restrict__ act, const int *__restrict__ act_n,
+                                                      unsigned long long *kc) {
+    count_kernel(kc);
+    if (!st->use_x0) return;
+    const int ng = (int)(D.n() >> 3);
+    FLUB_ACT_LOOP(g, act, act_n, ng) {
+        const uint2 cc = load_codes8(code + (g << 3));
+        if (!act && !group_has_fluid(cc)) continue;
+        float lx[8];
+        Row8 xc, rv;
+        lap_row8(x, code, D, g, cc, lx, xc);
+        load_row8_rw(r + (g << 3), rv);
+#pragma unroll
+        for (int m = 0; m < 8; m++)
+            if (code_at(cc, m) == kCodeFluid) rv.v[m] = __fsub_rn(rv.v[m], lx[m]);
+        store_row8(r + (g << 3), rv.v);
+    }
+}
+
+// gamma = (d . b) / (d . L d) over fluid cells (no reference counterpart): the
+// multiple of d closest to the solution of L x = b in the energy norm.
+__global__ void __launch_bounds__(kRedThreads) k8_x0_gamma(MgState *st, const float *__restrict__ d,
+                                                           const float *__restrict__ b,
+                                                           const uint8_t *__restrict__ code, Dims D, double *partials,
+                                                           const int *__restrict__ act,
+                                                           const int *__restrict__ act_n) {
+    __shared__ double red[32];
+    const int ng = (int)(D.n() >> 3);
+    double s_ld = 0.0, s_b = 0.0;
+    FLUB_ACT_LOOP(g, act, act_n, ng) {
+        const uint2 cc = load_codes8(code + (g << 3));
+        if (!act && !group_has_fluid(cc)) continue;
+        float ld[8];
+        Row8 dc, bv;
+        lap_row8(d, code, D, g, cc, ld, dc);
+        load_row8(b + (g << 3), bv);
+#pragma unroll
+        for (int m = 0; m < 8; m++) {
+            if (code_at(cc, m) != kCodeFluid) continue;
+            s_ld = fma((double)dc.v[m], (double)ld[m], s_ld);
+            s_b = fma((double)dc.v[m], (double)bv.v[m], s_b);
+        }
+    }
+    const double bb = block_sum(s_b, red);
+    __syncthreads();
+    if (threadIdx.x == 0) partials[kMaxRedBlocks + blockIdx.x] = bb;
+    double total;
+    if (finish_partials(s_ld, partials, &st->ticket, red, &total)) {
+        __syncthreads();
+        double t2 = 0.0;
+        for (unsigned q = threadIdx.x; q < gridDim.x; q += blockDim.x) t2 += __ldcg(&partials[kMaxRedBlocks + q]);
+        t2 = block_sum(t2, red);
+        if (threadIdx.x == 0) {
+            const double gm = t2 / total;
+            st->x0_scale = (total != 0.0 && isfinite(gm)) ? gm : 0.0;
+        }
+    }
+}
+
 // On convergence: x += alpha p (mgpcg.py:444-446).
 __global__ void __launch_bounds__(256) k8_solve_end(MgState *st, float *__restrict__ x, const float *__restrict__ p,
                                                     const uint8_t *__restrict__ code, int64_t n,
+                                                    const int *__restrict__ act, const int *__restrict__ act_n,
                                                     unsigned long long *kc) {
     count_kernel(kc);
     if (!st->converged) return;
     const float a = (float)st->alpha;
     const int ng = (int)(n >> 3);
-    FLUB_GROUP_LOOP(g, ng) {
-        if (!group_has_fluid(load_codes8(code + (g << 3)))) continue;
+    FLUB_ACT_LOOP(g, act, act_n, ng) {
+        if (!act && !group_has_fluid(load_codes8(code + (g << 3)))) continue;
         Row8 xv, pv;
         load_row8_rw(x + (g << 3), xv);
         load_row8(p + (g << 3), pv);

@@ -42,6 +42,9 @@ struct Level {
     // mixed precision: FP16 copies at scale 8^-l (level 0: rh is the FP16 copy
     // of the CG residual, zh is unused, z is the FP32 CG vector)
     __half *rh, *zh, *z2h;
+    // active 8-cell groups (ascending) and their count on the device; NULL
+    // when nz is not a multiple of 8 (the scalar kernels run there)
+    int *act, *act_n;
 };
 
 struct LaunchCtx {
@@ -63,6 +66,7 @@ struct flub_mg {
     flub::Level lv[flub::kMaxLevels];
     float *x, *p, *Ap;
     float *r_old;  // mixed precision: the residual of the previous iteration (flexible CG)
+    int *act_scratch;  // block counts for building the active lists
     flub::MgState *st;
     double *partials;
     double *hist;
@@ -131,7 +135,14 @@ static size_t carve(flub_mg *mg, char *base) {
             L.zh = l ? (__half *)take(sizeof(__half) * nl) : nullptr;
             L.z2h = (__half *)take(sizeof(__half) * nl);
         }
+        L.act = L.act_n = nullptr;
+        if (L.D.nz % 8 == 0) {
+            L.act = (int *)take(sizeof(int) * (size_t)(nl >> 3));
+            L.act_n = (int *)take(sizeof(int));
+        }
     }
+    // per-block counts of the active-list build (level 0 has the most blocks)
+    mg->act_scratch = (int *)take(sizeof(int) * (size_t)((n / 8 + kActPerBlock - 1) / kActPerBlock + 1));
     mg->r_old = mg->precision == FLUB_PRECISION_MIXED ? (float *)take(sizeof(float) * n) : nullptr;
     return off;
 }
@@ -357,17 +368,19 @@ template <typename TO, typename TI, typename TR, typename TC>
 static int sweep8(const LaunchCtx &c, const Level &L, int phase, int mode, int skip, const TR *r, const TI *zin,
                   TO *zout, const TC *zc, float zc_scale) {
     const Dims D = L.D;
-    const int nz8 = D.nz >> 3;
-    const int bx = nz8 < 32 ? nz8 : 32, by = 256 / bx;
-    const dim3 blk(bx, by), grd((nz8 + bx - 1) / bx, (D.ny + by - 1) / by, D.nx);
+    // skip: the caller asserts z = 0 off the fluid in zout, so only the active
+    // groups are visited; one resident wave of blocks, grid-stride
+    const int *act = skip ? L.act : nullptr;
+    const int *act_n = skip ? L.act_n : nullptr;
+    const dim3 blk(256), grd(blocks_for(D.n() >> 3, 256, kNumSMs * 4));
     if (mode == kSweepFromZero)
         return launch_pdl(k_smooth8<true, false, TO, TO, TR, TC>, grd, blk, 0, c.s, zout, (const TO *)zout,
-                          (const TC *)nullptr, 1.0f, r, (const uint8_t *)L.code, D, phase, skip, c.kc);
+                          (const TC *)nullptr, 1.0f, r, (const uint8_t *)L.code, D, phase, act, act_n, c.kc);
     if (mode == kSweepProlong)
         return launch_pdl(k_smooth8<false, true, TO, TI, TR, TC>, grd, blk, 0, c.s, zout, zin, zc, zc_scale, r,
-                          (const uint8_t *)L.code, D, phase, skip, c.kc);
+                          (const uint8_t *)L.code, D, phase, act, act_n, c.kc);
     return launch_pdl(k_smooth8<false, false, TO, TO, TR, TC>, grd, blk, 0, c.s, zout, (const TO *)zout,
-                      (const TC *)nullptr, 1.0f, r, (const uint8_t *)L.code, D, phase, skip, c.kc);
+                      (const TC *)nullptr, 1.0f, r, (const uint8_t *)L.code, D, phase, act, act_n, c.kc);
 }
 
 static int sweep(const LaunchCtx &c, const Level &L, int phase, int mode, int skip, const float *r,
@@ -573,22 +586,23 @@ static int enqueue_prologue_mixed(flub_mg *mg, const LaunchCtx &c, int smoother)
     const unsigned bg = red_blocks(mg->n / 8 + 1);
     if (smoother == FLUB_SMOOTHER_FRACTION) FLUB_TRY(enqueue_mean_removal(mg, c, 0));
     FLUB_TRY(launch_pdl(k8_dot_rr0, dim3(bg), dim3(kRedThreads), 0, c.s, mg->st, L0.r, L0.code, mg->n, mg->partials,
-                        c.kc));
-    FLUB_TRY(launch_pdl(k_residual_x0, dim3(blocks_for(mg->n, 256)), dim3(256), 0, c.s, mg->st, L0.r, mg->x, L0.code,
-                        L0.D, c.kc));
+                        (const int *)L0.act, (const int *)L0.act_n, c.kc));
+    FLUB_TRY(launch_pdl(k8_residual_x0, dim3(blocks_for(mg->n / 8, 256, kNumSMs * 8)), dim3(256), 0, c.s, mg->st,
+                        L0.r, (const float *)mg->x, (const uint8_t *)L0.code, L0.D, (const int *)L0.act,
+                        (const int *)L0.act_n, c.kc));
     if (smoother == FLUB_SMOOTHER_FRACTION) FLUB_TRY(enqueue_mean_removal(mg, c, 2));
     FLUB_TRY(launch_pdl(k8_to_half, dim3(blocks_for(mg->n / 8, 256)), dim3(256), 0, c.s, mg->st, (const float *)L0.r, L0.rh,
                         mg->n, c.kc));
     FLUB_TRY(enqueue_vcycle_mixed(mg, c, L0.z, true));
     return launch_pdl(k8_dot_zr<true, true>, dim3(bg), dim3(kRedThreads), 0, c.s, mg->st, L0.z, L0.r, mg->p, L0.code,
-                      mg->n, mg->partials, c.kc);
+                      mg->n, mg->partials, (const int *)L0.act, (const int *)L0.act_n, c.kc);
 }
 
 static int enqueue_first_half_mixed(flub_mg *mg, const LaunchCtx &c, int smoother) {
     const Level &L0 = mg->lv[0];
     const unsigned b = red_blocks(mg->n), bg = red_blocks(mg->n / 8 + 1);
     FLUB_TRY(launch_pdl(k8_matvec_pap, dim3(bg), dim3(kRedThreads), 0, c.s, mg->st, mg->p, mg->Ap, L0.code, L0.D,
-                        mg->partials, c.kc));
+                        mg->partials, (const int *)L0.act, (const int *)L0.act_n, c.kc));
     if (smoother == FLUB_SMOOTHER_FRACTION) {
         FLUB_CHECK_CUDA(cudaMemcpyAsync(mg->r_old, L0.r, sizeof(float) * mg->n, cudaMemcpyDeviceToDevice, c.s));
         FLUB_TRY(launch_pdl(k_update_r, dim3(b), dim3(kRedThreads), 0, c.s, mg->st, L0.r, mg->Ap, mg->n, c.kc));
@@ -596,10 +610,12 @@ static int enqueue_first_half_mixed(flub_mg *mg, const LaunchCtx &c, int smoothe
         FLUB_TRY(launch_pdl(k8_to_half, dim3(blocks_for(mg->n / 8, 256)), dim3(256), 0, c.s, mg->st, (const float *)L0.r,
                             L0.rh, mg->n, c.kc));
         return launch_pdl(k8_update_r_rr<false>, dim3(bg), dim3(kRedThreads), 0, c.s, mg->st, L0.r, mg->Ap, L0.code,
-                          mg->n, mg->partials, mg->hist, c.h, c.set_cond, c.kc);
+                          mg->n, mg->partials, mg->hist, c.h, c.set_cond, (const int *)L0.act, (const int *)L0.act_n,
+                          c.kc);
     }
     return launch_pdl(k8_update_r_rr_mixed, dim3(bg), dim3(kRedThreads), 0, c.s, mg->st, L0.r, mg->r_old, L0.rh,
-                      mg->Ap, L0.code, mg->n, mg->partials, mg->hist, c.h, c.set_cond, c.kc);
+                      mg->Ap, L0.code, mg->n, mg->partials, mg->hist, c.h, c.set_cond, (const int *)L0.act,
+                      (const int *)L0.act_n, c.kc);
 }
 
 static int enqueue_second_half_mixed(flub_mg *mg, const LaunchCtx &c) {
@@ -607,9 +623,9 @@ static int enqueue_second_half_mixed(flub_mg *mg, const LaunchCtx &c) {
     const unsigned bg = red_blocks(mg->n / 8 + 1);
     FLUB_TRY(enqueue_vcycle_mixed(mg, c, L0.z, true));
     FLUB_TRY(launch_pdl(k8_dot_zr_flex, dim3(bg), dim3(kRedThreads), 0, c.s, mg->st, L0.z, L0.r, mg->r_old, L0.code,
-                        mg->n, mg->partials, c.kc));
-    return launch_pdl(k8_update_xp<true>, dim3(blocks_for(mg->n / 8, 256)), dim3(256), 0, c.s, mg->st, mg->x, mg->p, L0.z,
-                      L0.code, mg->n, c.kc);
+                        mg->n, mg->partials, (const int *)L0.act, (const int *)L0.act_n, c.kc));
+    return launch_pdl(k8_update_xp<true>, dim3(blocks_for(mg->n / 8, 256, kNumSMs * 8)), dim3(256), 0, c.s, mg->st,
+                      mg->x, mg->p, L0.z, L0.code, mg->n, (const int *)L0.act, (const int *)L0.act_n, c.kc);
 }
 
 static int enqueue_prologue(flub_mg *mg, const LaunchCtx &c, int smoother) {
@@ -621,16 +637,21 @@ static int enqueue_prologue(flub_mg *mg, const LaunchCtx &c, int smoother) {
     if (smoother == FLUB_SMOOTHER_FRACTION) FLUB_TRY(enqueue_mean_removal(mg, c, 0));
     if (v8)
         FLUB_TRY(launch_pdl(k8_dot_rr0, dim3(bg), dim3(kRedThreads), 0, c.s, mg->st, L0.r, L0.code, mg->n,
-                            mg->partials, c.kc));
+                            mg->partials, (const int *)L0.act, (const int *)L0.act_n, c.kc));
     else
         FLUB_TRY(launch_pdl(k_dot_rr0, dim3(b), dim3(kRedThreads), 0, c.s, mg->st, L0.r, mg->n, mg->partials, c.kc));
-    FLUB_TRY(launch_pdl(k_residual_x0, dim3(blocks_for(mg->n, 256)), dim3(256), 0, c.s, mg->st, L0.r, mg->x, L0.code,
-                        L0.D, c.kc));
+    if (v8)
+        FLUB_TRY(launch_pdl(k8_residual_x0, dim3(blocks_for(mg->n / 8, 256, kNumSMs * 8)), dim3(256), 0, c.s,
+                            mg->st, L0.r, (const float *)mg->x, (const uint8_t *)L0.code, L0.D, (const int *)L0.act,
+                            (const int *)L0.act_n, c.kc));
+    else
+        FLUB_TRY(launch_pdl(k_residual_x0, dim3(blocks_for(mg->n, 256)), dim3(256), 0, c.s, mg->st, L0.r, mg->x,
+                            L0.code, L0.D, c.kc));
     if (smoother == FLUB_SMOOTHER_FRACTION) FLUB_TRY(enqueue_mean_removal(mg, c, 2));
     FLUB_TRY(enqueue_vcycle(mg, c, L0.r, L0.z, true));
     if (v8)
         return launch_pdl(k8_dot_zr<true, false>, dim3(bg), dim3(kRedThreads), 0, c.s, mg->st, L0.z, L0.r, mg->p, L0.code,
-                          mg->n, mg->partials, c.kc);
+                          mg->n, mg->partials, (const int *)L0.act, (const int *)L0.act_n, c.kc);
     return launch_pdl(k_dot_zr_init, dim3(b), dim3(kRedThreads), 0, c.s, mg->st, L0.z, L0.r, mg->p, mg->n,
                       mg->partials, c.kc);
 }
@@ -644,7 +665,7 @@ static int enqueue_first_half(flub_mg *mg, const LaunchCtx &c, int smoother) {
     const unsigned bg = red_blocks(mg->n / 8 + 1);
     if (v8)
         FLUB_TRY(launch_pdl(k8_matvec_pap, dim3(bg), dim3(kRedThreads), 0, c.s, mg->st, mg->p, mg->Ap, L0.code, L0.D,
-                            mg->partials, c.kc));
+                            mg->partials, (const int *)L0.act, (const int *)L0.act_n, c.kc));
     else
         FLUB_TRY(launch_pdl(k_matvec_pap, dim3(b), dim3(kRedThreads), 0, c.s, mg->st, mg->p, mg->Ap, L0.code, L0.D,
                             mg->partials, c.kc));
@@ -653,13 +674,15 @@ static int enqueue_first_half(flub_mg *mg, const LaunchCtx &c, int smoother) {
         FLUB_TRY(enqueue_mean_removal(mg, c, 1));
         if (v8)
             return launch_pdl(k8_update_r_rr<false>, dim3(bg), dim3(kRedThreads), 0, c.s, mg->st, L0.r, mg->Ap,
-                              L0.code, mg->n, mg->partials, mg->hist, c.h, c.set_cond, c.kc);
+                              L0.code, mg->n, mg->partials, mg->hist, c.h, c.set_cond, (const int *)L0.act,
+                              (const int *)L0.act_n, c.kc);
         return launch_pdl(k_update_r_rr<false>, dim3(b), dim3(kRedThreads), 0, c.s, mg->st, L0.r, mg->Ap, mg->n,
                           mg->partials, mg->hist, c.h, c.set_cond, c.kc);
     }
     if (v8)
         return launch_pdl(k8_update_r_rr<true>, dim3(bg), dim3(kRedThreads), 0, c.s, mg->st, L0.r, mg->Ap, L0.code,
-                          mg->n, mg->partials, mg->hist, c.h, c.set_cond, c.kc);
+                          mg->n, mg->partials, mg->hist, c.h, c.set_cond, (const int *)L0.act,
+                          (const int *)L0.act_n, c.kc);
     return launch_pdl(k_update_r_rr<true>, dim3(b), dim3(kRedThreads), 0, c.s, mg->st, L0.r, mg->Ap, mg->n,
                       mg->partials, mg->hist, c.h, c.set_cond, c.kc);
 }
@@ -673,9 +696,11 @@ static int enqueue_second_half(flub_mg *mg, const LaunchCtx &c) {
     if ((L0.D.nz % 8) == 0) {
         const unsigned bg = red_blocks(mg->n / 8 + 1);
         FLUB_TRY(launch_pdl(k8_dot_zr<false>, dim3(bg), dim3(kRedThreads), 0, c.s, mg->st, L0.z, L0.r,
-                            (float *)nullptr, L0.code, mg->n, mg->partials, c.kc));
-        return launch_pdl(k8_update_xp<false>, dim3(blocks_for(mg->n / 8, 256)), dim3(256), 0, c.s, mg->st, mg->x, mg->p,
-                          L0.z, L0.code, mg->n, c.kc);
+                            (float *)nullptr, L0.code, mg->n, mg->partials, (const int *)L0.act,
+                            (const int *)L0.act_n, c.kc));
+        return launch_pdl(k8_update_xp<false>, dim3(blocks_for(mg->n / 8, 256, kNumSMs * 8)), dim3(256), 0, c.s,
+                          mg->st, mg->x, mg->p, L0.z, L0.code, mg->n, (const int *)L0.act, (const int *)L0.act_n,
+                          c.kc);
     }
     FLUB_TRY(launch_pdl(k_dot_zr_beta, dim3(b), dim3(kRedThreads), 0, c.s, mg->st, L0.z, L0.r, mg->n, mg->partials,
                         c.kc));
@@ -686,8 +711,8 @@ static int enqueue_second_half(flub_mg *mg, const LaunchCtx &c) {
 static int enqueue_epilogue(flub_mg *mg, const LaunchCtx &c) {
     const Level &L0 = mg->lv[0];
     if ((L0.D.nz % 8) == 0)
-        return launch_pdl(k8_solve_end, dim3(blocks_for(mg->n / 8, 256)), dim3(256), 0, c.s, mg->st, mg->x, mg->p,
-                          L0.code, mg->n, c.kc);
+        return launch_pdl(k8_solve_end, dim3(blocks_for(mg->n / 8, 256, kNumSMs * 8)), dim3(256), 0, c.s, mg->st,
+                          mg->x, mg->p, L0.code, mg->n, (const int *)L0.act, (const int *)L0.act_n, c.kc);
     return launch_pdl(k_solve_end, dim3(blocks_for(mg->n, 256)), dim3(256), 0, c.s, mg->st, mg->x, mg->p, mg->n,
                       c.kc);
 }
@@ -994,6 +1019,19 @@ int flub_mg_set_tags(flub_mg *mg, const int32_t *tag, void *stream) {
         k_restrict_codes<<<blocks_for(C.D.n(), 256), 256, 0, s>>>(mg->lv[l].code, C.code, C.D);
         FLUB_CHECK_LAUNCH();
     }
+    // active 8-cell groups of every level that has them
+    for (int l = 0; l < mg->levels; l++) {
+        const Level &L = mg->lv[l];
+        if (!L.act) continue;
+        const int ng = (int)(L.D.n() >> 3);
+        const int nb = (ng + kActPerBlock - 1) / kActPerBlock;
+        k_act_count<<<nb, kActThreads, 0, s>>>(L.code, ng, mg->act_scratch);
+        FLUB_CHECK_LAUNCH();
+        k_act_scan<<<1, kActThreads, 0, s>>>(mg->act_scratch, nb, L.act_n);
+        FLUB_CHECK_LAUNCH();
+        k_act_write<<<nb, kActThreads, 0, s>>>(L.code, ng, mg->act_scratch, L.act);
+        FLUB_CHECK_LAUNCH();
+    }
     // new tags: re-establish z = p = Ap = 0 off the fluid (the kernels skip
     // 8-cell groups without fluid and rely on it)
     for (int l = 0; l < mg->levels; l++) {
@@ -1120,7 +1158,11 @@ int flub_mg_set_x0_scaled(flub_mg *mg, const float *d, void *stream) {
     FLUB_REQUIRE(d != mg->x, "flub_mg_set_x0_scaled: d must not be the solution vector itself");
     cudaStream_t s = as_stream(stream);
     const Level &L0 = mg->lv[0];
-    k_x0_gamma<<<red_blocks(mg->n), kRedThreads, 0, s>>>(mg->st, d, L0.r, L0.code, L0.D, mg->partials);
+    if (L0.act)
+        k8_x0_gamma<<<red_blocks(mg->n / 8 + 1), kRedThreads, 0, s>>>(mg->st, d, L0.r, L0.code, L0.D, mg->partials,
+                                                                     L0.act, L0.act_n);
+    else
+        k_x0_gamma<<<red_blocks(mg->n), kRedThreads, 0, s>>>(mg->st, d, L0.r, L0.code, L0.D, mg->partials);
     FLUB_CHECK_LAUNCH();
     k_x0_apply<<<blocks_for(mg->n, 256), 256, 0, s>>>(mg->st, d, L0.code, mg->x, mg->n);
     FLUB_CHECK_LAUNCH();

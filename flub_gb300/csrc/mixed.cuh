@@ -79,7 +79,8 @@ __global__ void __launch_bounds__(256) k8_to_half(MgState *st, const float *__re
     const float hs = st ? fp16_residual_scale(st->rtr0, n) : 1.0f;
     if (st && (blockIdx.x | threadIdx.x) == 0) st->zscale = 1.0f / hs;
     const int ng = (int)(n >> 3);
-    FLUB_GROUP_LOOP(g, ng) {
+    // every group: afterwards rh = r / zscale everywhere (0 off the fluid when r is masked)
+    FLUB_ACT_LOOP(g, (const int *)nullptr, (const int *)nullptr, ng) {
         float v[8];
         St<float>::ld8_ro(r + (g << 3), v);
 #pragma unroll
@@ -96,6 +97,8 @@ __global__ void __launch_bounds__(kRedThreads) k8_update_r_rr_mixed(MgState *st,
                                                                     const uint8_t *__restrict__ code, int64_t n,
                                                                     double *partials, double *hist,
                                                                     cudaGraphConditionalHandle h, int set_cond,
+                                                                    const int *__restrict__ act,
+                                                                    const int *__restrict__ act_n,
                                                                     unsigned long long *kc) {
     __shared__ double red[32];
     count_kernel(kc);
@@ -105,14 +108,17 @@ __global__ void __launch_bounds__(kRedThreads) k8_update_r_rr_mixed(MgState *st,
     }
     const float a = (float)st->alpha;
     const int skip = st->skip_r;
+    // with a masked r the groups without fluid keep r = r_old = rh = 0 (the
+    // solve's first FP16 copy, k8_to_half, covered every group)
+    const int *ga = skip ? act : nullptr;
     // scale of the FP16 copy from the previous residual norm (st->rtr is only
     // overwritten by the last block, after every block has read it)
     const float hs = fp16_residual_scale(st->rtr, n);
     if ((blockIdx.x | threadIdx.x) == 0) st->zscale = 1.0f / hs;
     const int ng = (int)(n >> 3);
     double s = 0.0;
-    FLUB_GROUP_LOOP(g, ng) {
-        if (skip && !group_has_fluid(load_codes8(code + (g << 3)))) continue;
+    FLUB_ACT_LOOP(g, ga, act_n, ng) {
+        if (skip && !ga && !group_has_fluid(load_codes8(code + (g << 3)))) continue;
         float rv[8], av[8], hv[8];
         St<float>::ld8(r + (g << 3), rv);
         St<float>::ld8_ro(Ap + (g << 3), av);
@@ -143,14 +149,15 @@ __global__ void __launch_bounds__(kRedThreads) k8_dot_zr_flex(MgState *st, const
                                                               const float *__restrict__ r,
                                                               const float *__restrict__ r_old,
                                                               const uint8_t *__restrict__ code, int64_t n,
-                                                              double *partials, unsigned long long *kc) {
+                                                              double *partials, const int *__restrict__ act,
+                                                              const int *__restrict__ act_n, unsigned long long *kc) {
     __shared__ double red[32];
     count_kernel(kc);
     const int ng = (int)(n >> 3);
     const float zs = st->zscale;
     double s = 0.0, so = 0.0;
-    FLUB_GROUP_LOOP(g, ng) {
-        if (!group_has_fluid(load_codes8(code + (g << 3)))) continue;  // z = 0 there
+    FLUB_ACT_LOOP(g, act, act_n, ng) {
+        if (!act && !group_has_fluid(load_codes8(code + (g << 3)))) continue;  // z = 0 there
         float zv[8], rv[8], ov[8];
         St<float>::ld8_ro(z + (g << 3), zv);
 #pragma unroll

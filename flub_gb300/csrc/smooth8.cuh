@@ -70,21 +70,23 @@ __device__ __forceinline__ float coarse_at(const TC *__restrict__ p, float scale
 // the mixed-precision V-cycle); arithmetic is FP32 throughout.
 // Every non-fluid cell is written as 0 (its value is never read by a fluid
 // cell's update, and the reference's sweeps leave it 0 by the end of the
-// V-cycle), so a buffer that starts at 0 keeps z = 0 off the fluid.  With
-// skip_inactive set the caller asserts that invariant for zout, and a thread
-// whose 8 cells hold no fluid cell returns without touching z or r.
-// Grid: x over k groups of 8, y over j, z over i.  Requires nz % 8 == 0.
+// V-cycle), so a buffer that starts at 0 keeps z = 0 off the fluid.  With an
+// active list (act != NULL) the caller asserts that invariant for zout, and
+// only the groups of the list (those holding a fluid cell) are visited;
+// without one every group is.
+// Grid: one-dimensional, grid-stride over the groups.  Requires nz % 8 == 0.
 template <bool kFromZero, bool kProlong, typename TO, typename TI, typename TR, typename TC>
 __global__ void __launch_bounds__(256, 4) k_smooth8(TO *zout, const TI *zin, const TC *__restrict__ zc,
                                                     float zc_scale, const TR *__restrict__ r,
                                                     const uint8_t *__restrict__ code, Dims D, int phase,
-                                                    int skip_inactive, unsigned long long *kc) {
+                                                    const int *__restrict__ act, const int *__restrict__ act_n,
+                                                    unsigned long long *kc) {
     count_kernel(kc);
     const int nz8 = D.nz >> 3;
-    const int kg = blockIdx.x * blockDim.x + threadIdx.x;
-    const int j = blockIdx.y * blockDim.y + threadIdx.y;
-    const int i = blockIdx.z;
-    if (kg >= nz8 || j >= D.ny) return;
+    const int ng = (int)(D.n() >> 3);
+    FLUB_ACT_LOOP(g, act, act_n, ng) {
+    const int kg = g % nz8, jq = g / nz8;
+    const int j = jq % D.ny, i = jq / D.ny;
     const int k0 = kg << 3;
     const int sj = D.nz, si = D.ny * D.nz;
     const int c0 = (i * D.ny + j) * D.nz + k0;
@@ -95,7 +97,6 @@ __global__ void __launch_bounds__(256, 4) k_smooth8(TO *zout, const TI *zin, con
 
     // cell codes: centre row, +-i rows, +-j rows, and the two k neighbours
     const uint2 cc = load_codes8(code + c0);
-    if (skip_inactive && ((cc.x | cc.y) & 0x02020202u) == 0u) return;  // no fluid cell (code 2) in the row
     const uint2 cip = hip ? load_codes8(code + c0 + si) : make_uint2(0u, 0u);
     const uint2 cim = him ? load_codes8(code + c0 - si) : make_uint2(0u, 0u);
     const uint2 cjp = hjp ? load_codes8(code + c0 + sj) : make_uint2(0u, 0u);
@@ -170,6 +171,7 @@ __global__ void __launch_bounds__(256, 4) k_smooth8(TO *zout, const TI *zin, con
         out[m] = zn;
     }
     St<TO>::st8(zout + c0, out);
+    }
 }
 
 }  // namespace flub

@@ -16,19 +16,40 @@ namespace flub {
 
 __device__ __forceinline__ float bf(const __nv_bfloat16 v) { return __bfloat162float(v); }
 
-// Per-sample 1 / RMS of the right-hand side over fluid cells (1 if none).
-__global__ void __launch_bounds__(256) k_unet_rms(const float *__restrict__ div, const int32_t *__restrict__ tag,
-                                                  int64_t ncell, float *__restrict__ inv_scale) {
+// Per-sample 1 / RMS of the right-hand side over fluid cells (1 if none), in
+// two deterministic passes: kRmsBlocks blocks per sample write (sum, count)
+// partials, one block per sample combines them in index order.
+constexpr int kRmsBlocks = 152;
+
+__global__ void __launch_bounds__(256) k_unet_rms_part(const float *__restrict__ div, const int32_t *__restrict__ tag,
+                                                       int64_t ncell, double *__restrict__ work) {
     __shared__ double red[32], cnt_red[32];
-    const int b = blockIdx.x;
+    const int b = blockIdx.y;
     double s = 0.0, c = 0.0;
-    for (int64_t q = threadIdx.x; q < ncell; q += blockDim.x) {
+    for (int64_t q = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; q < ncell; q += (int64_t)gridDim.x * blockDim.x) {
         const int64_t v = b * ncell + q;
         if (tag[v] == 1) {
             const double d = div[v];
             s += d * d;
             c += 1.0;
         }
+    }
+    s = block_sum(s, red);
+    c = block_sum(c, cnt_red);
+    if (threadIdx.x == 0) {
+        work[2 * ((int64_t)b * gridDim.x + blockIdx.x)] = s;
+        work[2 * ((int64_t)b * gridDim.x + blockIdx.x) + 1] = c;
+    }
+}
+
+__global__ void __launch_bounds__(256) k_unet_rms_final(const double *__restrict__ work, int parts,
+                                                        float *__restrict__ inv_scale) {
+    __shared__ double red[32], cnt_red[32];
+    const int b = blockIdx.x;
+    double s = 0.0, c = 0.0;
+    for (int q = threadIdx.x; q < parts; q += blockDim.x) {
+        s += work[2 * ((int64_t)b * parts + q)];
+        c += work[2 * ((int64_t)b * parts + q) + 1];
     }
     s = block_sum(s, red);
     c = block_sum(c, cnt_red);
@@ -291,11 +312,14 @@ static inline unsigned nb(int64_t n) { return blocks_for(n, 256, 152 * 16); }
 
 extern "C" {
 
-int flub_unet_input(const float *div, const int32_t *tag, int B, int64_t ncell, float *inv_scale, void *out,
-                    void *stream) {
-    FLUB_REQUIRE(div && tag && inv_scale && out && B > 0 && ncell > 0, "flub_unet_input: bad arguments");
+int flub_unet_input(const float *div, const int32_t *tag, int B, int64_t ncell, float *inv_scale, double *work,
+                    void *out, void *stream) {
+    FLUB_REQUIRE(div && tag && inv_scale && work && out && B > 0 && ncell > 0, "flub_unet_input: bad arguments");
     cudaStream_t s = as_stream(stream);
-    k_unet_rms<<<B, 256, 0, s>>>(div, tag, ncell, inv_scale);
+    const int parts = (int)((ncell + 255) / 256 < kRmsBlocks ? (ncell + 255) / 256 : kRmsBlocks);
+    k_unet_rms_part<<<dim3(parts, B), 256, 0, s>>>(div, tag, ncell, work);
+    FLUB_CHECK_LAUNCH();
+    k_unet_rms_final<<<B, 256, 0, s>>>(work, parts, inv_scale);
     FLUB_CHECK_LAUNCH();
     const int64_t n = (int64_t)B * ncell;
     k_unet_input<<<nb(n), 256, 0, s>>>(div, tag, inv_scale, ncell, n, static_cast<__nv_bfloat16 *>(out));

@@ -126,27 +126,24 @@ class WarmStart:
     child sums, the hierarchy's own tags there); its output is prolonged to
     the grid by cell-centred trilinear interpolation and scaled on the device
     by gamma = (d . b) / (d . L d) (MGPCG.set_initial_guess_scaled).  With
-    level=None the level whose extent matches the training grid (``train_n``)
-    is chosen: 0 at 128^3, 1 at 256^3, 2 at 512^3."""
+    level=None the finest level whose extent is at most ``max_extent`` and
+    whose shape the network accepts is used (64: level 1 at 128^3, level 2 at
+    256^3, level 3 at 512^3), which keeps the network's cost a small fraction
+    of a solve."""
 
-    def __init__(self, net, level=None, train_n=128):
+    def __init__(self, net, level=None, max_extent=64):
         self.net = net
         self.level = level
-        self.train_n = train_n
+        self.max_extent = max_extent
 
     def choose_level(self, mg):
         if self.level is not None:
             return self.level
-        best = None
-        for l in range(mg.n_mg_levels):
-            shp = mg.level_shape(l)
-            if UNet3D.check_shape(shp):
-                best = l
-                if max(shp) <= self.train_n:
-                    break
-        if best is None:
+        ok = [l for l in range(mg.n_mg_levels) if UNet3D.check_shape(mg.level_shape(l))]
+        if not ok:
             raise ValueError(f"no level of a {mg.shape} hierarchy fits the network's shape rules")
-        return best
+        small = [l for l in ok if max(mg.level_shape(l)) <= self.max_extent]
+        return small[0] if small else ok[-1]
 
     def guess(self, mg, level=None):
         """Unscaled guess d on the grid (0 off fluid)."""

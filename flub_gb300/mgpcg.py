@@ -33,7 +33,7 @@ PRECISIONS = {"fp32": 0, "mixed": 1}
 # reference's 6 << level; iterations of each bottom order; restriction scale)
 SCHEDULES = {
     "reference": (-1, 3, 1.0),   # multigrid/mgpcg.py:296-349
-    "v22": (2, 8, 0.5),          # 2 + 2 iterations per level, 8 + 8 at the bottom, restriction / 2
+    "v22": (2, 4, 0.5),          # 2 + 2 iterations per level, 4 + 4 at the bottom, restriction / 2
     "v33": (3, 8, 0.5),
 }
 

@@ -140,7 +140,8 @@ def unet_input(div, tag, inv_scale=None, out=None):
         inv_scale = torch.empty(B, dtype=torch.float32, device=div.device)
     if out is None:
         out = torch.empty(tuple(div.shape) + (IN_CHANNELS,), dtype=BF16, device=div.device)
-    _lib.call("flub_unet_input", _p(div), _p(tag), B, ncell, _p(inv_scale), _p(out), _s())
+    work = torch.empty(2 * 152 * B, dtype=torch.float64, device=div.device)
+    _lib.call("flub_unet_input", _p(div), _p(tag), B, ncell, _p(inv_scale), _p(work), _p(out), _s())
     return out, inv_scale
 
 

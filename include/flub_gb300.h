@@ -303,9 +303,11 @@ int flub_conv_error(int *out, int reset);
 
 /* Network input (16 channels): div / rms(div over fluid), fluid mask, solid
  * mask, zeros; tag is the reference's (0 air, 1 fluid, 2 solid) per sample of
- * ncell cells.  inv_scale[b] = 1 / rms (1 without fluid). */
-int flub_unet_input(const float *div, const int32_t *tag, int B, int64_t ncell, float *inv_scale, void *out,
-                    void *stream);
+ * ncell cells.  inv_scale[b] = 1 / rms (1 without fluid).  work: device
+ * scratch of FLUB_UNET_INPUT_WORK(B) doubles. */
+#define FLUB_UNET_INPUT_WORK(B) (2 * 152 * (B))
+int flub_unet_input(const float *div, const int32_t *tag, int B, int64_t ncell, float *inv_scale, double *work,
+                    void *out, void *stream);
 /* 2x average pool and its gradient (dx = dy / 8, optionally added to dx);
  * NX, NY, NZ are the fine extents. */
 int flub_pool2_bf16(const void *x, void *y, int B, int NX, int NY, int NZ, int C, void *stream);
