@@ -129,6 +129,30 @@ def run_profile_kernel(args):
     return 0
 
 
+SEED_BASE = {"dam256": 2, "dam512": 2, "sphere128": 1, "box64": 0}
+
+
+def replica_seed(config, rank):
+    """Each replica projects its own seeded scene (no data-path collective)."""
+    return SEED_BASE.get(config, 0) + rank
+
+
+def max_over_ranks(ms, world, device):
+    """The job's time: the slowest rank's (all_reduce MAX; any backend)."""
+    if world <= 1:
+        return ms
+    import torch
+    import torch.distributed as dist
+    t = torch.tensor([float(ms)], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def job_ms_per_projection(elapsed_ms, steps, world):
+    """Whole-job ms per projection: steps x world projections in elapsed_ms."""
+    return elapsed_ms / (steps * world)
+
+
 def dist_env():
     return int(os.environ.get("RANK", 0)), int(os.environ.get("LOCAL_RANK", 0)), int(os.environ.get("WORLD_SIZE", 1))
 
@@ -257,8 +281,7 @@ def run_ours(args):
     from flub_gb300.unet import UNet3D
 
     lib = _lib.load()
-    seed_base = {"dam256": 2, "dam512": 2, "sphere128": 1, "box64": 0}.get(args.config, 0)
-    scene = scenes.CONFIGS[args.config](seed=seed_base + rank)
+    scene = scenes.CONFIGS[args.config](seed=replica_seed(args.config, rank))
     n = scene.n_cells
 
     def dev(a):
@@ -309,12 +332,8 @@ def run_ours(args):
         clocks = sampler.stop() if sampler else None
         if world > 1:
             dist.barrier()
-        elapsed = ev0.elapsed_time(ev1)
+        elapsed = max_over_ranks(ev0.elapsed_time(ev1), world, "cuda")
         launches = (lib.flub_launch_count() - host_l0) + (proj.mg.kernels_executed() - dev_l0)
-        if world > 1:
-            t = torch.tensor([elapsed], device="cuda")
-            dist.all_reduce(t, op=dist.ReduceOp.MAX)
-            elapsed = float(t.item())
         return elapsed, proj.mg.info(), launches, clocks
 
     head = args.variant
@@ -348,7 +367,7 @@ def run_ours(args):
     pressures[head] = proj.p.f.detach().clone()
     div_after = proj.max_abs_div(vel, velr)
     ms_per_step = elapsed / args.steps
-    value = elapsed / (args.steps * world)
+    value = job_ms_per_projection(elapsed, args.steps, world)
 
     # ---- end to end through the public API with host buffers
     e2e = None
@@ -377,12 +396,8 @@ def run_ours(args):
             step_e2e()
         e1.record(stream)
         torch.cuda.synchronize()
-        et = e0.elapsed_time(e1)
-        if world > 1:
-            t = torch.tensor([et], device="cuda")
-            dist.all_reduce(t, op=dist.ReduceOp.MAX)
-            et = float(t.item())
-        e2e = {"value": et / (args.steps * world), "unit": UNIT,
+        et = max_over_ranks(e0.elapsed_time(e1), world, "cuda")
+        e2e = {"value": job_ms_per_projection(et, args.steps, world), "unit": UNIT,
                "h2d_bytes_per_step": int(sum(t.numel() * t.element_size() for t in h_in)),
                "d2h_bytes_per_step": int(sum(t.numel() * t.element_size() for t in h_out))}
 

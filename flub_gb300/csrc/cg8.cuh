@@ -27,9 +27,8 @@ __device__ __forceinline__ void store_row8(float *p, const float v[8]) {
 // order as lap_at.  Non-fluid cells get 0.
 __device__ __forceinline__ void lap_row8(const float *__restrict__ x, const uint8_t *__restrict__ code, const Dims D,
                                          int g, uint2 cc, float out[8], Row8 &xc) {
-    const int nz8 = D.nz >> 3;
-    const int kg = g % nz8, q = g / nz8;
-    const int j = q % D.ny, i = q / D.ny;
+    int i, j, kg;
+    group_ijk(g, D, i, j, kg);
     const int k0 = kg << 3;
     const int sj = D.nz, si = D.ny * D.nz;
     const int c0 = g << 3;

@@ -104,33 +104,30 @@ __global__ void k_tag_neumann(const float *__restrict__ phr, int32_t *__restrict
         if (phr[c] < 0.0f) tag[c] = 2;
 }
 
-__global__ void k_phi_prims(float *__restrict__ phi, int nx, int ny, int nz, float h, float h0, float sx, float sy,
-                            float sz, const PrimSet ps) {
-    const int64_t n = (int64_t)nx * ny * nz;
-    for (int64_t c = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; c < n; c += (int64_t)gridDim.x * blockDim.x) {
-        const int k = (int)(c % nz);
-        const int64_t t = c / nz;
-        const int j = (int)(t % ny), i = (int)(t / ny);
-        phi[c] = phi_prims_at(i, j, k, h, h0, sx, sy, sz, ps);
-    }
+// Grid: row_grid(nx, ny, nz) (one thread per cell, k along x).
+__global__ void __launch_bounds__(kRowThreads) k_phi_prims(float *__restrict__ phi, int nx, int ny, int nz, float h,
+                                                          float h0, float sx, float sy, float sz, const PrimSet ps) {
+    const int k = blockIdx.x * blockDim.x + threadIdx.x, j = blockIdx.y, i = blockIdx.z;
+    if (k >= nz) return;
+    const int64_t c = ((int64_t)i * ny + j) * nz + k;
+    phi[c] = phi_prims_at(i, j, k, h, h0, sx, sy, sz, ps);
 }
 
 // Fused: tag from phi, then solid from the primitives' cell-centre SDF.
-__global__ void k_classify(const float *__restrict__ phi, int32_t *__restrict__ tag, float *__restrict__ phr,
-                           int nx, int ny, int nz, float h, float h0, const PrimSet ps) {
-    const int64_t n = (int64_t)nx * ny * nz;
-    for (int64_t c = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; c < n; c += (int64_t)gridDim.x * blockDim.x) {
-        int t = phi[c] > 0.0f ? 0 : 1;
-        if (ps.n > 0 || phr) {
-            const int k = (int)(c % nz);
-            const int64_t q = c / nz;
-            const int j = (int)(q % ny), i = (int)(q / ny);
-            const float s = phi_prims_at(i, j, k, h, h0, 0.5f, 0.5f, 0.5f, ps);
-            if (phr) phr[c] = s;
-            if (s < 0.0f) t = 2;
-        }
-        tag[c] = t;
+// Grid: row_grid(nx, ny, nz).
+__global__ void __launch_bounds__(kRowThreads) k_classify(const float *__restrict__ phi, int32_t *__restrict__ tag,
+                                                         float *__restrict__ phr, int nx, int ny, int nz, float h,
+                                                         float h0, const PrimSet ps) {
+    const int k = blockIdx.x * blockDim.x + threadIdx.x, j = blockIdx.y, i = blockIdx.z;
+    if (k >= nz) return;
+    const int64_t c = ((int64_t)i * ny + j) * nz + k;
+    int t = phi[c] > 0.0f ? 0 : 1;
+    if (ps.n > 0 || phr) {
+        const float s = phi_prims_at(i, j, k, h, h0, 0.5f, 0.5f, 0.5f, ps);
+        if (phr) phr[c] = s;
+        if (s < 0.0f) t = 2;
     }
+    tag[c] = t;
 }
 
 static int make_primset(const flub_prim *prims, int nprims, PrimSet *ps) {
@@ -172,7 +169,8 @@ int flub_phi_prims(float *phi, int nx, int ny, int nz, float h, float h0, float 
     PrimSet ps;
     int st = make_primset(prims, nprims, &ps);
     if (st) return st;
-    k_phi_prims<<<blocks_for(n, 256), 256, 0, as_stream(stream)>>>(phi, nx, ny, nz, h, h0, sx, sy, sz, ps);
+    FLUB_REQUIRE(nx < 65536 && ny < 65536, "flub_phi_prims: nx, ny must be below 65536");
+    k_phi_prims<<<row_grid(nx, ny, nz), kRowThreads, 0, as_stream(stream)>>>(phi, nx, ny, nz, h, h0, sx, sy, sz, ps);
     FLUB_CHECK_LAUNCH();
     return FLUB_OK;
 }
@@ -186,7 +184,9 @@ int flub_classify(const float *phi, const flub_prim *prims, int nprims, int nx, 
     PrimSet ps;
     int st = make_primset(prims, nprims, &ps);
     if (st) return st;
-    k_classify<<<blocks_for(n, 256), 256, 0, as_stream(stream)>>>(phi, tag, phi_rigid, nx, ny, nz, h, h0, ps);
+    FLUB_REQUIRE(nx < 65536 && ny < 65536, "flub_classify: nx, ny must be below 65536");
+    k_classify<<<row_grid(nx, ny, nz), kRowThreads, 0, as_stream(stream)>>>(phi, tag, phi_rigid, nx, ny, nz, h, h0,
+                                                                          ps);
     FLUB_CHECK_LAUNCH();
     return FLUB_OK;
 }

@@ -55,6 +55,13 @@ static inline unsigned blocks_for(int64_t n, int threads, int64_t cap = 152 * 32
     return (unsigned)b;
 }
 
+// Row-wise launch for per-cell / per-face kernels: blockIdx.z = i, blockIdx.y
+// = j, k along x; no integer division per cell.
+constexpr int kRowThreads = 128;
+static inline dim3 row_grid(int nx, int ny, int nz) {
+    return dim3((unsigned)((nz + kRowThreads - 1) / kRowThreads), (unsigned)ny, (unsigned)nx);
+}
+
 // ------------------------------------------------------------------ cell codes
 // The solver stores one byte per cell.  The byte is chosen so that "outside
 // the domain" (a zero byte, e.g. a TMA out-of-bounds fill) behaves like a solid

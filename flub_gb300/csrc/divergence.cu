@@ -9,20 +9,20 @@
 namespace flub {
 
 template <bool kMasked>
-__global__ void __launch_bounds__(256) k_divergence(const float *__restrict__ u, const float *__restrict__ v,
+__global__ void __launch_bounds__(kRowThreads) k_divergence(const float *__restrict__ u, const float *__restrict__ v,
                                                     const float *__restrict__ w, const float *__restrict__ ur,
                                                     const float *__restrict__ vr, const float *__restrict__ wr,
                                                     const int32_t *__restrict__ tag, float *__restrict__ div, int nx,
                                                     int ny, int nz, float scale) {
-    const int64_t n = (int64_t)nx * ny * nz;
+    // grid: row_grid(nx, ny, nz)
+    const int k = blockIdx.x * blockDim.x + threadIdx.x, j = blockIdx.y, i = blockIdx.z;
+    if (k >= nz) return;
     const int64_t sj = nz, si = (int64_t)ny * nz;
-    for (int64_t c = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; c < n; c += (int64_t)gridDim.x * blockDim.x) {
-        const int k = (int)(c % nz);
-        const int64_t q = c / nz;
-        const int j = (int)(q % ny), i = (int)(q / ny);
+    const int64_t c = ((int64_t)i * ny + j) * nz + k;
+    {
         if (kMasked && __ldg(&tag[c]) != 1) {
             div[c] = 0.0f;
-            continue;
+            return;
         }
         // face indices: u (nx+1, ny, nz), v (nx, ny+1, nz), w (nx, ny, nz+1)
         const int64_t uL = c, uR = c + si;
@@ -54,6 +54,7 @@ __global__ void k_scale(float *__restrict__ q, float s, int64_t n) {
 static int check_div_args(const float *u, const float *v, const float *w, const float *ur, const float *vr,
                           const float *wr, const int32_t *tag, float *div, int nx, int ny, int nz) {
     FLUB_REQUIRE(nx > 0 && ny > 0 && nz > 0, "divergence: shape (%d, %d, %d) must be positive", nx, ny, nz);
+    FLUB_REQUIRE(nx < 65536 && ny < 65536, "divergence: nx, ny must be below 65536");
     FLUB_REQUIRE(u && v && w && ur && vr && wr && tag && div, "divergence: NULL pointer argument");
     return FLUB_OK;
 }
@@ -68,8 +69,7 @@ int flub_divergence_tag(const float *u, const float *v, const float *w, const fl
                         const float *wr, const int32_t *tag, float *div, int nx, int ny, int nz, void *stream) {
     int st = check_div_args(u, v, w, ur, vr, wr, tag, div, nx, ny, nz);
     if (st) return st;
-    const int64_t n = (int64_t)nx * ny * nz;
-    k_divergence<false><<<blocks_for(n, 256), 256, 0, as_stream(stream)>>>(u, v, w, ur, vr, wr, tag, div, nx, ny,
+    k_divergence<false><<<row_grid(nx, ny, nz), kRowThreads, 0, as_stream(stream)>>>(u, v, w, ur, vr, wr, tag, div, nx, ny,
                                                                            nz, 1.0f);
     FLUB_CHECK_LAUNCH();
     return FLUB_OK;
@@ -80,8 +80,7 @@ int flub_divergence_masked(const float *u, const float *v, const float *w, const
                            void *stream) {
     int st = check_div_args(u, v, w, ur, vr, wr, tag, div, nx, ny, nz);
     if (st) return st;
-    const int64_t n = (int64_t)nx * ny * nz;
-    k_divergence<true><<<blocks_for(n, 256), 256, 0, as_stream(stream)>>>(u, v, w, ur, vr, wr, tag, div, nx, ny,
+    k_divergence<true><<<row_grid(nx, ny, nz), kRowThreads, 0, as_stream(stream)>>>(u, v, w, ur, vr, wr, tag, div, nx, ny,
                                                                           nz, scale);
     FLUB_CHECK_LAUNCH();
     return FLUB_OK;

@@ -16,17 +16,18 @@ __device__ __forceinline__ float grad_face(float uf, float urf, float plo, float
     return 0.0f;
 }
 
-__global__ void __launch_bounds__(256) k_subtract_gradient_axis(float *__restrict__ uf, const float *__restrict__ urf,
-                                                                const float *__restrict__ p,
-                                                                const int32_t *__restrict__ tag, int nx, int ny,
-                                                                int nz, int d) {
-    const int fx = nx + (d == 1), fy = ny + (d == 2), fz = nz + (d == 3);
+// Grid: row_grid over the face array's extents (fx, fy, fz).
+__global__ void __launch_bounds__(kRowThreads) k_subtract_gradient_axis(float *__restrict__ uf,
+                                                                       const float *__restrict__ urf,
+                                                                       const float *__restrict__ p,
+                                                                       const int32_t *__restrict__ tag, int nx, int ny,
+                                                                       int nz, int d) {
+    const int fy = ny + (d == 2), fz = nz + (d == 3);
     const int nd = d == 1 ? nx : (d == 2 ? ny : nz);
-    const int64_t n = (int64_t)fx * fy * fz;
-    for (int64_t f = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; f < n; f += (int64_t)gridDim.x * blockDim.x) {
-        const int k = (int)(f % fz);
-        const int64_t q = f / fz;
-        const int j = (int)(q % fy), i = (int)(q / fy);
+    const int k = blockIdx.x * blockDim.x + threadIdx.x, j = blockIdx.y, i = blockIdx.z;
+    if (k >= fz) return;
+    const int64_t f = ((int64_t)i * fy + j) * fz + k;
+    {
         const int ii = d == 1 ? i : (d == 2 ? j : k);
         if (0 < ii && ii < nd) {
             const int64_t chi = ((int64_t)i * ny + j) * nz + k;
@@ -39,20 +40,19 @@ __global__ void __launch_bounds__(256) k_subtract_gradient_axis(float *__restric
     }
 }
 
-__global__ void __launch_bounds__(256) k_subtract_gradient_all(float *__restrict__ u, float *__restrict__ v,
+__global__ void __launch_bounds__(kRowThreads) k_subtract_gradient_all(float *__restrict__ u, float *__restrict__ v,
                                                                float *__restrict__ w, const float *__restrict__ ur,
                                                                const float *__restrict__ vr,
                                                                const float *__restrict__ wr,
                                                                const float *__restrict__ p, float ps,
                                                                const int32_t *__restrict__ tag, int nx, int ny,
                                                                int nz) {
-    const int ex = nx + 1, ey = ny + 1, ez = nz + 1;
-    const int64_t n = (int64_t)ex * ey * ez;
+    // grid: row_grid(nx + 1, ny + 1, nz + 1), one thread per (i, j, k) of the extended index space
+    const int ey = ny + 1, ez = nz + 1;
     const int64_t si = (int64_t)ny * nz, sj = nz;
-    for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < n; e += (int64_t)gridDim.x * blockDim.x) {
-        const int k = (int)(e % ez);
-        const int64_t q = e / ez;
-        const int j = (int)(q % ey), i = (int)(q / ey);
+    const int k = blockIdx.x * blockDim.x + threadIdx.x, j = blockIdx.y, i = blockIdx.z;
+    if (k >= ez) return;
+    {
         const int64_t c = ((int64_t)i * ny + j) * nz + k;  // cell (i, j, k) when inside
         if (j < ny && k < nz) {  // u face (i, j, k), i in [0, nx]
             const int64_t f = ((int64_t)i * ny + j) * nz + k;
@@ -92,8 +92,9 @@ int flub_subtract_gradient_tag(float *uf, const float *urf, const float *p, cons
     FLUB_REQUIRE(nx > 0 && ny > 0 && nz > 0, "subtract_gradient: shape must be positive");
     FLUB_REQUIRE(d >= 1 && d <= 3, "subtract_gradient: d=%d must be 1, 2 or 3", d);
     FLUB_REQUIRE(uf && urf && p && tag, "subtract_gradient: NULL pointer argument");
-    const int64_t n = (int64_t)(nx + (d == 1)) * (ny + (d == 2)) * (nz + (d == 3));
-    k_subtract_gradient_axis<<<blocks_for(n, 256), 256, 0, as_stream(stream)>>>(uf, urf, p, tag, nx, ny, nz, d);
+    FLUB_REQUIRE(nx < 65535 && ny < 65535, "subtract_gradient: nx, ny must be below 65535");
+    k_subtract_gradient_axis<<<row_grid(nx + (d == 1), ny + (d == 2), nz + (d == 3)), kRowThreads, 0,
+                               as_stream(stream)>>>(uf, urf, p, tag, nx, ny, nz, d);
     FLUB_CHECK_LAUNCH();
     return FLUB_OK;
 }
@@ -102,9 +103,9 @@ int flub_subtract_gradient(float *u, float *v, float *w, const float *ur, const 
                            const float *p, float p_scale, const int32_t *tag, int nx, int ny, int nz, void *stream) {
     FLUB_REQUIRE(nx > 0 && ny > 0 && nz > 0, "subtract_gradient: shape must be positive");
     FLUB_REQUIRE(u && v && w && ur && vr && wr && p && tag, "subtract_gradient: NULL pointer argument");
-    const int64_t n = (int64_t)(nx + 1) * (ny + 1) * (nz + 1);
-    k_subtract_gradient_all<<<blocks_for(n, 256), 256, 0, as_stream(stream)>>>(u, v, w, ur, vr, wr, p, p_scale, tag,
-                                                                               nx, ny, nz);
+    FLUB_REQUIRE(nx < 65535 && ny < 65535, "subtract_gradient: nx, ny must be below 65535");
+    k_subtract_gradient_all<<<row_grid(nx + 1, ny + 1, nz + 1), kRowThreads, 0, as_stream(stream)>>>(
+        u, v, w, ur, vr, wr, p, p_scale, tag, nx, ny, nz);
     FLUB_CHECK_LAUNCH();
     return FLUB_OK;
 }

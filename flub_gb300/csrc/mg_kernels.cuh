@@ -151,6 +151,23 @@ __global__ void k_restrict_codes(const uint8_t *__restrict__ cf, uint8_t *__rest
     }
 }
 
+// (i, j, kg) of group g (8 cells along k starting at k = 8 kg) of a grid with
+// nz % 8 == 0; shifts instead of divisions when nz / 8 and ny are powers of two.
+__device__ __forceinline__ void group_ijk(int g, const Dims D, int &i, int &j, int &kg) {
+    const int nz8 = D.nz >> 3;
+    if (((nz8 & (nz8 - 1)) | (D.ny & (D.ny - 1))) == 0) {
+        const int q = g >> (__ffs(nz8) - 1);
+        kg = g & (nz8 - 1);
+        j = q & (D.ny - 1);
+        i = q >> (__ffs(D.ny) - 1);
+    } else {
+        const int q = g / nz8;
+        kg = g - q * nz8;
+        j = q % D.ny;
+        i = q / D.ny;
+    }
+}
+
 // ---------------------------------------------------------------- active 8-cell groups
 // A level's "active list" holds, in ascending order, the index of every group
 // of 8 consecutive cells along k that contains a fluid cell.  Kernels that

@@ -20,6 +20,7 @@
 #include "cg8.cuh"
 #include "cluster.cuh"
 #include "mixed.cuh"
+#include "restrict8.cuh"
 #include "smooth8.cuh"
 #include "tail.cuh"
 
@@ -372,7 +373,7 @@ static int sweep8(const LaunchCtx &c, const Level &L, int phase, int mode, int s
     // groups are visited; one resident wave of blocks, grid-stride
     const int *act = skip ? L.act : nullptr;
     const int *act_n = skip ? L.act_n : nullptr;
-    const dim3 blk(256), grd(blocks_for(D.n() >> 3, 256, kNumSMs * 4));
+    const dim3 blk(256), grd(blocks_for(D.n() >> 3, 256, kNumSMs * 3));  // 3 resident blocks per SM
     if (mode == kSweepFromZero)
         return launch_pdl(k_smooth8<true, false, TO, TO, TR, TC>, grd, blk, 0, c.s, zout, (const TO *)zout,
                           (const TC *)nullptr, 1.0f, r, (const uint8_t *)L.code, D, phase, act, act_n, c.kc);
@@ -419,8 +420,14 @@ static int enqueue_vcycle(flub_mg *mg, const LaunchCtx &c, const float *r0, floa
             FLUB_TRY(sweep(c, L, 1, kSweepInPlace, sk, R(l), ZP(l), ZP(l), nullptr));
         }
         const Level &C = mg->lv[l + 1];
-        FLUB_TRY(launch_pdl(k_restrict, dim3(blocks_for(C.D.n(), 256, 1 << 20)), dim3(256), 0, c.s, R(l), ZP(l),
-                            L.code, C.r, C.code, C.D, mg->sched_rscale, c.kc));
+        if (L.D.nz % 8 == 0)
+            FLUB_TRY(launch_pdl(k_restrict8<float, float, float>, dim3(blocks_for(C.D.n() >> 2, 256, kNumSMs * 8)),
+                                dim3(256), 0, c.s, R(l), (const float *)ZP(l), (const uint8_t *)L.code, C.r,
+                                (const uint8_t *)C.code, C.D, mg->sched_rscale, (const int *)C.act,
+                                (const int *)C.act_n, c.kc));
+        else
+            FLUB_TRY(launch_pdl(k_restrict, dim3(blocks_for(C.D.n(), 256, 1 << 20)), dim3(256), 0, c.s, R(l), ZP(l),
+                                L.code, C.r, C.code, C.D, mg->sched_rscale, c.kc));
     }
     if (use_cl) {
         ClusterParams P = {};
@@ -518,9 +525,10 @@ static int enqueue_vcycle_mixed(flub_mg *mg, const LaunchCtx &c, float *z0, bool
                                                             1.0f));
         }
         const Level &C = mg->lv[l + 1];
-        FLUB_TRY(launch_pdl(k_restrict_t<__half, __half, __half>, dim3(blocks_for(C.D.n(), 256, 1 << 20)), dim3(256),
-                            0, c.s, (const __half *)L.rh, (const __half *)L.z2h, (const uint8_t *)L.code, C.rh,
-                            (const uint8_t *)C.code, C.D, 0.125f * mg->sched_rscale, c.kc));
+        FLUB_TRY(launch_pdl(k_restrict8<__half, __half, __half>, dim3(blocks_for(C.D.n() >> 2, 256, kNumSMs * 8)),
+                            dim3(256), 0, c.s, (const __half *)L.rh, (const __half *)L.z2h, (const uint8_t *)L.code,
+                            C.rh, (const uint8_t *)C.code, C.D, 0.125f * mg->sched_rscale, (const int *)C.act,
+                            (const int *)C.act_n, c.kc));
     }
     if (lt < Lm) {
         if (lt == 0)
@@ -1036,6 +1044,10 @@ int flub_mg_set_tags(flub_mg *mg, const int32_t *tag, void *stream) {
     // 8-cell groups without fluid and rely on it)
     for (int l = 0; l < mg->levels; l++) {
         const size_t b = sizeof(float) * (size_t)mg->lv[l].D.n();
+        // coarse residuals: the list-based restriction writes only groups with
+        // fluid; the others must read 0
+        if (l > 0) FLUB_CHECK_CUDA(cudaMemsetAsync(mg->lv[l].r, 0, b, s));
+        if (l > 0 && mg->lv[l].rh) FLUB_CHECK_CUDA(cudaMemsetAsync(mg->lv[l].rh, 0, b / 2, s));
         FLUB_CHECK_CUDA(cudaMemsetAsync(mg->lv[l].z, 0, b, s));
         FLUB_CHECK_CUDA(cudaMemsetAsync(mg->lv[l].z2, 0, b, s));
         if (mg->lv[l].zh) FLUB_CHECK_CUDA(cudaMemsetAsync(mg->lv[l].zh, 0, b / 2, s));

@@ -76,17 +76,16 @@ __device__ __forceinline__ float coarse_at(const TC *__restrict__ p, float scale
 // without one every group is.
 // Grid: one-dimensional, grid-stride over the groups.  Requires nz % 8 == 0.
 template <bool kFromZero, bool kProlong, typename TO, typename TI, typename TR, typename TC>
-__global__ void __launch_bounds__(256, 4) k_smooth8(TO *zout, const TI *zin, const TC *__restrict__ zc,
+__global__ void __launch_bounds__(256, 3) k_smooth8(TO *zout, const TI *zin, const TC *__restrict__ zc,
                                                     float zc_scale, const TR *__restrict__ r,
                                                     const uint8_t *__restrict__ code, Dims D, int phase,
                                                     const int *__restrict__ act, const int *__restrict__ act_n,
                                                     unsigned long long *kc) {
     count_kernel(kc);
-    const int nz8 = D.nz >> 3;
     const int ng = (int)(D.n() >> 3);
     FLUB_ACT_LOOP(g, act, act_n, ng) {
-    const int kg = g % nz8, jq = g / nz8;
-    const int j = jq % D.ny, i = jq / D.ny;
+    int i, j, kg;
+    group_ijk(g, D, i, j, kg);
     const int k0 = kg << 3;
     const int sj = D.nz, si = D.ny * D.nz;
     const int c0 = (i * D.ny + j) * D.nz + k0;

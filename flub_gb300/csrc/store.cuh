@@ -31,6 +31,9 @@ struct St<float> {
         reinterpret_cast<float4 *>(p)[0] = make_float4(v[0], v[1], v[2], v[3]);
         reinterpret_cast<float4 *>(p)[1] = make_float4(v[4], v[5], v[6], v[7]);
     }
+    static __device__ __forceinline__ void st4(float *p, const float v[4]) {
+        *reinterpret_cast<float4 *>(p) = make_float4(v[0], v[1], v[2], v[3]);
+    }
 };
 
 template <>
@@ -65,6 +68,13 @@ struct St<__half> {
 #pragma unroll
         for (int q = 0; q < 4; q++) h[q] = __floats2half2_rn(v[2 * q], v[2 * q + 1]);
         *reinterpret_cast<uint4 *>(p) = u;
+    }
+    static __device__ __forceinline__ void st4(__half *p, const float v[4]) {
+        uint2 u;
+        __half2 *h = reinterpret_cast<__half2 *>(&u);
+        h[0] = __floats2half2_rn(v[0], v[1]);
+        h[1] = __floats2half2_rn(v[2], v[3]);
+        *reinterpret_cast<uint2 *>(p) = u;
     }
 };
 
