@@ -11,8 +11,9 @@ loaded on first use; there is no CPU fallback.
 """
 from .fields import (DEFAULT_SHAPE, Field, IntField, MACGrid, MACGridInt, field_like, field_shape, get_uf,
                      make_field, make_mac_grid)
-from .kernels import (_tag_dirichlet, _tag_neumann, classify, divergence, divergence_tag, launch, mask_with_tag,
-                      phi_prims, precompute_grid_point_phi_prims, scale_by_3d, subtract_gradient,
+from .kernels import (_tag_dirichlet, _tag_neumann, classify, divergence, divergence_tag, extrapolate,
+                      extrapolate_3d, extrapolate_by_1, flush_1_3d, launch, mask_with_tag, phi_prims,
+                      precompute_grid_point_phi_prims, scale_by_3d, set_unknown, set_unknown_3d, subtract_gradient,
                       subtract_gradient_tag, tag_dirichlet, tag_neumann)
 from ._lib import FlubError
 from .mgpcg import MGPCG
@@ -22,5 +23,6 @@ __all__ = [
     "DEFAULT_SHAPE", "Field", "IntField", "MACGrid", "MACGridInt", "field_like", "field_shape", "get_uf",
     "make_field", "make_mac_grid", "_tag_dirichlet", "_tag_neumann", "classify", "divergence", "divergence_tag",
     "launch", "mask_with_tag", "phi_prims", "precompute_grid_point_phi_prims", "scale_by_3d", "subtract_gradient",
-    "subtract_gradient_tag", "tag_dirichlet", "tag_neumann", "MGPCG", "Projection", "FlubError",
+    "subtract_gradient_tag", "tag_dirichlet", "tag_neumann", "MGPCG", "Projection", "FlubError", "extrapolate",
+    "extrapolate_3d", "extrapolate_by_1", "flush_1_3d", "set_unknown", "set_unknown_3d",
 ]

@@ -53,6 +53,10 @@ SIGNATURES = {
     "flub_divergence_masked": (_i32, [_vp] * 8 + [_f32, _i32, _i32, _i32, _vp]),
     "flub_subtract_gradient_tag": (_i32, [_vp, _vp, _vp, _vp, _i32, _i32, _i32, _i32, _vp]),
     "flub_subtract_gradient": (_i32, [_vp] * 7 + [_f32, _vp, _i32, _i32, _i32, _vp]),
+    "flub_set_unknown": (_i32, [_vp, _vp, _vp, _vp, _i32, _i32, _i32, _vp]),
+    "flub_extrapolate_axis": (_i32, [_vp, _vp, _i32, _i32, _i32, _i32, _vp]),
+    "flub_flush_unknown": (_i32, [_vp, _i64, _vp]),
+    "flub_extrapolate": (_i32, [_vp] * 7 + [_i32, _i32, _i32, _i32, _vp]),
     "flub_mg_workspace_bytes": (_sz, [_i32, _i32, _i32, _i32, _i32]),
     "flub_mg_create": (_i32, [_i32, _i32, _i32, _i32, _i32, _vp, _sz, ctypes.POINTER(_vp)]),
     "flub_mg_destroy": (_i32, [_vp]),

@@ -24,9 +24,10 @@ __device__ __forceinline__ void store_row8(float *p, const float v[8]) {
 }
 
 // L x for the 8 cells of the row starting at c0 (group g), same operation
-// order as lap_at.  Non-fluid cells get 0.
-__device__ __forceinline__ void lap_row8(const float *__restrict__ x, const uint8_t *__restrict__ code, const Dims D,
-                                         int g, uint2 cc, float out[8], Row8 &xc) {
+// order as lap_at, from the stencil words (sw, or the codes when sw is NULL).
+// Non-fluid cells get 0.
+__device__ __forceinline__ void lap_row8(const float *__restrict__ x, const uint8_t *__restrict__ code,
+                                         const uint16_t *__restrict__ sw, const Dims D, int g, float out[8], Row8 &xc) {
     int i, j, kg;
     group_ijk(g, D, i, j, kg);
     const int k0 = kg << 3;
@@ -34,13 +35,7 @@ __device__ __forceinline__ void lap_row8(const float *__restrict__ x, const uint
     const int c0 = g << 3;
     const bool hip = i + 1 < D.nx, him = i > 0, hjp = j + 1 < D.ny, hjm = j > 0;
     const bool hkp = k0 + 8 < D.nz, hkm = k0 > 0;
-    const uint2 z2 = make_uint2(0u, 0u);
-    const uint2 cip = hip ? load_codes8(code + c0 + si) : z2;
-    const uint2 cim = him ? load_codes8(code + c0 - si) : z2;
-    const uint2 cjp = hjp ? load_codes8(code + c0 + sj) : z2;
-    const uint2 cjm = hjm ? load_codes8(code + c0 - sj) : z2;
-    const uint8_t ckm = hkm ? __ldg(code + c0 - 1) : (uint8_t)0;
-    const uint8_t ckp = hkp ? __ldg(code + c0 + 8) : (uint8_t)0;
+    const uint4 wd = load_words8(sw, code, D, i, j, k0, c0);
     Row8 xip, xim, xjp, xjm;
     load_row8(x + c0, xc);
     if (hip) load_row8(x + c0 + si, xip); else zero_row8(xip);
@@ -52,33 +47,33 @@ __device__ __forceinline__ void lap_row8(const float *__restrict__ x, const uint
 #pragma unroll
     for (int m = 0; m < 8; m++) {
         out[m] = 0.0f;
-        if (code_at(cc, m) != kCodeFluid) continue;
+        const uint32_t w = word_at(wd, m);
+        if (sw_code(w, 0) != kCodeFluid) continue;
         const float c = xc.v[m];
         float tp, tm, ret = 0.0f;
-        uint8_t cn;
+        uint32_t cn;
         tp = 0.0f; tm = 0.0f;
-        cn = code_at(cip, m); if (cn != kCodeSolid) tp = __fsub_rn(cn == kCodeAir ? 0.0f : xip.v[m], c);
-        cn = code_at(cim, m); if (cn != kCodeSolid) tm = __fsub_rn(cn == kCodeAir ? 0.0f : xim.v[m], c);
+        cn = sw_code(w, 1); if (cn != kCodeSolid) tp = __fsub_rn(cn == kCodeAir ? 0.0f : xip.v[m], c);
+        cn = sw_code(w, 2); if (cn != kCodeSolid) tm = __fsub_rn(cn == kCodeAir ? 0.0f : xim.v[m], c);
         ret = __fadd_rn(ret, __fadd_rn(tp, tm));
         tp = 0.0f; tm = 0.0f;
-        cn = code_at(cjp, m); if (cn != kCodeSolid) tp = __fsub_rn(cn == kCodeAir ? 0.0f : xjp.v[m], c);
-        cn = code_at(cjm, m); if (cn != kCodeSolid) tm = __fsub_rn(cn == kCodeAir ? 0.0f : xjm.v[m], c);
+        cn = sw_code(w, 3); if (cn != kCodeSolid) tp = __fsub_rn(cn == kCodeAir ? 0.0f : xjp.v[m], c);
+        cn = sw_code(w, 4); if (cn != kCodeSolid) tm = __fsub_rn(cn == kCodeAir ? 0.0f : xjm.v[m], c);
         ret = __fadd_rn(ret, __fadd_rn(tp, tm));
         tp = 0.0f; tm = 0.0f;
-        cn = m < 7 ? code_at(cc, m + 1) : ckp;
+        cn = sw_code(w, 5);
         if (cn != kCodeSolid) tp = __fsub_rn(cn == kCodeAir ? 0.0f : (m < 7 ? xc.v[m + 1] : xkp), c);
-        cn = m > 0 ? code_at(cc, m - 1) : ckm;
+        cn = sw_code(w, 6);
         if (cn != kCodeSolid) tm = __fsub_rn(cn == kCodeAir ? 0.0f : (m > 0 ? xc.v[m - 1] : xkm), c);
         ret = __fadd_rn(ret, __fadd_rn(tp, tm));
         out[m] = ret;
     }
 }
 
-
 // Ap = L p, p.Ap -> alpha (mgpcg.py:410-419); guarded like k_matvec_pap.
 __global__ void __launch_bounds__(kRedThreads) k8_matvec_pap(MgState *st, const float *__restrict__ p,
                                                              float *__restrict__ Ap, const uint8_t *__restrict__ code,
-                                                             Dims D, double *partials, const int *__restrict__ act,
+                                                             const uint16_t *__restrict__ sw, Dims D, double *partials, const int *__restrict__ act,
                                                              const int *__restrict__ act_n, unsigned long long *kc) {
     __shared__ double red[32];
     count_kernel(kc);
@@ -90,7 +85,7 @@ __global__ void __launch_bounds__(kRedThreads) k8_matvec_pap(MgState *st, const 
         if (!act && !group_has_fluid(cc)) continue;  // Ap = 0 there already
         float a[8];
         Row8 pc;
-        lap_row8(p, code, D, g, cc, a, pc);
+        lap_row8(p, code, sw, D, g, a, pc);
         store_row8(Ap + (g << 3), a);
 #pragma unroll
         for (int m = 0; m < 8; m++) s = fma((double)pc.v[m], (double)a[m], s);
@@ -249,7 +244,8 @@ __global__ void __launch_bounds__(256) k8_update_xp(MgState *st, float *__restri
 // r -= L x0 when an initial guess was given (no reference counterpart); L x0
 // is 0 off the fluid, so only the active groups change.
 __global__ void __launch_bounds__(256) k8_residual_x0(MgState *st, float *__restrict__ r, const float *__restrict__ x,
-                                                      const uint8_t *__restrict__ code, Dims D,
+                                                      const uint8_t *__restrict__ code,
+                                                      const uint16_t *__restrict__ sw, Dims D,
                                                       const int *__restrict__ act, const int *__restrict__ act_n,
                                                       unsigned long long *kc) {
     count_kernel(kc);
@@ -260,7 +256,7 @@ __global__ void __launch_bounds__(256) k8_residual_x0(MgState *st, float *__rest
         if (!act && !group_has_fluid(cc)) continue;
         float lx[8];
         Row8 xc, rv;
-        lap_row8(x, code, D, g, cc, lx, xc);
+        lap_row8(x, code, sw, D, g, lx, xc);
         load_row8_rw(r + (g << 3), rv);
 #pragma unroll
         for (int m = 0; m < 8; m++)
@@ -273,7 +269,8 @@ __global__ void __launch_bounds__(256) k8_residual_x0(MgState *st, float *__rest
 // multiple of d closest to the solution of L x = b in the energy norm.
 __global__ void __launch_bounds__(kRedThreads) k8_x0_gamma(MgState *st, const float *__restrict__ d,
                                                            const float *__restrict__ b,
-                                                           const uint8_t *__restrict__ code, Dims D, double *partials,
+                                                           const uint8_t *__restrict__ code,
+                                                           const uint16_t *__restrict__ sw, Dims D, double *partials,
                                                            const int *__restrict__ act,
                                                            const int *__restrict__ act_n) {
     __shared__ double red[32];
@@ -284,7 +281,7 @@ __global__ void __launch_bounds__(kRedThreads) k8_x0_gamma(MgState *st, const fl
         if (!act && !group_has_fluid(cc)) continue;
         float ld[8];
         Row8 dc, bv;
-        lap_row8(d, code, D, g, cc, ld, dc);
+        lap_row8(d, code, sw, D, g, ld, dc);
         load_row8(b + (g << 3), bv);
 #pragma unroll
         for (int m = 0; m < 8; m++) {

@@ -46,6 +46,8 @@ struct Level {
     // active 8-cell groups (ascending) and their count on the device; NULL
     // when nz is not a multiple of 8 (the scalar kernels run there)
     int *act, *act_n;
+    // stencil words (smooth8.cuh), same condition
+    uint16_t *sw;
 };
 
 struct LaunchCtx {
@@ -137,9 +139,11 @@ static size_t carve(flub_mg *mg, char *base) {
             L.z2h = (__half *)take(sizeof(__half) * nl);
         }
         L.act = L.act_n = nullptr;
+        L.sw = nullptr;
         if (L.D.nz % 8 == 0) {
             L.act = (int *)take(sizeof(int) * (size_t)(nl >> 3));
             L.act_n = (int *)take(sizeof(int));
+            L.sw = (uint16_t *)take(sizeof(uint16_t) * (size_t)nl);
         }
     }
     // per-block counts of the active-list build (level 0 has the most blocks)
@@ -376,12 +380,14 @@ static int sweep8(const LaunchCtx &c, const Level &L, int phase, int mode, int s
     const dim3 blk(256), grd(blocks_for(D.n() >> 3, 256, kNumSMs * 3));  // 3 resident blocks per SM
     if (mode == kSweepFromZero)
         return launch_pdl(k_smooth8<true, false, TO, TO, TR, TC>, grd, blk, 0, c.s, zout, (const TO *)zout,
-                          (const TC *)nullptr, 1.0f, r, (const uint8_t *)L.code, D, phase, act, act_n, c.kc);
+                          (const TC *)nullptr, 1.0f, r, (const uint8_t *)L.code, (const uint16_t *)L.sw, D, phase,
+                          act, act_n, c.kc);
     if (mode == kSweepProlong)
         return launch_pdl(k_smooth8<false, true, TO, TI, TR, TC>, grd, blk, 0, c.s, zout, zin, zc, zc_scale, r,
-                          (const uint8_t *)L.code, D, phase, act, act_n, c.kc);
+                          (const uint8_t *)L.code, (const uint16_t *)L.sw, D, phase, act, act_n, c.kc);
     return launch_pdl(k_smooth8<false, false, TO, TO, TR, TC>, grd, blk, 0, c.s, zout, (const TO *)zout,
-                      (const TC *)nullptr, 1.0f, r, (const uint8_t *)L.code, D, phase, act, act_n, c.kc);
+                      (const TC *)nullptr, 1.0f, r, (const uint8_t *)L.code, (const uint16_t *)L.sw, D, phase, act,
+                      act_n, c.kc);
 }
 
 static int sweep(const LaunchCtx &c, const Level &L, int phase, int mode, int skip, const float *r,
@@ -422,7 +428,8 @@ static int enqueue_vcycle(flub_mg *mg, const LaunchCtx &c, const float *r0, floa
         const Level &C = mg->lv[l + 1];
         if (L.D.nz % 8 == 0)
             FLUB_TRY(launch_pdl(k_restrict8<float, float, float>, dim3(blocks_for(C.D.n() >> 2, 256, kNumSMs * 8)),
-                                dim3(256), 0, c.s, R(l), (const float *)ZP(l), (const uint8_t *)L.code, C.r,
+                                dim3(256), 0, c.s, R(l), (const float *)ZP(l), (const uint8_t *)L.code,
+                                (const uint16_t *)L.sw, C.r,
                                 (const uint8_t *)C.code, C.D, mg->sched_rscale, (const int *)C.act,
                                 (const int *)C.act_n, c.kc));
         else
@@ -527,7 +534,7 @@ static int enqueue_vcycle_mixed(flub_mg *mg, const LaunchCtx &c, float *z0, bool
         const Level &C = mg->lv[l + 1];
         FLUB_TRY(launch_pdl(k_restrict8<__half, __half, __half>, dim3(blocks_for(C.D.n() >> 2, 256, kNumSMs * 8)),
                             dim3(256), 0, c.s, (const __half *)L.rh, (const __half *)L.z2h, (const uint8_t *)L.code,
-                            C.rh, (const uint8_t *)C.code, C.D, 0.125f * mg->sched_rscale, (const int *)C.act,
+                            (const uint16_t *)L.sw, C.rh, (const uint8_t *)C.code, C.D, 0.125f * mg->sched_rscale, (const int *)C.act,
                             (const int *)C.act_n, c.kc));
     }
     if (lt < Lm) {
@@ -596,7 +603,8 @@ static int enqueue_prologue_mixed(flub_mg *mg, const LaunchCtx &c, int smoother)
     FLUB_TRY(launch_pdl(k8_dot_rr0, dim3(bg), dim3(kRedThreads), 0, c.s, mg->st, L0.r, L0.code, mg->n, mg->partials,
                         (const int *)L0.act, (const int *)L0.act_n, c.kc));
     FLUB_TRY(launch_pdl(k8_residual_x0, dim3(blocks_for(mg->n / 8, 256, kNumSMs * 8)), dim3(256), 0, c.s, mg->st,
-                        L0.r, (const float *)mg->x, (const uint8_t *)L0.code, L0.D, (const int *)L0.act,
+                        L0.r, (const float *)mg->x, (const uint8_t *)L0.code, (const uint16_t *)L0.sw, L0.D,
+                        (const int *)L0.act,
                         (const int *)L0.act_n, c.kc));
     if (smoother == FLUB_SMOOTHER_FRACTION) FLUB_TRY(enqueue_mean_removal(mg, c, 2));
     FLUB_TRY(launch_pdl(k8_to_half, dim3(blocks_for(mg->n / 8, 256)), dim3(256), 0, c.s, mg->st, (const float *)L0.r, L0.rh,
@@ -609,8 +617,8 @@ static int enqueue_prologue_mixed(flub_mg *mg, const LaunchCtx &c, int smoother)
 static int enqueue_first_half_mixed(flub_mg *mg, const LaunchCtx &c, int smoother) {
     const Level &L0 = mg->lv[0];
     const unsigned b = red_blocks(mg->n), bg = red_blocks(mg->n / 8 + 1);
-    FLUB_TRY(launch_pdl(k8_matvec_pap, dim3(bg), dim3(kRedThreads), 0, c.s, mg->st, mg->p, mg->Ap, L0.code, L0.D,
-                        mg->partials, (const int *)L0.act, (const int *)L0.act_n, c.kc));
+    FLUB_TRY(launch_pdl(k8_matvec_pap, dim3(bg), dim3(kRedThreads), 0, c.s, mg->st, mg->p, mg->Ap, L0.code,
+                        (const uint16_t *)L0.sw, L0.D, mg->partials, (const int *)L0.act, (const int *)L0.act_n, c.kc));
     if (smoother == FLUB_SMOOTHER_FRACTION) {
         FLUB_CHECK_CUDA(cudaMemcpyAsync(mg->r_old, L0.r, sizeof(float) * mg->n, cudaMemcpyDeviceToDevice, c.s));
         FLUB_TRY(launch_pdl(k_update_r, dim3(b), dim3(kRedThreads), 0, c.s, mg->st, L0.r, mg->Ap, mg->n, c.kc));
@@ -650,7 +658,8 @@ static int enqueue_prologue(flub_mg *mg, const LaunchCtx &c, int smoother) {
         FLUB_TRY(launch_pdl(k_dot_rr0, dim3(b), dim3(kRedThreads), 0, c.s, mg->st, L0.r, mg->n, mg->partials, c.kc));
     if (v8)
         FLUB_TRY(launch_pdl(k8_residual_x0, dim3(blocks_for(mg->n / 8, 256, kNumSMs * 8)), dim3(256), 0, c.s,
-                            mg->st, L0.r, (const float *)mg->x, (const uint8_t *)L0.code, L0.D, (const int *)L0.act,
+                            mg->st, L0.r, (const float *)mg->x, (const uint8_t *)L0.code, (const uint16_t *)L0.sw, L0.D,
+                        (const int *)L0.act,
                             (const int *)L0.act_n, c.kc));
     else
         FLUB_TRY(launch_pdl(k_residual_x0, dim3(blocks_for(mg->n, 256)), dim3(256), 0, c.s, mg->st, L0.r, mg->x,
@@ -672,8 +681,8 @@ static int enqueue_first_half(flub_mg *mg, const LaunchCtx &c, int smoother) {
     const bool v8 = (L0.D.nz % 8) == 0;
     const unsigned bg = red_blocks(mg->n / 8 + 1);
     if (v8)
-        FLUB_TRY(launch_pdl(k8_matvec_pap, dim3(bg), dim3(kRedThreads), 0, c.s, mg->st, mg->p, mg->Ap, L0.code, L0.D,
-                            mg->partials, (const int *)L0.act, (const int *)L0.act_n, c.kc));
+        FLUB_TRY(launch_pdl(k8_matvec_pap, dim3(bg), dim3(kRedThreads), 0, c.s, mg->st, mg->p, mg->Ap, L0.code,
+                            (const uint16_t *)L0.sw, L0.D, mg->partials, (const int *)L0.act, (const int *)L0.act_n, c.kc));
     else
         FLUB_TRY(launch_pdl(k_matvec_pap, dim3(b), dim3(kRedThreads), 0, c.s, mg->st, mg->p, mg->Ap, L0.code, L0.D,
                             mg->partials, c.kc));
@@ -807,6 +816,17 @@ static int read_info(flub_mg *mg, cudaStream_t s, flub_solve_info *info) {
     info->tol = h.tol;
     info->x0_scale = h.x0_scale;
     return FLUB_OK;
+}
+
+// Stencil words of every group of a level (nz % 8 == 0).
+__global__ void __launch_bounds__(256) k_stencil_words(const uint8_t *__restrict__ code, uint16_t *__restrict__ sw,
+                                                       Dims D) {
+    const int ng = (int)(D.n() >> 3);
+    for (int g = blockIdx.x * blockDim.x + threadIdx.x; g < ng; g += gridDim.x * blockDim.x) {
+        int i, j, kg;
+        group_ijk(g, D, i, j, kg);
+        *reinterpret_cast<uint4 *>(sw + ((int64_t)g << 3)) = words8_from_codes(code, D, i, j, kg << 3, g << 3);
+    }
 }
 
 // ---------------------------------------------------------------- warm-start support (no reference counterpart)
@@ -1027,9 +1047,13 @@ int flub_mg_set_tags(flub_mg *mg, const int32_t *tag, void *stream) {
         k_restrict_codes<<<blocks_for(C.D.n(), 256), 256, 0, s>>>(mg->lv[l].code, C.code, C.D);
         FLUB_CHECK_LAUNCH();
     }
-    // active 8-cell groups of every level that has them
+    // stencil words and active 8-cell groups of every level that has them
     for (int l = 0; l < mg->levels; l++) {
         const Level &L = mg->lv[l];
+        if (L.sw) {
+            k_stencil_words<<<blocks_for(L.D.n() >> 3, 256), 256, 0, s>>>(L.code, L.sw, L.D);
+            FLUB_CHECK_LAUNCH();
+        }
         if (!L.act) continue;
         const int ng = (int)(L.D.n() >> 3);
         const int nb = (ng + kActPerBlock - 1) / kActPerBlock;
@@ -1171,8 +1195,8 @@ int flub_mg_set_x0_scaled(flub_mg *mg, const float *d, void *stream) {
     cudaStream_t s = as_stream(stream);
     const Level &L0 = mg->lv[0];
     if (L0.act)
-        k8_x0_gamma<<<red_blocks(mg->n / 8 + 1), kRedThreads, 0, s>>>(mg->st, d, L0.r, L0.code, L0.D, mg->partials,
-                                                                     L0.act, L0.act_n);
+        k8_x0_gamma<<<red_blocks(mg->n / 8 + 1), kRedThreads, 0, s>>>(mg->st, d, L0.r, L0.code, L0.sw, L0.D,
+                                                                     mg->partials, L0.act, L0.act_n);
     else
         k_x0_gamma<<<red_blocks(mg->n), kRedThreads, 0, s>>>(mg->st, d, L0.r, L0.code, L0.D, mg->partials);
     FLUB_CHECK_LAUNCH();

@@ -12,32 +12,27 @@
 
 namespace flub {
 
-// (r + L z) on the 8 cells of fine group g (L z is 0 at non-fluid cells).
+// (r + L z) on the 8 cells of fine group g (L z is 0 at non-fluid cells),
+// neighbour codes from the stencil words (sw, or the codes when sw is NULL).
 template <typename TR, typename TZ>
 __device__ __forceinline__ void residual_row8(const TR *__restrict__ r, const TZ *__restrict__ z,
-                                              const uint8_t *__restrict__ code, const Dims D, int g, float out[8]) {
+                                              const uint8_t *__restrict__ code, const uint16_t *__restrict__ sw,
+                                              const Dims D, int g, float out[8]) {
     int i, j, kg;
     group_ijk(g, D, i, j, kg);
     const int k0 = kg << 3;
     const int sj = D.nz, si = D.ny * D.nz;
     const int c0 = g << 3;
-    const uint2 cc = load_codes8(code + c0);
     float rv[8];
     St<TR>::ld8_ro(r + c0, rv);
-    if (!group_has_fluid(cc)) {
+    const uint4 wd = load_words8(sw, code, D, i, j, k0, c0);
+    if (!words_have_fluid(wd)) {
 #pragma unroll
         for (int m = 0; m < 8; m++) out[m] = __fadd_rn(rv[m], 0.0f);
         return;
     }
     const bool hip = i + 1 < D.nx, him = i > 0, hjp = j + 1 < D.ny, hjm = j > 0;
     const bool hkp = k0 + 8 < D.nz, hkm = k0 > 0;
-    const uint2 z2 = make_uint2(0u, 0u);
-    const uint2 cip = hip ? load_codes8(code + c0 + si) : z2;
-    const uint2 cim = him ? load_codes8(code + c0 - si) : z2;
-    const uint2 cjp = hjp ? load_codes8(code + c0 + sj) : z2;
-    const uint2 cjm = hjm ? load_codes8(code + c0 - sj) : z2;
-    const uint8_t ckm = hkm ? __ldg(code + c0 - 1) : (uint8_t)0;
-    const uint8_t ckp = hkp ? __ldg(code + c0 + 8) : (uint8_t)0;
     float xc[8], xip[8], xim[8], xjp[8], xjm[8];
     St<TZ>::ld8_ro(z + c0, xc);
 #pragma unroll
@@ -51,23 +46,22 @@ __device__ __forceinline__ void residual_row8(const TR *__restrict__ r, const TZ
 #pragma unroll
     for (int m = 0; m < 8; m++) {
         float lz = 0.0f;
-        if (code_at(cc, m) == kCodeFluid) {
+        const uint32_t w = word_at(wd, m);
+        if (sw_code(w, 0) == kCodeFluid) {
             const float c = xc[m];
             float tp, tm;
-            uint8_t cn;
+            uint32_t cn;
             tp = 0.0f; tm = 0.0f;
-            cn = code_at(cip, m); if (cn != kCodeSolid) tp = __fsub_rn(cn == kCodeAir ? 0.0f : xip[m], c);
-            cn = code_at(cim, m); if (cn != kCodeSolid) tm = __fsub_rn(cn == kCodeAir ? 0.0f : xim[m], c);
+            cn = sw_code(w, 1); if (cn != kCodeSolid) tp = __fsub_rn(cn == kCodeAir ? 0.0f : xip[m], c);
+            cn = sw_code(w, 2); if (cn != kCodeSolid) tm = __fsub_rn(cn == kCodeAir ? 0.0f : xim[m], c);
             lz = __fadd_rn(lz, __fadd_rn(tp, tm));
             tp = 0.0f; tm = 0.0f;
-            cn = code_at(cjp, m); if (cn != kCodeSolid) tp = __fsub_rn(cn == kCodeAir ? 0.0f : xjp[m], c);
-            cn = code_at(cjm, m); if (cn != kCodeSolid) tm = __fsub_rn(cn == kCodeAir ? 0.0f : xjm[m], c);
+            cn = sw_code(w, 3); if (cn != kCodeSolid) tp = __fsub_rn(cn == kCodeAir ? 0.0f : xjp[m], c);
+            cn = sw_code(w, 4); if (cn != kCodeSolid) tm = __fsub_rn(cn == kCodeAir ? 0.0f : xjm[m], c);
             lz = __fadd_rn(lz, __fadd_rn(tp, tm));
             tp = 0.0f; tm = 0.0f;
-            cn = m < 7 ? code_at(cc, m + 1) : ckp;
-            if (cn != kCodeSolid) tp = __fsub_rn(cn == kCodeAir ? 0.0f : (m < 7 ? xc[m + 1] : xkp), c);
-            cn = m > 0 ? code_at(cc, m - 1) : ckm;
-            if (cn != kCodeSolid) tm = __fsub_rn(cn == kCodeAir ? 0.0f : (m > 0 ? xc[m - 1] : xkm), c);
+            cn = sw_code(w, 5); if (cn != kCodeSolid) tp = __fsub_rn(cn == kCodeAir ? 0.0f : (m < 7 ? xc[m + 1] : xkp), c);
+            cn = sw_code(w, 6); if (cn != kCodeSolid) tm = __fsub_rn(cn == kCodeAir ? 0.0f : (m > 0 ? xc[m - 1] : xkm), c);
             lz = __fadd_rn(lz, __fadd_rn(tp, tm));
         }
         out[m] = __fadd_rn(rv[m], lz);
@@ -81,7 +75,8 @@ __device__ __forceinline__ void residual_row8(const TR *__restrict__ r, const TZ
 // out_scale: restriction scale (times 1/8 between FP16 levels at 8^-l).
 template <typename TRI, typename TZI, typename TRO>
 __global__ void __launch_bounds__(256) k_restrict8(const TRI *__restrict__ rf, const TZI *__restrict__ zf,
-                                                   const uint8_t *__restrict__ cf, TRO *__restrict__ rc,
+                                                   const uint8_t *__restrict__ cf, const uint16_t *__restrict__ swf,
+                                                   TRO *__restrict__ rc,
                                                    const uint8_t *__restrict__ cc, Dims C, float out_scale,
                                                    const int *__restrict__ act, const int *__restrict__ act_n,
                                                    unsigned long long *kc) {
@@ -112,7 +107,7 @@ __global__ void __launch_bounds__(256) k_restrict8(const TRI *__restrict__ rf, c
                 for (int jj = 0; jj < 2; jj++) {
                     const int g = ((2 * I + ii) * F.ny + 2 * J + jj) * fz8 + K4;  // fine group at k = 8 K4
                     float v[8];
-                    residual_row8(rf, zf, cf, F, g, v);
+                    residual_row8(rf, zf, cf, swf, F, g, v);
 #pragma unroll
                     for (int m = 0; m < 4; m++) {
 #pragma unroll

@@ -44,6 +44,52 @@ __device__ __forceinline__ uint8_t code_at(uint2 c, int m) {
     return (uint8_t)(((m < 4 ? c.x : c.y) >> (8 * (m & 3))) & 0xffu);
 }
 
+// ---------------------------------------------------------------- stencil words
+// One 16-bit word per cell: bits 0-1 its code, then 2 bits per neighbour in
+// the order i+, i-, j+, j-, k+, k- (code 0 -- excluded -- for a neighbour
+// outside the domain).  set_tags stores them per level (Level::sw); a kernel
+// then loads the 8 words of a group with one 16-byte load instead of five rows
+// of codes.  Without stored words (sw == NULL) they are assembled from the
+// codes by the same function set_tags uses.
+__device__ __forceinline__ uint32_t sw_code(uint32_t w, int q) { return (w >> (2 * q)) & 3u; }
+
+__device__ __forceinline__ uint32_t word_at(const uint4 &u, int m) {
+    const uint32_t v = m < 2 ? u.x : (m < 4 ? u.y : (m < 6 ? u.z : u.w));
+    return (m & 1) ? (v >> 16) : (v & 0xffffu);
+}
+
+// Words of the 8 cells of the row starting at c0 = (i, j, k0), from the codes.
+__device__ __forceinline__ uint4 words8_from_codes(const uint8_t *__restrict__ code, const Dims D, int i, int j,
+                                                   int k0, int c0) {
+    const int sj = D.nz, si = D.ny * D.nz;
+    const uint2 z2 = make_uint2(0u, 0u);
+    const uint2 cc = load_codes8(code + c0);
+    const uint2 cip = i + 1 < D.nx ? load_codes8(code + c0 + si) : z2;
+    const uint2 cim = i > 0 ? load_codes8(code + c0 - si) : z2;
+    const uint2 cjp = j + 1 < D.ny ? load_codes8(code + c0 + sj) : z2;
+    const uint2 cjm = j > 0 ? load_codes8(code + c0 - sj) : z2;
+    const uint32_t ckm = k0 > 0 ? __ldg(code + c0 - 1) : 0u;
+    const uint32_t ckp = k0 + 8 < D.nz ? __ldg(code + c0 + 8) : 0u;
+    uint32_t w[8];
+#pragma unroll
+    for (int m = 0; m < 8; m++)
+        w[m] = (uint32_t)code_at(cc, m) | ((uint32_t)code_at(cip, m) << 2) | ((uint32_t)code_at(cim, m) << 4) |
+               ((uint32_t)code_at(cjp, m) << 6) | ((uint32_t)code_at(cjm, m) << 8) |
+               ((m < 7 ? (uint32_t)code_at(cc, m + 1) : ckp) << 10) |
+               ((m > 0 ? (uint32_t)code_at(cc, m - 1) : ckm) << 12);
+    return make_uint4(w[0] | (w[1] << 16), w[2] | (w[3] << 16), w[4] | (w[5] << 16), w[6] | (w[7] << 16));
+}
+
+__device__ __forceinline__ uint4 load_words8(const uint16_t *__restrict__ sw, const uint8_t *__restrict__ code,
+                                             const Dims D, int i, int j, int k0, int c0) {
+    return sw ? __ldg(reinterpret_cast<const uint4 *>(sw + c0)) : words8_from_codes(code, D, i, j, k0, c0);
+}
+
+__device__ __forceinline__ bool words_have_fluid(const uint4 &u) {
+    // a centre code of 2 in any of the 8 words (bit 1 of each 16-bit half)
+    return (((u.x | u.y | u.z | u.w) & 0x00020002u) != 0u);
+}
+
 // z_eff[m] += scale * zc[parent] for the 8 cells of a row whose coarse row
 // starts at pc (4 coarse values: cell m has parent m / 2).  scale is 1 for FP32
 // levels and 8 between FP16 levels stored at 8^-l (exact powers of two).
@@ -78,7 +124,8 @@ __device__ __forceinline__ float coarse_at(const TC *__restrict__ p, float scale
 template <bool kFromZero, bool kProlong, typename TO, typename TI, typename TR, typename TC>
 __global__ void __launch_bounds__(256, 3) k_smooth8(TO *zout, const TI *zin, const TC *__restrict__ zc,
                                                     float zc_scale, const TR *__restrict__ r,
-                                                    const uint8_t *__restrict__ code, Dims D, int phase,
+                                                    const uint8_t *__restrict__ code,
+                                                    const uint16_t *__restrict__ sw, Dims D, int phase,
                                                     const int *__restrict__ act, const int *__restrict__ act_n,
                                                     unsigned long long *kc) {
     count_kernel(kc);
@@ -94,14 +141,8 @@ __global__ void __launch_bounds__(256, 3) k_smooth8(TO *zout, const TI *zin, con
     const int par = 1 - phase;
     const int b0 = (i + j + k0 + par) & 1;  // cell m is updated iff (m & 1) == b0
 
-    // cell codes: centre row, +-i rows, +-j rows, and the two k neighbours
-    const uint2 cc = load_codes8(code + c0);
-    const uint2 cip = hip ? load_codes8(code + c0 + si) : make_uint2(0u, 0u);
-    const uint2 cim = him ? load_codes8(code + c0 - si) : make_uint2(0u, 0u);
-    const uint2 cjp = hjp ? load_codes8(code + c0 + sj) : make_uint2(0u, 0u);
-    const uint2 cjm = hjm ? load_codes8(code + c0 - sj) : make_uint2(0u, 0u);
-    const uint8_t ckm = hkm ? __ldg(code + c0 - 1) : (uint8_t)0;
-    const uint8_t ckp = hkp ? __ldg(code + c0 + 8) : (uint8_t)0;
+    // stencil words of the 8 cells (codes of each cell and its 6 neighbours)
+    const uint4 wd = load_words8(sw, code, D, i, j, k0, c0);
 
     Row8 rr;
     St<TR>::ld8_ro(r + c0, rr.v);
@@ -134,7 +175,8 @@ __global__ void __launch_bounds__(256, 3) k_smooth8(TO *zout, const TI *zin, con
     float out[8];
 #pragma unroll
     for (int m = 0; m < 8; m++) {
-        const uint8_t cm = code_at(cc, m);
+        const uint32_t w = word_at(wd, m);
+        const uint32_t cm = sw_code(w, 0);
         out[m] = cm == kCodeFluid ? zc0.v[m] : 0.0f;
         if ((m & 1) != b0) continue;
         float zn = 0.0f;
@@ -142,22 +184,22 @@ __global__ void __launch_bounds__(256, 3) k_smooth8(TO *zout, const TI *zin, con
             const float xc = zc0.v[m];
             int d = 0;
             float tp, tm, ret = 0.0f;
-            uint8_t cn;
+            uint32_t cn;
             // axis i
             tp = 0.0f; tm = 0.0f;
-            cn = code_at(cip, m); if (cn != kCodeSolid) { tp = __fsub_rn(cn == kCodeAir ? 0.0f : zip.v[m], xc); d++; }
-            cn = code_at(cim, m); if (cn != kCodeSolid) { tm = __fsub_rn(cn == kCodeAir ? 0.0f : zim.v[m], xc); d++; }
+            cn = sw_code(w, 1); if (cn != kCodeSolid) { tp = __fsub_rn(cn == kCodeAir ? 0.0f : zip.v[m], xc); d++; }
+            cn = sw_code(w, 2); if (cn != kCodeSolid) { tm = __fsub_rn(cn == kCodeAir ? 0.0f : zim.v[m], xc); d++; }
             ret = __fadd_rn(ret, __fadd_rn(tp, tm));
             // axis j
             tp = 0.0f; tm = 0.0f;
-            cn = code_at(cjp, m); if (cn != kCodeSolid) { tp = __fsub_rn(cn == kCodeAir ? 0.0f : zjp.v[m], xc); d++; }
-            cn = code_at(cjm, m); if (cn != kCodeSolid) { tm = __fsub_rn(cn == kCodeAir ? 0.0f : zjm.v[m], xc); d++; }
+            cn = sw_code(w, 3); if (cn != kCodeSolid) { tp = __fsub_rn(cn == kCodeAir ? 0.0f : zjp.v[m], xc); d++; }
+            cn = sw_code(w, 4); if (cn != kCodeSolid) { tm = __fsub_rn(cn == kCodeAir ? 0.0f : zjm.v[m], xc); d++; }
             ret = __fadd_rn(ret, __fadd_rn(tp, tm));
             // axis k
             tp = 0.0f; tm = 0.0f;
-            cn = m < 7 ? code_at(cc, m + 1) : ckp;
+            cn = sw_code(w, 5);
             if (cn != kCodeSolid) { tp = __fsub_rn(cn == kCodeAir ? 0.0f : (m < 7 ? zc0.v[m + 1] : zkp), xc); d++; }
-            cn = m > 0 ? code_at(cc, m - 1) : ckm;
+            cn = sw_code(w, 6);
             if (cn != kCodeSolid) { tm = __fsub_rn(cn == kCodeAir ? 0.0f : (m > 0 ? zc0.v[m - 1] : zkm), xc); d++; }
             ret = __fadd_rn(ret, __fadd_rn(tp, tm));
             if (d != 0) {

@@ -175,6 +175,56 @@ def subtract_gradient(vel, vel_rigid, p, tag, d=None, p_scale=1.0):
                   pp, tp, *shape, int(d), _stream())
 
 
+# ------------------------------------------------------------------ velocity extrapolation
+
+def _int_faces(tags, shape):
+    return [_ptr(_f(t), torch.int32, field_shape(shape, d + 1), "tag." + "uvw"[d])
+            for d, t in enumerate((tags.u, tags.v, tags.w))]
+
+
+def set_unknown(phi, tags):
+    """utils/util.py:423-437: face flags 1 where phi >= 0, else 0 (face
+    index (i, j, k) < the cell grid; the last face layer keeps its flags)."""
+    phi = _f(phi)
+    shape = tuple(phi.shape)
+    _lib.call("flub_set_unknown", _ptr(phi, torch.float32, shape, "phi"), *_int_faces(tags, shape), *shape, _stream())
+
+
+def extrapolate_axis(vel, tags, d):
+    """extrapolate.py:8-30 extrapolate_3d on axis d (flags of extrapolated
+    faces become -1, as in the reference)."""
+    q = _f((vel.u, vel.v, vel.w)[d - 1])
+    t = _f((tags.u, tags.v, tags.w)[d - 1])
+    fs = tuple(q.shape)
+    shape = (fs[0] - (d == 1), fs[1] - (d == 2), fs[2] - (d == 3))
+    _lib.call("flub_extrapolate_axis", _ptr(q, torch.float32, fs, "q"), _ptr(t, torch.int32, fs, "unknown"), *shape,
+              int(d), _stream())
+
+
+def flush_unknown(tag):
+    """extrapolate.py:32-36 flush_1_3d: flags -1 -> 1."""
+    t = _f(tag)
+    _lib.call("flub_flush_unknown", _ptr(t, torch.int32, name="tag"), t.numel(), _stream())
+
+
+def extrapolate_by_1(vel, tags):
+    """extrapolate.py:39-47: one pass on the three axes, then the flush."""
+    for d in (1, 2, 3):
+        extrapolate_axis(vel, tags, d)
+    for t in (tags.u, tags.v, tags.w):
+        flush_unknown(t)
+
+
+def extrapolate(vel, tags, phi, n_cells):
+    """water_3d.py:70-73 extrapolate: set_unknown, then n_cells passes of
+    extrapolate_by_1, as one sequence of fused passes (one kernel per axis per
+    pass; the flush is implied, see flub_extrapolate)."""
+    phi = _f(phi)
+    shape = tuple(phi.shape)
+    _lib.call("flub_extrapolate", *_faces(vel, shape), *_int_faces(tags, shape), _ptr(phi, torch.float32, shape, "phi"),
+              *shape, int(n_cells), _stream())
+
+
 # ------------------------------------------------------------------ wp.launch mirror
 
 class Kernel:
@@ -223,6 +273,11 @@ subtract_gradient_tag = Kernel("subtract_gradient_tag",
 _tag_dirichlet = Kernel("_tag_dirichlet", tag_dirichlet, _dim_of(1))
 _tag_neumann = Kernel("_tag_neumann", tag_neumann, _dim_of(1))
 precompute_grid_point_phi_prims = Kernel("precompute_grid_point_phi_prims", _phi_prims_launch, _dim_of(0))
+# the reference passes the MACGrid and MACGridInt and the axis: wp.launch(extrapolate_3d, dim=shapeu, inputs=[vel, tag, 1])
+extrapolate_3d = Kernel("extrapolate_3d", lambda vel, tags, d: extrapolate_axis(vel, tags, int(d)),
+                        lambda inputs: tuple(_f((inputs[0].u, inputs[0].v, inputs[0].w)[int(inputs[2]) - 1]).shape))
+flush_1_3d = Kernel("flush_1_3d", flush_unknown, _dim_of(0))
+set_unknown_3d = Kernel("set_unknown", set_unknown, _dim_of(0))
 
 
 def launch(kernel, dim, inputs, device=None, stream=None):

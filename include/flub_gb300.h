@@ -113,6 +113,32 @@ int flub_subtract_gradient(float *u, float *v, float *w, const float *ur, const 
                            const float *p, float p_scale, const int32_t *tag, int nx, int ny, int nz,
                            void *stream);
 
+/* ---------------------------------------------------------------- velocity extrapolation */
+
+/* utils/util.py:423-437 set_unknown over the cell grid: the face flag arrays
+ * tu (nx+1, ny, nz), tv (nx, ny+1, nz), tw (nx, ny, nz+1) get 1 where
+ * phi >= 0 and 0 where phi < 0 at face index (i, j, k), i < nx, j < ny,
+ * k < nz (the last face layer of each array keeps its flags, as in the
+ * reference). */
+int flub_set_unknown(const float *phi, int32_t *tu, int32_t *tv, int32_t *tw, int nx, int ny, int nz, void *stream);
+
+/* extrapolate.py:8-30 extrapolate_3d on axis d of the face array q with flags
+ * unk (same shape): every face with flag 1 takes the mean of its in-bounds
+ * 3x3x3 neighbours with flag 0, summed in (ii, jj, kk) order, and its flag
+ * becomes -1; with no such neighbour the face becomes 0. */
+int flub_extrapolate_axis(float *q, int32_t *unk, int nx, int ny, int nz, int d, void *stream);
+
+/* extrapolate.py:32-36 flush_1_3d: flags -1 -> 1 over n entries. */
+int flub_flush_unknown(int32_t *unk, int64_t n, void *stream);
+
+/* water_3d.py:70-73 extrapolate: set_unknown (skipped when phi is NULL), then
+ * n_passes of extrapolate_by_1 (extrapolate.py:39-47) on the three axes.  Each
+ * pass leaves the flags as the reference's flush does (extrapolated faces
+ * back to 1), so the faces extrapolated and their values are the reference's
+ * pass for pass. */
+int flub_extrapolate(float *u, float *v, float *w, int32_t *tu, int32_t *tv, int32_t *tw, const float *phi, int nx,
+                     int ny, int nz, int n_passes, void *stream);
+
 /* ---------------------------------------------------------------- MGPCG */
 
 /* multigrid/mgpcg.py:234-490 class MGPCG.  One handle = one level hierarchy

@@ -71,6 +71,9 @@ def _declare(L):
     L.oracle_num_threads.restype = i32
     L.oracle_set_schedule.argtypes = [i32, i32, f64]
     L.oracle_set_schedule.restype = None
+    L.oracle_set_unknown.argtypes = [vp, vp, vp, vp, i32, i32, i32]
+    L.oracle_extrapolate_axis.argtypes = [vp, vp, i32, i32, i32]
+    L.oracle_flush_unknown.argtypes = [vp, i64]
 
 
 REFERENCE_SCHEDULE = (-1, 3, 1.0)
@@ -174,6 +177,38 @@ def subtract_gradient(uf, urf, p, tag, d):
     lib().oracle_subtract_gradient(_ptr(uf), _ptr(_c(urf, np.float32)), _ptr(_c(p, np.float32)),
                                    _ptr(_c(tag, np.int32)), nx, ny, nz, d)
     return uf
+
+
+# ---------------------------------------------------------------- velocity extrapolation
+
+def set_unknown(phi, tu, tv, tw):
+    """utils/util.py:423-437 set_unknown (in place on the three int32 flag arrays)."""
+    nx, ny, nz = phi.shape
+    for t in (tu, tv, tw):
+        assert t.dtype == np.int32 and t.flags.c_contiguous
+    lib().oracle_set_unknown(_ptr(_c(phi, np.float32)), _ptr(tu), _ptr(tv), _ptr(tw), nx, ny, nz)
+
+
+def extrapolate_axis(q, unk):
+    """extrapolate.py:8-30 extrapolate_3d on one face array (in place)."""
+    assert q.dtype == np.float32 and q.flags.c_contiguous and unk.dtype == np.int32 and unk.flags.c_contiguous
+    lib().oracle_extrapolate_axis(_ptr(q), _ptr(unk), *q.shape)
+
+
+def flush_unknown(unk):
+    """extrapolate.py:32-36 flush_1_3d (in place)."""
+    lib().oracle_flush_unknown(_ptr(unk), unk.size)
+
+
+def extrapolate(u, v, w, tu, tv, tw, phi, n_cells):
+    """water_3d.py:70-73 extrapolate: set_unknown, then n_cells times
+    extrapolate_by_1 (extrapolate.py:39-47), all in place."""
+    set_unknown(phi, tu, tv, tw)
+    for _ in range(n_cells):
+        for q, t in ((u, tu), (v, tv), (w, tw)):
+            extrapolate_axis(q, t)
+        for t in (tu, tv, tw):
+            flush_unknown(t)
 
 
 # ---------------------------------------------------------------- multigrid

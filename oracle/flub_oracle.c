@@ -209,6 +209,67 @@ void oracle_subtract_gradient(float *uf, const float *urf, const float *p, const
             }
 }
 
+/* ---------------- velocity extrapolation ---------------- */
+
+/* utils/util.py:423-437 set_unknown, launched over the cell grid (nx, ny, nz):
+ * the face flag arrays tu (nx+1, ny, nz), tv (nx, ny+1, nz), tw (nx, ny, nz+1)
+ * get 1 (unknown) where phi >= 0 and 0 (known) where phi < 0, at face index
+ * (i, j, k) with i < nx, j < ny, k < nz; the last face layer of each array
+ * keeps its previous flags. */
+void oracle_set_unknown(const float *phi, int32_t *tu, int32_t *tv, int32_t *tw, int nx, int ny, int nz) {
+#pragma omp parallel for schedule(static)
+    for (int i = 0; i < nx; i++)
+        for (int j = 0; j < ny; j++)
+            for (int k = 0; k < nz; k++) {
+                int32_t v = phi[IX(i, j, k)] >= 0.0f ? 1 : 0;
+                tu[((int64_t)i * ny + j) * nz + k] = v;
+                tv[((int64_t)i * (ny + 1) + j) * nz + k] = v;
+                tw[((int64_t)i * ny + j) * (nz + 1) + k] = v;
+            }
+}
+
+/* extrapolate.py:8-30 extrapolate_3d on one face array q of shape (fx, fy, fz)
+ * with flags unk: every face with flag 1 takes the mean of its in-bounds
+ * neighbours (the 3x3x3 block, itself included) whose flag is 0, summed in
+ * (ii, jj, kk) order from -1 to 1, kk fastest, and its flag becomes -1; with
+ * no such neighbour the face becomes 0.  Only faces with flag 0 are read and
+ * only faces with flag 1 are written, so the result does not depend on the
+ * order the faces are visited in. */
+void oracle_extrapolate_axis(float *q, int32_t *unk, int fx, int fy, int fz) {
+#pragma omp parallel for schedule(static)
+    for (int i = 0; i < fx; i++)
+        for (int j = 0; j < fy; j++)
+            for (int k = 0; k < fz; k++) {
+                int64_t f = ((int64_t)i * fy + j) * fz + k;
+                if (unk[f] != 1) continue;
+                int n = 0;
+                float s = 0.0f;
+                for (int ii = -1; ii <= 1; ii++)
+                    for (int jj = -1; jj <= 1; jj++)
+                        for (int kk = -1; kk <= 1; kk++) {
+                            int a = i + ii, b = j + jj, c = k + kk;
+                            if (a < 0 || a >= fx || b < 0 || b >= fy || c < 0 || c >= fz) continue;
+                            int64_t g = ((int64_t)a * fy + b) * fz + c;
+                            if (unk[g] != 0) continue;
+                            n++;
+                            s = s + q[g];
+                        }
+                if (n > 0) {
+                    q[f] = s / (float)n;
+                    unk[f] = -1;
+                } else {
+                    q[f] = 0.0f;
+                }
+            }
+}
+
+/* extrapolate.py:32-36 flush_1_3d: flag -1 -> 1. */
+void oracle_flush_unknown(int32_t *unk, int64_t n) {
+#pragma omp parallel for schedule(static)
+    for (int64_t c = 0; c < n; c++)
+        if (unk[c] == -1) unk[c] = 1;
+}
+
 /* multigrid/mgpcg.py:360-370 set_tags: coarse tag levels (restrict_tag). */
 void oracle_tag_levels(int32_t **tagl, int levels, int nx, int ny, int nz) {
     for (int l = 0; l + 1 < levels; l++)

@@ -294,3 +294,49 @@ def test_max_iters_zero_and_one():
     assert r0["iters"] == 0 and not r0["converged"] and np.all(r0["x"] == 0)
     r1 = O.pcg(b, tags, max_iters=1)
     assert r1["iters"] == 1 and np.any(r1["x"] != 0)
+
+
+# ---------------------------------------------------------------- velocity extrapolation (extrapolate.py)
+
+def test_set_unknown_kat():
+    phi = np.array([[[-1.0, 0.0]]], np.float32)  # (1, 1, 2): fluid, surface
+    tu = np.full((2, 1, 2), 7, np.int32)
+    tv = np.full((1, 2, 2), 7, np.int32)
+    tw = np.full((1, 1, 3), 7, np.int32)
+    O.set_unknown(phi, tu, tv, tw)
+    assert tu[0].tolist() == [[0, 1]] and tu[1].tolist() == [[7, 7]]       # last layer untouched
+    assert tv[0, 0].tolist() == [0, 1] and tv[0, 1].tolist() == [7, 7]
+    assert tw[0, 0].tolist() == [0, 1, 7]
+
+
+def test_extrapolate_axis_kat():
+    q = np.zeros((3, 3, 3), np.float32)
+    t = np.ones((3, 3, 3), np.int32)
+    t[0, 0, 0], q[0, 0, 0] = 0, 6.0
+    t[2, 2, 2], q[2, 2, 2] = 0, 3.0
+    O.extrapolate_axis(q, t)
+    assert q[1, 1, 1] == 4.5 and t[1, 1, 1] == -1          # both known corners
+    assert q[0, 0, 1] == 6.0 and q[1, 2, 2] == 3.0
+    assert q[0, 2, 0] == 0.0 and t[0, 2, 0] == 1            # no known neighbour: zeroed, still unknown
+    assert q[0, 0, 0] == 6.0 and t[0, 0, 0] == 0            # known faces untouched
+    O.flush_unknown(t)
+    assert set(np.unique(t)) <= {0, 1}
+
+
+def test_extrapolation_passes_repeat_the_first():
+    """flush_1_3d turns -1 back into 1, so the known set never grows and every
+    pass recomputes the first one (the reference's behaviour, reproduced)."""
+    rng = np.random.default_rng(3)
+    phi = rng.standard_normal((6, 5, 4)).astype(np.float32)
+    faces = [rng.standard_normal(s).astype(np.float32) for s in ((7, 5, 4), (6, 6, 4), (6, 5, 5))]
+    flags = [np.zeros(f.shape, np.int32) for f in faces]
+    one = [f.copy() for f in faces]
+    t1 = [f.copy() for f in flags]
+    O.extrapolate(*one, *t1, phi, 1)
+    many = [f.copy() for f in faces]
+    t4 = [f.copy() for f in flags]
+    O.extrapolate(*many, *t4, phi, 4)
+    for a, b in zip(one, many):
+        assert np.array_equal(a, b)
+    for a, b in zip(t1, t4):
+        assert np.array_equal(a, b)
