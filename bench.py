@@ -433,6 +433,28 @@ def run_ours(args):
                 "alg_bytes_per_launch": alg_bytes, "launch_ms": launch_ms,
                 "active_group_fraction": n_active / n_groups}
 
+    # ---- velocity extrapolation after the projection (water_3d.py:70-73, the
+    # step after project()): one pass over the three face arrays, timed warm
+    from flub_gb300 import kernels as K
+    from flub_gb300.fields import IntField, MACGridInt
+    tags = MACGridInt(*(IntField(torch.zeros_like(a, dtype=torch.int32), d=d + 1)
+                        for d, a in enumerate((vel.u.f, vel.v.f, vel.w.f))))
+    K.set_unknown(phi, tags)
+    K.extrapolate(vel, tags, None, 1)
+    torch.cuda.synchronize()
+    x0e, x1e = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    x0e.record(stream)
+    for _ in range(10):
+        K.extrapolate(vel, tags, None, 1)
+    x1e.record(stream)
+    torch.cuda.synchronize()
+    ext_ms = x0e.elapsed_time(x1e) / 10
+    n_faces = sum(a.numel() for a in (vel.u.f, vel.v.f, vel.w.f))
+    extrapolation = {"ms_per_pass": ext_ms, "passes_per_step_in_reference": 16 * scene.shape[0] // 128,
+                     "faces": n_faces, "alg_bytes_per_pass": 12 * n_faces,
+                     "achieved_GBps": 12 * n_faces / (ext_ms * 1e-3) / 1e9,
+                     "note": "algorithmic bytes: read value and flag, write value, 12 B per face"}
+
     # ---- CPU baseline: the oracle on the host cores (rank 0, N = 1 only)
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu_baseline and args.cpu_baseline_steps > 0:
@@ -466,6 +488,7 @@ def run_ours(args):
                        "max_abs_div_after": div_after, "l2_flush": "inputs larger than L2 (~1.3 GB working set)",
                        "parallelism": f"replicas x{world}"},
             "roofline": roofline, "cpu_baseline": cpu, "e2e": e2e, "gpu_launches": int(launches),
+            "extrapolation": extrapolation,
             "clocks": clocks,
         }
         print(json.dumps(out), flush=True)

@@ -218,11 +218,12 @@ def extrapolate_by_1(vel, tags):
 def extrapolate(vel, tags, phi, n_cells):
     """water_3d.py:70-73 extrapolate: set_unknown, then n_cells passes of
     extrapolate_by_1, as one sequence of fused passes (one kernel per axis per
-    pass; the flush is implied, see flub_extrapolate)."""
-    phi = _f(phi)
-    shape = tuple(phi.shape)
-    _lib.call("flub_extrapolate", *_faces(vel, shape), *_int_faces(tags, shape), _ptr(phi, torch.float32, shape, "phi"),
-              *shape, int(n_cells), _stream())
+    pass; the flush is implied, see flub_extrapolate).  phi=None skips
+    set_unknown (the flags are used as they are)."""
+    u = _f(vel.u)
+    shape = (u.shape[0] - 1, u.shape[1], u.shape[2])
+    pp = _ptr(_f(phi), torch.float32, shape, "phi") if phi is not None else None
+    _lib.call("flub_extrapolate", *_faces(vel, shape), *_int_faces(tags, shape), pp, *shape, int(n_cells), _stream())
 
 
 # ------------------------------------------------------------------ wp.launch mirror
