@@ -377,7 +377,7 @@ static int sweep8(const LaunchCtx &c, const Level &L, int phase, int mode, int s
     // groups are visited; one resident wave of blocks, grid-stride
     const int *act = skip ? L.act : nullptr;
     const int *act_n = skip ? L.act_n : nullptr;
-    const dim3 blk(256), grd(blocks_for(D.n() >> 3, 256, kNumSMs * 3));  // 3 resident blocks per SM
+    const dim3 blk(256), grd(blocks_for(D.n() >> 2, 256, kNumSMs * 6));  // two lanes per group, 6 resident blocks per SM
     if (mode == kSweepFromZero)
         return launch_pdl(k_smooth8<true, false, TO, TO, TR, TC>, grd, blk, 0, c.s, zout, (const TO *)zout,
                           (const TC *)nullptr, 1.0f, r, (const uint8_t *)L.code, (const uint16_t *)L.sw, D, phase,

@@ -106,112 +106,147 @@ __device__ __forceinline__ float coarse_at(const TC *__restrict__ p, float scale
     return __fmul_rn(St<TC>::ld_ro(p), scale);
 }
 
-// One half-sweep over 8 cells per thread.
+// One half-sweep over the 8-cell groups; a pair of adjacent lanes shares a
+// group, each lane owning 4 consecutive cells (its "half") -- 4-wide vector
+// loads per row and about half the registers of one lane per group, so twice
+// as many lanes are resident to hide memory latency.  The k neighbours across
+// the middle of the group come from the partner lane by a shuffle.
 //   kFromZero: z is 0 before the sweep (first sweep of a level in the V-cycle);
 //              zin and zc are not read.
 //   kProlong:  the sweep reads zin + zc[I/2] (multigrid/mgpcg.py:113-116 fused
 //              into the first post-smoothing sweep) and writes every cell to
 //              zout != zin; otherwise zout == zin (in place).
 // TO/TI/TR/TC: storage of zout, zin, r and the coarse zc (float, or __half in
-// the mixed-precision V-cycle); arithmetic is FP32 throughout.
+// the mixed-precision V-cycle); arithmetic is FP32 throughout, cell by cell in
+// the reference's order (multigrid/mgpcg.py:72-86), so results are bit-exact.
 // Every non-fluid cell is written as 0 (its value is never read by a fluid
 // cell's update, and the reference's sweeps leave it 0 by the end of the
 // V-cycle), so a buffer that starts at 0 keeps z = 0 off the fluid.  With an
 // active list (act != NULL) the caller asserts that invariant for zout, and
 // only the groups of the list (those holding a fluid cell) are visited;
 // without one every group is.
-// Grid: one-dimensional, grid-stride over the groups.  Requires nz % 8 == 0.
+// Grid: one-dimensional; each warp walks 16 groups (32 halves) per step,
+// grid-stride, so both lanes of a pair always run the same iterations.
+// Requires nz % 8 == 0.
 template <bool kFromZero, bool kProlong, typename TO, typename TI, typename TR, typename TC>
-__global__ void __launch_bounds__(256, 3) k_smooth8(TO *zout, const TI *zin, const TC *__restrict__ zc,
+__global__ void __launch_bounds__(256, 6) k_smooth8(TO *zout, const TI *zin, const TC *__restrict__ zc,
                                                     float zc_scale, const TR *__restrict__ r,
                                                     const uint8_t *__restrict__ code,
                                                     const uint16_t *__restrict__ sw, Dims D, int phase,
                                                     const int *__restrict__ act, const int *__restrict__ act_n,
                                                     unsigned long long *kc) {
     count_kernel(kc);
-    const int ng = (int)(D.n() >> 3);
-    FLUB_ACT_LOOP(g, act, act_n, ng) {
-    int i, j, kg;
-    group_ijk(g, D, i, j, kg);
-    const int k0 = kg << 3;
-    const int sj = D.nz, si = D.ny * D.nz;
-    const int c0 = (i * D.ny + j) * D.nz + k0;
-    const bool hip = i + 1 < D.nx, him = i > 0, hjp = j + 1 < D.ny, hjm = j > 0;
-    const bool hkp = k0 + 8 < D.nz, hkm = k0 > 0;
-    const int par = 1 - phase;
-    const int b0 = (i + j + k0 + par) & 1;  // cell m is updated iff (m & 1) == b0
+    const int lane = threadIdx.x & 31;
+    const int total = 2 * (act ? *act_n : (int)(D.n() >> 3));
+    const int stride = gridDim.x * blockDim.x;
+    for (int base = blockIdx.x * blockDim.x + (threadIdx.x & ~31); base < total; base += stride) {
+        const int t = base + lane;
+        const bool valid = t < total;  // both lanes of a pair agree (total is even)
+        const int h = t & 1;           // half: cells 4h .. 4h + 3 of the group
+        const int g = valid ? (act ? __ldg(act + (t >> 1)) : (t >> 1)) : 0;
+        int i, j, kg;
+        group_ijk(g, D, i, j, kg);
+        const int k0 = kg << 3;
+        const int sj = D.nz, si = D.ny * D.nz;
+        const int c0 = (i * D.ny + j) * D.nz + k0;
+        const int ch = c0 + 4 * h;
+        const bool hip = i + 1 < D.nx, him = i > 0, hjp = j + 1 < D.ny, hjm = j > 0;
+        const bool hkp = k0 + 8 < D.nz, hkm = k0 > 0;
+        const int par = 1 - phase;
+        const int b0 = (i + j + k0 + par) & 1;  // cell m of the group is updated iff (m & 1) == b0
 
-    // stencil words of the 8 cells (codes of each cell and its 6 neighbours)
-    const uint4 wd = load_words8(sw, code, D, i, j, k0, c0);
-
-    Row8 rr;
-    St<TR>::ld8_ro(r + c0, rr.v);
-    Row8 zc0, zip, zim, zjp, zjm;
-    float zkm = 0.0f, zkp = 0.0f;
-    if (kFromZero) {
-        zero_row8(zc0);
-    } else {
-        St<TI>::ld8(zin + c0, zc0.v);
-        if (hip) St<TI>::ld8(zin + c0 + si, zip.v); else zero_row8(zip);
-        if (him) St<TI>::ld8(zin + c0 - si, zim.v); else zero_row8(zim);
-        if (hjp) St<TI>::ld8(zin + c0 + sj, zjp.v); else zero_row8(zjp);
-        if (hjm) St<TI>::ld8(zin + c0 - sj, zjm.v); else zero_row8(zjm);
-        if (hkm) zkm = St<TI>::ld(zin + c0 - 1);
-        if (hkp) zkp = St<TI>::ld(zin + c0 + 8);
-        if (kProlong) {
-            const int cy = D.ny >> 1, cz = D.nz >> 1;
-            const int ci = i >> 1, cj = j >> 1, ck = k0 >> 1;
-            const int cb = (ci * cy + cj) * cz + ck;
-            add_coarse_row8(zc0, zc + cb, zc_scale);
-            if (hip) add_coarse_row8(zip, zc + (((i + 1) >> 1) * cy + cj) * cz + ck, zc_scale);
-            if (him) add_coarse_row8(zim, zc + (((i - 1) >> 1) * cy + cj) * cz + ck, zc_scale);
-            if (hjp) add_coarse_row8(zjp, zc + (ci * cy + ((j + 1) >> 1)) * cz + ck, zc_scale);
-            if (hjm) add_coarse_row8(zjm, zc + (ci * cy + ((j - 1) >> 1)) * cz + ck, zc_scale);
-            if (hkm) zkm = __fadd_rn(zkm, coarse_at(zc + cb - 1, zc_scale));
-            if (hkp) zkp = __fadd_rn(zkp, coarse_at(zc + cb + 4, zc_scale));
-        }
+        uint2 wd = make_uint2(0u, 0u);
+        float rr[4] = {0.0f, 0.0f, 0.0f, 0.0f}, zc0[4] = {0.0f, 0.0f, 0.0f, 0.0f};
+        float zip[4] = {0.0f, 0.0f, 0.0f, 0.0f}, zim[4] = {0.0f, 0.0f, 0.0f, 0.0f};
+        float zjp[4] = {0.0f, 0.0f, 0.0f, 0.0f}, zjm[4] = {0.0f, 0.0f, 0.0f, 0.0f};
+        float zout_k = 0.0f;  // the k neighbour outside the group (cell -1 for h = 0, cell 8 for h = 1)
+        if (valid) {
+            if (sw) {
+                wd = __ldg(reinterpret_cast<const uint2 *>(sw + ch));
+            } else {
+                const uint4 w8 = words8_from_codes(code, D, i, j, k0, c0);
+                wd = h ? make_uint2(w8.z, w8.w) : make_uint2(w8.x, w8.y);
+            }
+            St<TR>::ld4_ro(r + ch, rr);
+            if (!kFromZero) {
+                St<TI>::ld4(zin + ch, zc0);
+                if (hip) St<TI>::ld4(zin + ch + si, zip);
+                if (him) St<TI>::ld4(zin + ch - si, zim);
+                if (hjp) St<TI>::ld4(zin + ch + sj, zjp);
+                if (hjm) St<TI>::ld4(zin + ch - sj, zjm);
+                if (h == 0 && hkm) zout_k = St<TI>::ld(zin + c0 - 1);
+                if (h == 1 && hkp) zout_k = St<TI>::ld(zin + c0 + 8);
+                if (kProlong) {
+                    const int cy = D.ny >> 1, cz = D.nz >> 1;
+                    const int ci = i >> 1, cj = j >> 1, ck = (k0 >> 1) + 2 * h;
+                    const int cb = (ci * cy + cj) * cz + ck;
+                    float cv[2];
+#define FLUB_ADD_COARSE(row, p)                                                         \
+    {                                                                                   \
+        St<TC>::ld2_ro((p), cv);                                                        \
+        _Pragma("unroll") for (int mm = 0; mm < 4; mm++)                                \
+            row[mm] = __fadd_rn(row[mm], __fmul_rn(cv[mm >> 1], zc_scale));             \
     }
-
-    float out[8];
-#pragma unroll
-    for (int m = 0; m < 8; m++) {
-        const uint32_t w = word_at(wd, m);
-        const uint32_t cm = sw_code(w, 0);
-        out[m] = cm == kCodeFluid ? zc0.v[m] : 0.0f;
-        if ((m & 1) != b0) continue;
-        float zn = 0.0f;
-        if (cm == kCodeFluid) {
-            const float xc = zc0.v[m];
-            int d = 0;
-            float tp, tm, ret = 0.0f;
-            uint32_t cn;
-            // axis i
-            tp = 0.0f; tm = 0.0f;
-            cn = sw_code(w, 1); if (cn != kCodeSolid) { tp = __fsub_rn(cn == kCodeAir ? 0.0f : zip.v[m], xc); d++; }
-            cn = sw_code(w, 2); if (cn != kCodeSolid) { tm = __fsub_rn(cn == kCodeAir ? 0.0f : zim.v[m], xc); d++; }
-            ret = __fadd_rn(ret, __fadd_rn(tp, tm));
-            // axis j
-            tp = 0.0f; tm = 0.0f;
-            cn = sw_code(w, 3); if (cn != kCodeSolid) { tp = __fsub_rn(cn == kCodeAir ? 0.0f : zjp.v[m], xc); d++; }
-            cn = sw_code(w, 4); if (cn != kCodeSolid) { tm = __fsub_rn(cn == kCodeAir ? 0.0f : zjm.v[m], xc); d++; }
-            ret = __fadd_rn(ret, __fadd_rn(tp, tm));
-            // axis k
-            tp = 0.0f; tm = 0.0f;
-            cn = sw_code(w, 5);
-            if (cn != kCodeSolid) { tp = __fsub_rn(cn == kCodeAir ? 0.0f : (m < 7 ? zc0.v[m + 1] : zkp), xc); d++; }
-            cn = sw_code(w, 6);
-            if (cn != kCodeSolid) { tm = __fsub_rn(cn == kCodeAir ? 0.0f : (m > 0 ? zc0.v[m - 1] : zkm), xc); d++; }
-            ret = __fadd_rn(ret, __fadd_rn(tp, tm));
-            if (d != 0) {
-                if (kFromZero)
-                    zn = __fdiv_rn(rr.v[m], (float)d);  // 0 + (r + L 0) / d, L 0 = 0
-                else
-                    zn = __fadd_rn(xc, __fdiv_rn(__fadd_rn(rr.v[m], ret), (float)d));
+                    FLUB_ADD_COARSE(zc0, zc + cb)
+                    if (hip) FLUB_ADD_COARSE(zip, zc + (((i + 1) >> 1) * cy + cj) * cz + ck)
+                    if (him) FLUB_ADD_COARSE(zim, zc + (((i - 1) >> 1) * cy + cj) * cz + ck)
+                    if (hjp) FLUB_ADD_COARSE(zjp, zc + (ci * cy + ((j + 1) >> 1)) * cz + ck)
+                    if (hjm) FLUB_ADD_COARSE(zjm, zc + (ci * cy + ((j - 1) >> 1)) * cz + ck)
+#undef FLUB_ADD_COARSE
+                    if (h == 0 && hkm) zout_k = __fadd_rn(zout_k, coarse_at(zc + cb - 1, zc_scale));
+                    if (h == 1 && hkp) zout_k = __fadd_rn(zout_k, coarse_at(zc + cb + 2, zc_scale));
+                }
             }
         }
-        out[m] = zn;
-    }
-    St<TO>::st8(zout + c0, out);
+        // the partner's cell next to the middle of the group: h = 0 needs cell 4
+        // (partner's first), h = 1 needs cell 3 (partner's last)
+        const float send = h ? zc0[0] : zc0[3];
+        const float zmid = __shfl_xor_sync(0xffffffffu, send, 1);
+        const float zkm = h ? zmid : zout_k;  // neighbour below cell 4h
+        const float zkp = h ? zout_k : zmid;  // neighbour above cell 4h + 3
+        if (!valid) continue;
+
+        float out[4];
+#pragma unroll
+        for (int mm = 0; mm < 4; mm++) {
+            const int m = 4 * h + mm;  // cell index in the group (parity of m == parity of mm)
+            const uint32_t w = (mm & 1) ? ((mm < 2 ? wd.x : wd.y) >> 16) : ((mm < 2 ? wd.x : wd.y) & 0xffffu);
+            const uint32_t cm = sw_code(w, 0);
+            out[mm] = cm == kCodeFluid ? zc0[mm] : 0.0f;
+            if ((m & 1) != b0) continue;
+            float zn = 0.0f;
+            if (cm == kCodeFluid) {
+                const float xc = zc0[mm];
+                int d = 0;
+                float tp, tm, ret = 0.0f;
+                uint32_t cn;
+                // axis i
+                tp = 0.0f; tm = 0.0f;
+                cn = sw_code(w, 1); if (cn != kCodeSolid) { tp = __fsub_rn(cn == kCodeAir ? 0.0f : zip[mm], xc); d++; }
+                cn = sw_code(w, 2); if (cn != kCodeSolid) { tm = __fsub_rn(cn == kCodeAir ? 0.0f : zim[mm], xc); d++; }
+                ret = __fadd_rn(ret, __fadd_rn(tp, tm));
+                // axis j
+                tp = 0.0f; tm = 0.0f;
+                cn = sw_code(w, 3); if (cn != kCodeSolid) { tp = __fsub_rn(cn == kCodeAir ? 0.0f : zjp[mm], xc); d++; }
+                cn = sw_code(w, 4); if (cn != kCodeSolid) { tm = __fsub_rn(cn == kCodeAir ? 0.0f : zjm[mm], xc); d++; }
+                ret = __fadd_rn(ret, __fadd_rn(tp, tm));
+                // axis k
+                tp = 0.0f; tm = 0.0f;
+                cn = sw_code(w, 5);
+                if (cn != kCodeSolid) { tp = __fsub_rn(cn == kCodeAir ? 0.0f : (mm < 3 ? zc0[mm + 1] : zkp), xc); d++; }
+                cn = sw_code(w, 6);
+                if (cn != kCodeSolid) { tm = __fsub_rn(cn == kCodeAir ? 0.0f : (mm > 0 ? zc0[mm - 1] : zkm), xc); d++; }
+                ret = __fadd_rn(ret, __fadd_rn(tp, tm));
+                if (d != 0) {
+                    if (kFromZero)
+                        zn = __fdiv_rn(rr[mm], (float)d);  // 0 + (r + L 0) / d, L 0 = 0
+                    else
+                        zn = __fadd_rn(xc, __fdiv_rn(__fadd_rn(rr[mm], ret), (float)d));
+                }
+            }
+            out[mm] = zn;
+        }
+        St<TO>::st4(zout + ch, out);
     }
 }
 

@@ -27,6 +27,14 @@ struct St<float> {
         const float4 a = __ldg(reinterpret_cast<const float4 *>(p));
         o[0] = a.x; o[1] = a.y; o[2] = a.z; o[3] = a.w;
     }
+    static __device__ __forceinline__ void ld4(const float *p, float o[4]) {
+        const float4 a = *reinterpret_cast<const float4 *>(p);
+        o[0] = a.x; o[1] = a.y; o[2] = a.z; o[3] = a.w;
+    }
+    static __device__ __forceinline__ void ld2_ro(const float *p, float o[2]) {
+        const float2 a = __ldg(reinterpret_cast<const float2 *>(p));
+        o[0] = a.x; o[1] = a.y;
+    }
     static __device__ __forceinline__ void st8(float *p, const float v[8]) {
         reinterpret_cast<float4 *>(p)[0] = make_float4(v[0], v[1], v[2], v[3]);
         reinterpret_cast<float4 *>(p)[1] = make_float4(v[4], v[5], v[6], v[7]);
@@ -61,6 +69,16 @@ struct St<__half> {
         const __half2 *h = reinterpret_cast<const __half2 *>(&u);
         const float2 a = __half22float2(h[0]), b = __half22float2(h[1]);
         o[0] = a.x; o[1] = a.y; o[2] = b.x; o[3] = b.y;
+    }
+    static __device__ __forceinline__ void ld4(const __half *p, float o[4]) {
+        const uint2 u = *reinterpret_cast<const uint2 *>(p);
+        const __half2 *h = reinterpret_cast<const __half2 *>(&u);
+        const float2 a = __half22float2(h[0]), b = __half22float2(h[1]);
+        o[0] = a.x; o[1] = a.y; o[2] = b.x; o[3] = b.y;
+    }
+    static __device__ __forceinline__ void ld2_ro(const __half *p, float o[2]) {
+        const float2 a = __half22float2(__ldg(reinterpret_cast<const __half2 *>(p)));
+        o[0] = a.x; o[1] = a.y;
     }
     static __device__ __forceinline__ void st8(__half *p, const float v[8]) {
         uint4 u;
