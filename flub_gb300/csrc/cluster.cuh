@@ -23,6 +23,7 @@
 #include <cuda_fp16.h>
 
 #include "mg_kernels.cuh"
+#include "tail.cuh"
 
 namespace flub {
 
@@ -51,6 +52,11 @@ struct ClusterParams {
     int nu;        // red-black iterations per side at every level (< 0: 6 << level, the reference's)
     int nbottom;   // iterations of each of the two bottom orders (3 in the reference)
     float rscale;  // restriction scale (1 in the reference)
+    // Levels below the distributed ones (at most kTailMaxCells cells) run in
+    // block 0 alone, with block barriers: tail != 0, tp their layout at byte
+    // offset tail_off of block 0's shared memory.
+    int tail, tail_off;
+    TailParams tp;
 };
 
 struct ClusterCtx {
@@ -196,6 +202,65 @@ __device__ __forceinline__ void cl_restrict(const ClusterCtx &x, const ClusterPa
     x.cl.sync();
 }
 
+// cl_restrict from the last distributed level t into the first tail level,
+// whose dense r array lives in block 0's shared memory.
+__device__ __forceinline__ void cl_restrict_tail(const ClusterCtx &x, const ClusterParams &P, int t) {
+    const ClusterLevel &F = P.lv[t];
+    const TailLevel &T = P.tp.lv[0];
+    const int lg_cy = F.lg_ny - 1, lg_cz = F.lg_nz - 1;
+    if (x.rank < (unsigned)F.ncta) {
+        const float *zs = cl_z(x, F);
+        const uint8_t *cs = cl_c(x, F);
+        float *rdst = x.cl.map_shared_rank(reinterpret_cast<float *>(x.smem + P.tail_off + T.off_r), 0u);
+        const int cpl = F.P >> 1;
+        const int n = cpl << (lg_cy + lg_cz);
+        for (int q = threadIdx.x; q < n; q += blockDim.x) {
+            const int K = q & (T.D.nz - 1), J = (q >> lg_cz) & (T.D.ny - 1), Il = q >> (lg_cy + lg_cz);
+            const int gI = (int)x.rank * cpl + Il;
+            const int cq = (gI << (lg_cy + lg_cz)) + (J << lg_cz) + K;
+            float s = 0.0f;
+            if (__ldg(T.code + cq) == kCodeFluid) {
+                bool first = true;
+#pragma unroll
+                for (int ii = 0; ii < 2; ii++)
+#pragma unroll
+                    for (int jj = 0; jj < 2; jj++)
+#pragma unroll
+                        for (int kk = 0; kk < 2; kk++) {
+                            const int il = 2 * Il + ii, j = 2 * J + jj, k = 2 * K + kk;
+                            const int c = ((il + 1) << (F.lg_ny + F.lg_nz)) + (j << F.lg_nz) + k;
+                            const float v = __fadd_rn(cl_rval(x, F, P, il, j, k), cl_lap(zs, cs, c, j, k, F.D));
+                            s = first ? v : __fadd_rn(s, v);
+                            first = false;
+                        }
+            }
+            rdst[cq] = __fmul_rn(s, P.rscale);
+        }
+    }
+    x.cl.sync();
+}
+
+// cl_prolong into the last distributed level t from the first tail level's
+// dense z array in block 0's shared memory.
+__device__ __forceinline__ void cl_prolong_tail(const ClusterCtx &x, const ClusterParams &P, int t) {
+    const ClusterLevel &F = P.lv[t];
+    const TailLevel &T = P.tp.lv[0];
+    const int lg_cy = F.lg_ny - 1, lg_cz = F.lg_nz - 1;
+    if (x.rank < (unsigned)F.ncta) {
+        float *zs = cl_z(x, F);
+        const float *zc = x.cl.map_shared_rank(reinterpret_cast<float *>(x.smem + P.tail_off + T.off_z), 0u);
+        const int n = F.P << (F.lg_ny + F.lg_nz);
+        for (int q = threadIdx.x; q < n; q += blockDim.x) {
+            const int k = q & (F.D.nz - 1), j = (q >> F.lg_nz) & (F.D.ny - 1), il = q >> (F.lg_ny + F.lg_nz);
+            const int gI = ((int)x.rank * F.P + il) >> 1;
+            const float add = zc[(gI << (lg_cy + lg_cz)) + ((j >> 1) << lg_cz) + (k >> 1)];
+            const int c = ((il + 1) << (F.lg_ny + F.lg_nz)) + (j << F.lg_nz) + k;
+            cl_store(x, F, zs, il, j, k, __fadd_rn(zs[c], add));
+        }
+    }
+    x.cl.sync();
+}
+
 // z_t += z_{t+1}[I/2] (mgpcg.py:113-116), ghost planes included; then a barrier.
 __device__ __forceinline__ void cl_prolong(const ClusterCtx &x, const ClusterParams &P, int t) {
     const ClusterLevel &F = P.lv[t], &C = P.lv[t + 1];
@@ -249,6 +314,34 @@ __global__ void __launch_bounds__(kClusterThreads, 1) k_cluster_vcycle(const Clu
         }
     }
     x.cl.sync();
+    if (P.tail) {
+        // distributed levels 0 .. nl-1 down, the tail levels in block 0, then up
+        const int nd = P.nl;
+        for (int t = 0; t < nd; t++) {
+            const int iters = P.nu < 0 ? (6 << P.lv[t].abs_level) : P.nu;
+            for (int it = 0; it < iters; it++) {
+                cl_half(x, P, t, 0, it == 0);
+                cl_half(x, P, t, 1, false);
+            }
+            if (t + 1 < nd)
+                cl_restrict(x, P, t);
+            else
+                cl_restrict_tail(x, P, t);
+        }
+        if (x.rank == 0) tail_run(P.tp, x.smem + P.tail_off, false);
+        x.cl.sync();
+        for (int t = nd - 1; t >= 0; t--) {
+            if (t + 1 < nd)
+                cl_prolong(x, P, t);
+            else
+                cl_prolong_tail(x, P, t);
+            const int iters = P.nu < 0 ? (6 << P.lv[t].abs_level) : P.nu;
+            for (int it = 0; it < iters; it++) {
+                cl_half(x, P, t, 1, false);
+                cl_half(x, P, t, 0, false);
+            }
+        }
+    } else {
     const int nb = P.nl - 1;
     for (int t = 0; t < nb; t++) {
         const int iters = P.nu < 0 ? (6 << P.lv[t].abs_level) : P.nu;
@@ -273,6 +366,7 @@ __global__ void __launch_bounds__(kClusterThreads, 1) k_cluster_vcycle(const Clu
             cl_half(x, P, t, 1, false);
             cl_half(x, P, t, 0, false);
         }
+    }
     }
     const ClusterLevel &L = P.lv[0];
     if (x.rank < (unsigned)L.ncta) {

@@ -220,8 +220,19 @@ static size_t cluster_layout(const flub_mg *mg, int lc, int C, ClusterParams *P)
         off += (b + 15) & ~(size_t)15;
         return (int)o;
     };
+    P->tail = 0;
+    P->tail_off = 0;
+    // block 0 takes over the <= 16^3 levels when their schedule is long (the
+    // reference's 6 << l sweeps, hundreds of barriers); a light schedule has
+    // too few sweeps there to pay for the hand-off
+    const bool want_tail = mg->sched_nu < 0 || mg->sched_nu >= 4;
+    int lt = mg->levels;  // first level run by block 0 alone (== levels: none)
     for (int l = lc; l < mg->levels; l++) {
         const Dims D{mg->nx >> l, mg->ny >> l, mg->nz >> l};
+        if (want_tail && l > lc && D.n() <= kTailMaxCells && tail_layout(mg, l, &P->tp) > 0) {
+            lt = l;
+            break;
+        }
         if (!is_pow2(D.nx) || !is_pow2(D.ny) || !is_pow2(D.nz) || D.nx < 2 || D.nz < 2) return 0;
         ClusterLevel &L = P->lv[l - lc];
         L.D = D;
@@ -236,7 +247,13 @@ static size_t cluster_layout(const flub_mg *mg, int lc, int C, ClusterParams *P)
         L.off_c = take((L.P + 2) * plane);
         L.off_r = take(sizeof(float) * L.P * plane);
     }
-    P->nl = mg->levels - lc;
+    P->nl = lt - lc;
+    if (lt < mg->levels) {
+        // the coarsest levels in block 0: the tail layout after the distributed ones
+        const size_t tb = tail_layout(mg, lt, &P->tp);
+        P->tail = 1;
+        P->tail_off = take(tb);
+    }
     P->nu = mg->sched_nu;
     P->nbottom = mg->sched_bottom;
     P->rscale = mg->sched_rscale;
@@ -1186,6 +1203,8 @@ int flub_mg_set_schedule(flub_mg *mg, int smooth_iters, int bottom_iters, float 
     mg->sched_nu = smooth_iters;
     mg->sched_bottom = bottom_iters;
     mg->sched_rscale = restrict_scale;
+    // the cluster kernel's layout depends on the schedule
+    FLUB_TRY(choose_cluster(mg));
     return FLUB_OK;
 }
 

@@ -178,18 +178,21 @@ __device__ __forceinline__ void tail_prolong(float *zf, const float *zc, const D
     __syncthreads();
 }
 
-__global__ void __launch_bounds__(kTailThreads) k_tail_vcycle(const TailParams P, unsigned long long *kc) {
-    extern __shared__ __align__(16) unsigned char tail_smem[];
-    count_kernel(kc);
-    auto Z = [&](int t) { return reinterpret_cast<float *>(tail_smem + P.lv[t].off_z); };
-    auto R = [&](int t) { return reinterpret_cast<float *>(tail_smem + P.lv[t].off_r); };
-    auto C = [&](int t) { return reinterpret_cast<uint8_t *>(tail_smem + P.lv[t].off_c); };
+// The tail sub-V-cycle on one block with the layout P in the shared memory at
+// smem.  io: the first level's r comes from P.r_top / P.r_top_h and its z goes
+// back to P.z_top / P.z_top_h; otherwise both stay in shared memory (the
+// cluster kernel writes r there and reads z back through distributed shared
+// memory).
+__device__ __forceinline__ void tail_run(const TailParams &P, unsigned char *smem, bool io) {
+    auto Z = [&](int t) { return reinterpret_cast<float *>(smem + P.lv[t].off_z); };
+    auto R = [&](int t) { return reinterpret_cast<float *>(smem + P.lv[t].off_r); };
+    auto C = [&](int t) { return reinterpret_cast<uint8_t *>(smem + P.lv[t].off_c); };
     for (int t = 0; t < P.nt; t++) {
         const int n = P.lv[t].D.nx * P.lv[t].D.ny * P.lv[t].D.nz;
         uint8_t *c = C(t);
         for (int q = threadIdx.x; q < n; q += blockDim.x) c[q] = P.lv[t].code[q];
     }
-    {
+    if (io) {
         const Dims D = P.lv[0].D;
         const int n = D.nx * D.ny * D.nz;
         float *r = R(0);
@@ -233,7 +236,7 @@ __global__ void __launch_bounds__(kTailThreads) k_tail_vcycle(const TailParams P
             tail_half_lean(Z(t), tc, D, 0, false);
         }
     }
-    {
+    if (io) {
         const Dims D = P.lv[0].D;
         const int n = D.nx * D.ny * D.nz;
         const float *z = Z(0);
@@ -242,6 +245,12 @@ __global__ void __launch_bounds__(kTailThreads) k_tail_vcycle(const TailParams P
         else
             for (int q = threadIdx.x; q < n; q += blockDim.x) P.z_top[q] = z[q];
     }
+}
+
+__global__ void __launch_bounds__(kTailThreads) k_tail_vcycle(const TailParams P, unsigned long long *kc) {
+    extern __shared__ __align__(16) unsigned char tail_smem[];
+    count_kernel(kc);
+    tail_run(P, tail_smem, true);
 }
 
 }  // namespace flub
