@@ -344,3 +344,30 @@ def test_trained_network_saves_iterations():
         assert r["warm"] <= r["cold"], r
         assert r["err_warm"] <= 1e-5, r
         assert r["err_net"] < 0.5, r
+
+
+def test_warm_start_graph_equals_eager():
+    """The captured-graph guess is the eager guess, bit for bit, and a warm
+    solve through it converges to the same tolerance."""
+    from flub_gb300 import Projection, learned
+    from flub_gb300.unet import UNet3D
+    from flub_gb300.fields import Field, MACGrid
+    from flub_gb300 import scenes
+    dev = _dev()
+    net = UNet3D(device=dev, seed=5)
+    sc = scenes.dam(128, 2)
+    d_ = lambda a: torch.as_tensor(a).to(dev)
+    outs = {}
+    for graph in (False, True):
+        proj = Projection(sc.shape, sc.levels, precision="mixed", schedule="v22")
+        vel = MACGrid(*(Field(d_(a), d=i + 1) for i, a in enumerate((sc.u, sc.v, sc.w))))
+        velr = MACGrid(*(Field(d_(a), d=i + 1) for i, a in enumerate((sc.ur, sc.vr, sc.wr))))
+        ws = learned.WarmStart(net, graph=graph)
+        info = proj.project(vel, velr, d_(sc.phi), sc.prims, warm_start=ws)
+        # a second projection of the original velocities (a graph replay on new inputs)
+        vel = MACGrid(*(Field(d_(a), d=i + 1) for i, a in enumerate((sc.u, sc.v, sc.w))))
+        info2 = proj.project(vel, velr, d_(sc.phi), sc.prims, warm_start=ws)
+        assert info["converged"] and info2["converged"]
+        outs[graph] = (info["x0_scale"], info2["x0_scale"], proj.p.f.cpu())
+    assert outs[False][0] == outs[True][0] and outs[False][1] == outs[True][1]
+    assert torch.equal(outs[False][2], outs[True][2])
