@@ -11,10 +11,13 @@ loaded on first use; there is no CPU fallback.
 """
 from .fields import (DEFAULT_SHAPE, Field, IntField, MACGrid, MACGridInt, field_like, field_shape, get_uf,
                      make_field, make_mac_grid)
-from .kernels import (_tag_dirichlet, _tag_neumann, classify, divergence, divergence_tag, extrapolate,
-                      extrapolate_3d, extrapolate_by_1, flush_1_3d, launch, mask_with_tag, phi_prims,
-                      precompute_grid_point_phi_prims, scale_by_3d, set_unknown, set_unknown_3d, subtract_gradient,
-                      subtract_gradient_tag, tag_dirichlet, tag_neumann)
+from .kernels import (_tag_dirichlet, _tag_neumann, classify, divergence, divergence_fractional,
+                      divergence_fractional_3d, divergence_tag, extrapolate, extrapolate_3d, extrapolate_by_1,
+                      flush_1_3d, launch, mask_with_tag, phi_prims, phi_to_fraction, phi_to_fraction_3d,
+                      precompute_grid_point_phi_prims, precompute_solid_vel, scale_by_3d, set_unknown, set_unknown_3d,
+                      solid_vel, subtract_gradient, subtract_gradient_batty, subtract_gradient_tag, tag_dirichlet,
+                      tag_neumann, u_subtract_gradient_batty_3d, v_subtract_gradient_batty_3d,
+                      w_subtract_gradient_batty_3d)
 from ._lib import FlubError
 from .mgpcg import MGPCG
 from .projection import Projection
@@ -24,5 +27,8 @@ __all__ = [
     "make_field", "make_mac_grid", "_tag_dirichlet", "_tag_neumann", "classify", "divergence", "divergence_tag",
     "launch", "mask_with_tag", "phi_prims", "precompute_grid_point_phi_prims", "scale_by_3d", "subtract_gradient",
     "subtract_gradient_tag", "tag_dirichlet", "tag_neumann", "MGPCG", "Projection", "FlubError", "extrapolate",
-    "extrapolate_3d", "extrapolate_by_1", "flush_1_3d", "set_unknown", "set_unknown_3d",
+    "extrapolate_3d", "extrapolate_by_1", "flush_1_3d", "set_unknown", "set_unknown_3d", "divergence_fractional",
+    "divergence_fractional_3d", "phi_to_fraction", "phi_to_fraction_3d", "precompute_solid_vel", "solid_vel",
+    "subtract_gradient_batty", "u_subtract_gradient_batty_3d", "v_subtract_gradient_batty_3d",
+    "w_subtract_gradient_batty_3d",
 ]

@@ -53,6 +53,10 @@ SIGNATURES = {
     "flub_divergence_masked": (_i32, [_vp] * 8 + [_f32, _i32, _i32, _i32, _vp]),
     "flub_subtract_gradient_tag": (_i32, [_vp, _vp, _vp, _vp, _i32, _i32, _i32, _i32, _vp]),
     "flub_subtract_gradient": (_i32, [_vp] * 7 + [_f32, _vp, _i32, _i32, _i32, _vp]),
+    "flub_solid_vel": (_i32, [_vp, _vp, _i32, _i32, _i32, _i32, _f32, _vp, _vp, _vp, _i32, _vp]),
+    "flub_phi_to_fraction": (_i32, [_vp, _vp, _i32, _i32, _i32, _i32, _vp]),
+    "flub_divergence_fractional": (_i32, [_vp] * 10 + [_i32, _i32, _i32, _vp]),
+    "flub_subtract_gradient_batty": (_i32, [_vp] * 5 + [_i32, _i32, _i32, _i32, _f32, _f32, _vp]),
     "flub_set_unknown": (_i32, [_vp, _vp, _vp, _vp, _i32, _i32, _i32, _vp]),
     "flub_extrapolate_axis": (_i32, [_vp, _vp, _i32, _i32, _i32, _i32, _vp]),
     "flub_flush_unknown": (_i32, [_vp, _i64, _vp]),

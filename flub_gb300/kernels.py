@@ -175,6 +175,60 @@ def subtract_gradient(vel, vel_rigid, p, tag, d=None, p_scale=1.0):
                   pp, tp, *shape, int(d), _stream())
 
 
+# ------------------------------------------------------------------ rigid face velocities, cut cells
+
+def _host_vec3(a, name):
+    if isinstance(a, torch.Tensor):
+        a = a.detach().cpu().numpy()
+    a = np.ascontiguousarray(np.asarray(a, dtype=np.float32).reshape(-1, 3))
+    return a
+
+
+def solid_vel(vel_rigid, vel_owner, d, x, v, omega, h0=None):
+    """rigid_coupling.py:51-70 precompute_solid_vel for axis d: the rigid
+    velocity of each face's owner body (x, v, omega: one vec3 per body)."""
+    ur = _f((vel_rigid.u, vel_rigid.v, vel_rigid.w)[d - 1])
+    ow = _f((vel_owner.u, vel_owner.v, vel_owner.w)[d - 1])
+    fs = tuple(ur.shape)
+    shape = (fs[0] - (d == 1), fs[1] - (d == 2), fs[2] - (d == 3))
+    bx, bv, bw = (_host_vec3(a, n) for a, n in ((x, "x"), (v, "v"), (omega, "omega")))
+    hh = float(h0) if h0 is not None else 1.0 / shape[0]
+    _lib.call("flub_solid_vel", _ptr(ur, torch.float32, fs, "u_rigid"), _ptr(ow, torch.int32, fs, "owner"), *shape,
+              int(d), hh, bx.ctypes.data_as(ctypes.c_void_p), bv.ctypes.data_as(ctypes.c_void_p),
+              bw.ctypes.data_as(ctypes.c_void_p), bx.shape[0], _stream())
+
+
+def phi_to_fraction(phi_nodes, frac, d):
+    """geometry.py phi_to_fraction: face fractions of axis d in place (frac
+    holds the face-centre SDF on entry; phi_nodes: SDF at the grid nodes)."""
+    pn = _f(phi_nodes)
+    shape = tuple(s - 1 for s in pn.shape)
+    fa = _f((frac.u, frac.v, frac.w)[d - 1])
+    _lib.call("flub_phi_to_fraction", _ptr(pn, torch.float32, tuple(pn.shape), "phi"),
+              _ptr(fa, torch.float32, field_shape(shape, d), "frac"), *shape, int(d), _stream())
+
+
+def divergence_fractional(uf, vf, wf, div, fu, fv, fw, ur, vr, wr):
+    """divergence.py:4-42 divergence_fractional_3d (raw face arrays)."""
+    div = _f(div)
+    shape = tuple(div.shape)
+    faces = [(_f(a), d) for a, d in ((uf, 1), (vf, 2), (wf, 3), (fu, 1), (fv, 2), (fw, 3), (ur, 1), (vr, 2), (wr, 3))]
+    ptrs = [_ptr(a, torch.float32, field_shape(shape, d), "face array") for a, d in faces]
+    _lib.call("flub_divergence_fractional", *ptrs[:3], _ptr(div, torch.float32, shape, "div"), *ptrs[3:], *shape,
+              _stream())
+    return div
+
+
+def subtract_gradient_batty(uf, pf, frac, phi, urf, d, lo, h):
+    """subtract_gradient.py:7-122 u/v/w_subtract_gradient_batty_3d on axis d."""
+    phi, pf = _f(phi), _f(pf)
+    shape = tuple(phi.shape)
+    fs = field_shape(shape, d)
+    _lib.call("flub_subtract_gradient_batty", _ptr(_f(uf), torch.float32, fs, "uf"), _ptr(pf, torch.float32, shape, "p"),
+              _ptr(_f(frac), torch.float32, fs, "frac"), _ptr(phi, torch.float32, shape, "phi"),
+              _ptr(_f(urf), torch.float32, fs, "u_rigid"), *shape, int(d), float(lo), float(h), _stream())
+
+
 # ------------------------------------------------------------------ velocity extrapolation
 
 def _int_faces(tags, shape):
@@ -278,6 +332,27 @@ precompute_grid_point_phi_prims = Kernel("precompute_grid_point_phi_prims", _phi
 extrapolate_3d = Kernel("extrapolate_3d", lambda vel, tags, d: extrapolate_axis(vel, tags, int(d)),
                         lambda inputs: tuple(_f((inputs[0].u, inputs[0].v, inputs[0].w)[int(inputs[2]) - 1]).shape))
 flush_1_3d = Kernel("flush_1_3d", flush_unknown, _dim_of(0))
+# rigid_coupling.py precompute_solid_vel: inputs=[x, v, omega, vel_rigid, vel_owner, d]
+precompute_solid_vel = Kernel(
+    "precompute_solid_vel", lambda x, v, omega, vel_rigid, vel_owner, d: solid_vel(vel_rigid, vel_owner, int(d), x, v,
+                                                                                   omega),
+    lambda inputs: tuple(_f((inputs[3].u, inputs[3].v, inputs[3].w)[int(inputs[5]) - 1]).shape))
+# geometry.py phi_to_fraction: inputs=[phi, frac, dim]
+phi_to_fraction_3d = Kernel("phi_to_fraction", lambda phi, frac, dim: phi_to_fraction(phi, frac, int(dim)),
+                            lambda inputs: tuple(_f((inputs[1].u, inputs[1].v, inputs[1].w)[int(inputs[2]) - 1]).shape))
+divergence_fractional_3d = Kernel("divergence_fractional_3d", divergence_fractional, _dim_of(3))
+u_subtract_gradient_batty_3d = Kernel("u_subtract_gradient_batty_3d",
+                                      lambda uf, pf, fu, phi, ur, l, r, h: subtract_gradient_batty(uf, pf, fu, phi, ur,
+                                                                                                   1, l, h),
+                                      _dim_of(0))
+v_subtract_gradient_batty_3d = Kernel("v_subtract_gradient_batty_3d",
+                                      lambda vf, pf, fv, phi, vr, b, t, h: subtract_gradient_batty(vf, pf, fv, phi, vr,
+                                                                                                   2, b, h),
+                                      _dim_of(0))
+w_subtract_gradient_batty_3d = Kernel("w_subtract_gradient_batty_3d",
+                                      lambda wf, pf, fw, phi, wr, far, near, h: subtract_gradient_batty(
+                                          wf, pf, fw, phi, wr, 3, far, h),
+                                      _dim_of(0))
 set_unknown_3d = Kernel("set_unknown", set_unknown, _dim_of(0))
 
 

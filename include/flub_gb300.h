@@ -113,6 +113,39 @@ int flub_subtract_gradient(float *u, float *v, float *w, const float *ur, const 
                            const float *p, float p_scale, const int32_t *tag, int nx, int ny, int nz,
                            void *stream);
 
+/* ---------------------------------------------------------------- rigid face velocities, cut cells */
+
+/* rigid_coupling.py:51-70 precompute_solid_vel on the face array ur of axis d
+ * (shape (nx+[d==1], ny+[d==2], nz+[d==3])) with face owners (int32, -1 none):
+ * (v + omega x (pos - x))[d-1] of the owner body at the face centre
+ * pos = ((i, j, k) + stagger) * h0 where 0.01 h0 < i * h0 < 1 - 0.01 h0 (the
+ * reference tests the first index on every axis), else 0.  Bodies: HOST
+ * arrays bx, bv, bw of nbodies x 3 floats (position, velocity, angular
+ * velocity), nbodies <= 64; an owner >= nbodies counts as none. */
+int flub_solid_vel(float *ur, const int32_t *owner, int nx, int ny, int nz, int d, float h0, const float *bx,
+                   const float *bv, const float *bw, int nbodies, void *stream);
+
+/* geometry.py phi_to_fraction with utils/util.py:169-228 fraction_edge /
+ * fraction_triangle / fraction_quad: face fractions (sdf > 0 part) of axis d
+ * in place on frac, which holds the face-centre SDF on entry; phi_nodes is
+ * the SDF at the grid nodes, shape (nx+1, ny+1, nz+1). */
+int flub_phi_to_fraction(const float *phi_nodes, float *frac, int nx, int ny, int nz, int d, void *stream);
+
+/* divergence.py:4-42 divergence_fractional_3d: div (nx, ny, nz) = fraction-
+ * weighted face velocities plus the rigid velocities on the solid parts. */
+int flub_divergence_fractional(const float *u, const float *v, const float *w, float *div, const float *fu,
+                               const float *fv, const float *fw, const float *ur, const float *vr, const float *wr,
+                               int nx, int ny, int nz, void *stream);
+
+/* subtract_gradient.py:7-122 u/v/w_subtract_gradient_batty_3d on the face
+ * array uf of axis d: ghost-fluid pressure gradient divided by the fluid
+ * fraction theta >= 0.01 of the face (phi: cell-centre level set), the rigid
+ * velocity where the face fraction frac is 0, 0 between two air cells; the
+ * domain-boundary face layers become 0 where lo <= 1e-5 or
+ * lo + index * h >= 1 - 1e-5 (lo: the domain's offset on axis d). */
+int flub_subtract_gradient_batty(float *uf, const float *p, const float *frac, const float *phi, const float *ur,
+                                 int nx, int ny, int nz, int d, float lo, float h, void *stream);
+
 /* ---------------------------------------------------------------- velocity extrapolation */
 
 /* utils/util.py:423-437 set_unknown over the cell grid: the face flag arrays

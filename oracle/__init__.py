@@ -71,6 +71,12 @@ def _declare(L):
     L.oracle_num_threads.restype = i32
     L.oracle_set_schedule.argtypes = [i32, i32, f64]
     L.oracle_set_schedule.restype = None
+    L.oracle_solid_vel.argtypes = [vp, vp, i32, i32, i32, i32, f32, vp, vp, vp, i32]
+    L.oracle_fraction_quad.argtypes = [f32, f32, f32, f32, f32]
+    L.oracle_fraction_quad.restype = f32
+    L.oracle_phi_to_fraction.argtypes = [vp, vp, i32, i32, i32, i32]
+    L.oracle_divergence_fractional.argtypes = [vp] * 10 + [i32, i32, i32]
+    L.oracle_subtract_gradient_batty.argtypes = [vp] * 5 + [i32, i32, i32, i32, f32, f32]
     L.oracle_set_unknown.argtypes = [vp, vp, vp, vp, i32, i32, i32]
     L.oracle_extrapolate_axis.argtypes = [vp, vp, i32, i32, i32]
     L.oracle_flush_unknown.argtypes = [vp, i64]
@@ -176,6 +182,50 @@ def subtract_gradient(uf, urf, p, tag, d):
     assert uf.dtype == np.float32 and uf.flags.c_contiguous
     lib().oracle_subtract_gradient(_ptr(uf), _ptr(_c(urf, np.float32)), _ptr(_c(p, np.float32)),
                                    _ptr(_c(tag, np.int32)), nx, ny, nz, d)
+    return uf
+
+
+# ---------------------------------------------------------------- rigid face velocities, cut cells
+
+def solid_vel(ur, owner, d, h0, bx, bv, bw):
+    """rigid_coupling.py:51-70 precompute_solid_vel on the face array of axis d (in place)."""
+    assert ur.dtype == np.float32 and ur.flags.c_contiguous
+    bx, bv, bw = (np.ascontiguousarray(a, np.float32).reshape(-1, 3) for a in (bx, bv, bw))
+    lib().oracle_solid_vel(_ptr(ur), _ptr(_c(owner, np.int32)), *ur.shape, int(d), float(h0), _ptr(bx), _ptr(bv),
+                           _ptr(bw), bx.shape[0])
+    return ur
+
+
+def fraction_quad(ya, yb, yc, yd, yctr):
+    """utils/util.py:221-228 fraction_quad."""
+    return float(lib().oracle_fraction_quad(ya, yb, yc, yd, yctr))
+
+
+def phi_to_fraction(phi_nodes, frac, d):
+    """geometry.py phi_to_fraction (in place on frac, which holds the face-centre SDF)."""
+    nx, ny, nz = (s - 1 for s in phi_nodes.shape)
+    assert frac.dtype == np.float32 and frac.flags.c_contiguous
+    lib().oracle_phi_to_fraction(_ptr(_c(phi_nodes, np.float32)), _ptr(frac), nx, ny, nz, int(d))
+    return frac
+
+
+def divergence_fractional(u, v, w, fu, fv, fw, ur, vr, wr):
+    """divergence.py:4-42 divergence_fractional_3d."""
+    nx, ny, nz = u.shape[0] - 1, u.shape[1], u.shape[2]
+    div = np.zeros((nx, ny, nz), np.float32)
+    arrs = [_c(a, np.float32) for a in (u, v, w)]
+    lib().oracle_divergence_fractional(*(_ptr(a) for a in arrs), _ptr(div),
+                                       *(_ptr(_c(a, np.float32)) for a in (fu, fv, fw, ur, vr, wr)), nx, ny, nz)
+    return div
+
+
+def subtract_gradient_batty(uf, p, frac, phi, urf, d, lo, h):
+    """subtract_gradient.py:7-122 u/v/w_subtract_gradient_batty_3d (in place on uf)."""
+    nx, ny, nz = phi.shape
+    assert uf.dtype == np.float32 and uf.flags.c_contiguous
+    lib().oracle_subtract_gradient_batty(_ptr(uf), _ptr(_c(p, np.float32)), _ptr(_c(frac, np.float32)),
+                                         _ptr(_c(phi, np.float32)), _ptr(_c(urf, np.float32)), nx, ny, nz, int(d),
+                                         float(lo), float(h))
     return uf
 
 

@@ -209,6 +209,176 @@ void oracle_subtract_gradient(float *uf, const float *urf, const float *p, const
             }
 }
 
+/* ---------------- rigid face velocities and cut cells ---------------- */
+
+/* rigid_coupling.py:51-70 precompute_solid_vel for the face array of axis d
+ * (shape (fx, fy, fz)) with face owners owner (-1: none): the rigid velocity
+ * v + omega x (pos - x) of the owner body at the face centre
+ * pos = ((i, j, k) + stagger) * h0, component d-1, where i * h0 lies strictly
+ * inside (0.01 h0, 1 - 0.01 h0) -- the reference tests the first index i for
+ * every axis -- else 0.  Bodies: x, v, omega as n x 3 floats; an owner >= n
+ * counts as none. */
+void oracle_solid_vel(float *ur, const int32_t *owner, int fx, int fy, int fz, int d, float h0, const float *bx,
+                      const float *bv, const float *bw, int n) {
+    float st[3] = {0.5f, 0.5f, 0.5f};
+    st[d - 1] = 0.0f;
+    float eps = h0 * 0.01f;
+#pragma omp parallel for schedule(static)
+    for (int i = 0; i < fx; i++)
+        for (int j = 0; j < fy; j++)
+            for (int k = 0; k < fz; k++) {
+                int64_t f = ((int64_t)i * fy + j) * fz + k;
+                int o = owner[f];
+                float tmp = (float)i * h0;
+                if (eps < tmp && tmp < 1.0f - eps && o >= 0 && o < n) {
+                    float pos[3] = {((float)i + st[0]) * h0, ((float)j + st[1]) * h0, ((float)k + st[2]) * h0};
+                    float p[3] = {pos[0] - bx[3 * o], pos[1] - bx[3 * o + 1], pos[2] - bx[3 * o + 2]};
+                    const float *w = bw + 3 * o, *v = bv + 3 * o;
+                    float c[3] = {w[1] * p[2] - w[2] * p[1], w[2] * p[0] - w[0] * p[2], w[0] * p[1] - w[1] * p[0]};
+                    ur[f] = v[d - 1] + c[d - 1];
+                } else {
+                    ur[f] = 0.0f;
+                }
+            }
+}
+
+/* utils/util.py:169-187 fraction_edge, :190-219 fraction_triangle, :221-228
+ * fraction_quad: the fraction of a face with sdf > 0 from its 4 corner values
+ * and its centre value. */
+static float fr_edge(float yl, float yr) {
+    float ret;
+    if (yl > 0.0f && yr > 0.0f) ret = 1.0f;
+    else if (yl > 0.0f) ret = yl / (yl - yr);
+    else if (yr > 0.0f) ret = yr / (yr - yl);
+    else ret = 0.0f;
+    if (ret < 0.1f) ret = 0.0f;
+    else if (ret > 1.0f) ret = 1.0f;
+    return ret;
+}
+
+static float fr_tri(float ya, float yb, float yc) {
+    float fab = fr_edge(ya, yb), fbc = fr_edge(yb, yc), fca = fr_edge(yc, ya), ret;
+    if (ya > 0.0f && yb > 0.0f && yc > 0.0f) ret = 1.0f;
+    else if (ya > 0.0f && yb > 0.0f) ret = 1.0f - (1.0f - fca) * (1.0f - fbc);
+    else if (ya > 0.0f && yc > 0.0f) ret = 1.0f - (1.0f - fab) * (1.0f - fbc);
+    else if (yb > 0.0f && yc > 0.0f) ret = 1.0f - (1.0f - fab) * (1.0f - fca);
+    else if (ya > 0.0f) ret = fca * fab;
+    else if (yb > 0.0f) ret = fab * fbc;
+    else if (yc > 0.0f) ret = fbc * fca;
+    else ret = 0.0f;
+    return ret < 0.0f ? 0.0f : (ret > 1.0f ? 1.0f : ret);
+}
+
+float oracle_fraction_quad(float ya, float yb, float yc, float yd, float yctr) {
+    float f = fr_tri(ya, yb, yctr) + fr_tri(yb, yc, yctr) + fr_tri(yc, yd, yctr) + fr_tri(yd, ya, yctr);
+    f = f * 0.25f;
+    if (f < 0.1f) f = 0.0f;
+    else if (f > 1.0f) f = 1.0f;
+    return f;
+}
+
+/* geometry.py phi_to_fraction: face fractions of axis d in place; frac holds the
+ * face-centre SDF on entry; phi is the SDF at the grid nodes, shape
+ * (nx+1, ny+1, nz+1). */
+void oracle_phi_to_fraction(const float *phi, float *frac, int nx, int ny, int nz, int d) {
+    int fx = nx + (d == 1), fy = ny + (d == 2), fz = nz + (d == 3);
+    int py = ny + 1, pz = nz + 1;
+#define PN(a, b, c) phi[((int64_t)(a) * py + (b)) * pz + (c)]
+#pragma omp parallel for schedule(static)
+    for (int i = 0; i < fx; i++)
+        for (int j = 0; j < fy; j++)
+            for (int k = 0; k < fz; k++) {
+                float ya = PN(i, j, k), yb, yc, yd;
+                if (d == 1) { yb = PN(i, j + 1, k); yc = PN(i, j + 1, k + 1); yd = PN(i, j, k + 1); }
+                else if (d == 2) { yb = PN(i + 1, j, k); yc = PN(i + 1, j, k + 1); yd = PN(i, j, k + 1); }
+                else { yb = PN(i + 1, j, k); yc = PN(i + 1, j + 1, k); yd = PN(i, j + 1, k); }
+                int64_t f = ((int64_t)i * fy + j) * fz + k;
+                frac[f] = oracle_fraction_quad(ya, yb, yc, yd, frac[f]);
+            }
+#undef PN
+}
+
+static inline int clampi(int v, int lo, int hi) { return v < lo ? lo : (v > hi ? hi : v); }
+
+/* divergence.py:4-42 divergence_fractional_3d: face-fraction weighted
+ * divergence plus the rigid velocities on the solid parts of the faces. */
+void oracle_divergence_fractional(const float *u, const float *v, const float *w, float *div, const float *fu,
+                                  const float *fv, const float *fw, const float *ur, const float *vr, const float *wr,
+                                  int nx, int ny, int nz) {
+#define SU(a, q, i, j, k) a[((int64_t)clampi(i, 0, nx) * ny + clampi(j, 0, ny - 1)) * nz + clampi(k, 0, nz - 1)]
+#define SV(a, q, i, j, k) a[((int64_t)clampi(i, 0, nx - 1) * (ny + 1) + clampi(j, 0, ny)) * nz + clampi(k, 0, nz - 1)]
+#define SW(a, q, i, j, k) a[((int64_t)clampi(i, 0, nx - 1) * ny + clampi(j, 0, ny - 1)) * (nz + 1) + clampi(k, 0, nz)]
+#pragma omp parallel for schedule(static)
+    for (int i = 0; i < nx; i++)
+        for (int j = 0; j < ny; j++)
+            for (int k = 0; k < nz; k++) {
+                float vl = SU(u, 0, i, j, k), vr_ = SU(u, 0, i + 1, j, k);
+                float vb = SV(v, 0, i, j, k), vt = SV(v, 0, i, j + 1, k);
+                float vf = SW(w, 0, i, j, k), vn = SW(w, 0, i, j, k + 1);
+                float l = SU(fu, 0, i, j, k), r = SU(fu, 0, i + 1, j, k);
+                float b = SV(fv, 0, i, j, k), t = SV(fv, 0, i, j + 1, k);
+                float f = SW(fw, 0, i, j, k), n = SW(fw, 0, i, j, k + 1);
+                float vls = SU(ur, 0, i, j, k), vrs = SU(ur, 0, i + 1, j, k);
+                float vbs = SV(vr, 0, i, j, k), vts = SV(vr, 0, i, j + 1, k);
+                float vfs = SW(wr, 0, i, j, k), vns = SW(wr, 0, i, j, k + 1);
+                float a = vr_ * r - vl * l + vt * t - vb * b + vn * n - vf * f;
+                float s = (1.0f - r) * vrs - (1.0f - l) * vls + (1.0f - t) * vts - (1.0f - b) * vbs +
+                          (1.0f - n) * vns - (1.0f - f) * vfs;
+                div[IX(i, j, k)] = a + s;
+            }
+#undef SU
+#undef SV
+#undef SW
+}
+
+/* utils/util.py:404-412 fraction_of_fluid. */
+static float frac_fluid(float p1, float p2) {
+    if (p1 < 0.0f && p2 < 0.0f) return 1.0f;
+    if (p1 >= 0.0f && p2 >= 0.0f) return 0.0f;
+    return 1.0f - fmaxf(p1, p2) / fabsf(p1 - p2);
+}
+
+/* subtract_gradient.py:7-122 u/v/w_subtract_gradient_batty_3d on the face array
+ * of axis d: ghost-fluid pressure gradient over the fluid fraction theta
+ * (at least 0.01), the rigid velocity on faces of zero fraction, 0 on faces
+ * between two air cells; on the domain-boundary face layers the face becomes 0
+ * when lo <= 1e-5 or lo + index * h >= 1 - 1e-5 (lo: the domain's offset on
+ * that axis), else it is left as it is. */
+void oracle_subtract_gradient_batty(float *uf, const float *p, const float *fr, const float *phi, const float *ur,
+                                    int nx, int ny, int nz, int d, float lo, float h) {
+    const float eps = 1e-5f;
+    int fx = nx + (d == 1), fy = ny + (d == 2), fz = nz + (d == 3);
+    int gridn = (d == 1 ? fx : (d == 2 ? fy : fz)) - 1;
+#define PC(a, i, j, k) a[((int64_t)clampi(i, 0, nx - 1) * ny + clampi(j, 0, ny - 1)) * nz + clampi(k, 0, nz - 1)]
+#pragma omp parallel for schedule(static)
+    for (int i = 0; i < fx; i++)
+        for (int j = 0; j < fy; j++)
+            for (int k = 0; k < fz; k++) {
+                int64_t f = ((int64_t)i * fy + j) * fz + k;
+                int ii = d == 1 ? i : (d == 2 ? j : k);
+                if (0 < ii && ii < gridn) {
+                    int il = i - (d == 1), jl = j - (d == 2), kl = k - (d == 3);
+                    float ph = phi[IX(i, j, k)], pl = phi[IX(il, jl, kl)];
+                    if (ph < 0.0f || pl < 0.0f) {
+                        if (fr[f] == 0.0f) {
+                            uf[f] = ur[f];
+                        } else {
+                            float plo = pl >= 0.0f ? 0.0f : PC(p, il, jl, kl);
+                            float phi_ = ph >= 0.0f ? 0.0f : PC(p, i, j, k);
+                            float theta = d == 3 ? frac_fluid(pl, ph) : frac_fluid(ph, pl);
+                            theta = fmaxf(0.01f, theta);
+                            uf[f] = uf[f] - (phi_ - plo) / theta;
+                        }
+                    } else {
+                        uf[f] = 0.0f;
+                    }
+                } else if (lo <= eps || lo + (float)ii * h >= 1.0f - eps) {
+                    uf[f] = 0.0f;
+                }
+            }
+#undef PC
+}
+
 /* ---------------- velocity extrapolation ---------------- */
 
 /* utils/util.py:423-437 set_unknown, launched over the cell grid (nx, ny, nz):

@@ -340,3 +340,66 @@ def test_extrapolation_passes_repeat_the_first():
         assert np.array_equal(a, b)
     for a, b in zip(t1, t4):
         assert np.array_equal(a, b)
+
+
+# ---------------------------------------------------------------- rigid face velocities, cut cells
+
+def test_fraction_edge_triangle_quad_kat():
+    # all positive / all negative / half-plane through the face centre
+    assert O.fraction_quad(1, 1, 1, 1, 1) == 1.0
+    assert O.fraction_quad(-1, -1, -1, -1, -1) == 0.0
+    assert O.fraction_quad(1, -1, -1, 1, 0.0) == 0.5
+    # small positive slivers are cut to 0 (edge fraction < 0.1, face fraction < 0.1)
+    assert O.fraction_quad(0.05, -1, -1, -1, -1) == 0.0
+
+
+def test_solid_vel_kat():
+    # one body rotating about z with omega = (0, 0, 2) at x = (0.5, 0.5, 0.5), v = (1, 0, 0)
+    n = 4
+    h0 = 1.0 / n
+    ur = np.zeros((n + 1, n, n), np.float32)
+    owner = np.zeros(ur.shape, np.int32)
+    owner[:, :, 0] = -1
+    O.solid_vel(ur, owner, 1, h0, [[0.5, 0.5, 0.5]], [[1.0, 0.0, 0.0]], [[0.0, 0.0, 2.0]])
+    # u = v_x + (omega x p)_x = 1 - 2 * p_y with p_y = (j + 0.5) h0 - 0.5
+    for i in range(n + 1):
+        for j in range(n):
+            for k in range(n):
+                inside = 0.01 * h0 < i * h0 < 1 - 0.01 * h0 and owner[i, j, k] != -1
+                expect = 1.0 - 2.0 * ((j + 0.5) * h0 - 0.5) if inside else 0.0
+                assert ur[i, j, k] == pytest.approx(expect, abs=1e-6)
+
+
+def test_divergence_fractional_full_fluid_is_plain_divergence():
+    rng = np.random.default_rng(8)
+    s = (5, 4, 3)
+    u = rng.standard_normal((6, 4, 3)).astype(np.float32)
+    v = rng.standard_normal((5, 5, 3)).astype(np.float32)
+    w = rng.standard_normal((5, 4, 4)).astype(np.float32)
+    ones = [np.ones_like(a) for a in (u, v, w)]
+    zeros = [np.zeros_like(a) for a in (u, v, w)]
+    d = O.divergence_fractional(u, v, w, *ones, *zeros)
+    ref = (u[1:] - u[:-1]) + (v[:, 1:] - v[:, :-1]) + (w[:, :, 1:] - w[:, :, :-1])
+    assert np.allclose(d, ref, atol=1e-5)
+    # fully solid faces: only the rigid velocities count
+    d2 = O.divergence_fractional(u, v, w, *zeros, *[a * 0 + 2.0 for a in (u, v, w)])
+    assert np.allclose(d2, 0.0)
+
+
+def test_subtract_gradient_batty_kat():
+    nx, ny, nz = 4, 1, 1
+    phi = np.array([-1.0, -1.0, 0.5, 1.0], np.float32).reshape(nx, ny, nz)   # fluid, fluid, air, air
+    p = np.array([3.0, 1.0, 9.0, 9.0], np.float32).reshape(nx, ny, nz)
+    uf = np.zeros((nx + 1, ny, nz), np.float32)
+    frac = np.ones_like(uf)
+    ur = np.full_like(uf, 7.0)
+    O.subtract_gradient_batty(uf, p, frac, phi, ur, 1, 0.0, 1.0 / nx)
+    assert uf[1, 0, 0] == pytest.approx(-(1.0 - 3.0))                   # fluid-fluid: theta = 1
+    theta = 1.0 - 0.5 / 1.5                                              # fluid (-1) next to air (0.5)
+    assert uf[2, 0, 0] == pytest.approx(-(0.0 - 1.0) / theta)            # ghost pressure 0 in the air
+    assert uf[3, 0, 0] == 0.0                                            # air-air
+    assert uf[0, 0, 0] == 0.0 and uf[4, 0, 0] == 0.0                     # domain boundary, lo = 0
+    frac[1] = 0.0
+    uf[:] = 0.0
+    O.subtract_gradient_batty(uf, p, frac, phi, ur, 1, 0.0, 1.0 / nx)
+    assert uf[1, 0, 0] == 7.0                                            # zero fraction: rigid velocity
