@@ -455,6 +455,35 @@ def run_ours(args):
                      "achieved_GBps": 12 * n_faces / (ext_ms * 1e-3) / 1e9,
                      "note": "algorithmic bytes: read value and flag, write value, 12 B per face"}
 
+    # ---- advection at the start of the reference's step (water_3d.py:34-37:
+    # advect_phi, then advect_uv_mc on the three face arrays), timed warm
+    from flub_gb300.fields import Field, MACGrid
+    new_phi = torch.empty_like(phi)
+    new_vel = MACGrid(*(Field(torch.empty_like(a), stagger=a_f.stagger, d=a_f.d)
+                        for a_f, a in ((vel.u, vel.u.f), (vel.v, vel.v.f), (vel.w, vel.w.f))))
+
+    def time_ms(fn, reps=10):
+        fn()
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        for _ in range(reps):
+            fn()
+        e1.record(stream)
+        torch.cuda.synchronize()
+        return e0.elapsed_time(e1) / reps
+
+    uv_ms = time_ms(lambda: K.advect_uv_mc(vel, new_vel))
+    phi_ms = time_ms(lambda: K.advect_phi_field(vel, Field(phi), Field(new_phi)))
+    n_cells = phi.numel()
+    advection = {"ms_advect_uv_mc": uv_ms, "ms_advect_phi": phi_ms, "faces": n_faces, "cells": n_cells,
+                 "faces_per_s": n_faces / (uv_ms * 1e-3), "cells_per_s": n_cells / (phi_ms * 1e-3),
+                 "alg_hbm_bytes": {"advect_uv_mc": 20 * n_faces, "advect_phi": 20 * n_cells},
+                 "achieved_GBps_uv_mc": 20 * n_faces / (uv_ms * 1e-3) / 1e9,
+                 "note": "algorithmic HBM bytes: the field read and written plus the three velocity components "
+                         "once, 20 B per element; the kernels gather about 280 (MacCormack) or 136 (phi) values "
+                         "per element through L1, which bounds them"}
+
     # ---- CPU baseline: the oracle on the host cores (rank 0, N = 1 only)
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu_baseline and args.cpu_baseline_steps > 0:
@@ -488,7 +517,7 @@ def run_ours(args):
                        "max_abs_div_after": div_after, "l2_flush": "inputs larger than L2 (~1.3 GB working set)",
                        "parallelism": f"replicas x{world}"},
             "roofline": roofline, "cpu_baseline": cpu, "e2e": e2e, "gpu_launches": int(launches),
-            "extrapolation": extrapolation,
+            "extrapolation": extrapolation, "advection": advection,
             "clocks": clocks,
         }
         print(json.dumps(out), flush=True)

@@ -61,6 +61,12 @@ SIGNATURES = {
     "flub_extrapolate_axis": (_i32, [_vp, _vp, _i32, _i32, _i32, _i32, _vp]),
     "flub_flush_unknown": (_i32, [_vp, _i64, _vp]),
     "flub_extrapolate": (_i32, [_vp] * 7 + [_i32, _i32, _i32, _i32, _vp]),
+    "flub_advect_mc": (_i32, [_vp, _vp, _vp, _i32, _i32, _i32, _vp, _vp, _vp, _i32, _i32, _i32, _f32, _f32, _f32,
+                              _f32, _f32, _f32, _i32, _vp]),
+    "flub_advect_velocity_mc": (_i32, [_vp] * 6 + [_i32, _i32, _i32, _f32, _f32, _f32, _vp]),
+    "flub_advect_phi": (_i32, [_vp, _vp, _vp, _i32, _i32, _i32, _vp, _vp, _i32, _i32, _i32, _f32, _f32, _f32, _f32,
+                               _f32, _f32, _vp]),
+    "flub_advect_simple": (_i32, [_vp, _vp, _vp, _i32, _i32, _i32, _vp, _vp, _i32, _i32, _i32, _f32, _f32, _vp]),
     "flub_mg_workspace_bytes": (_sz, [_i32, _i32, _i32, _i32, _i32]),
     "flub_mg_create": (_i32, [_i32, _i32, _i32, _i32, _i32, _vp, _sz, ctypes.POINTER(_vp)]),
     "flub_mg_destroy": (_i32, [_vp]),

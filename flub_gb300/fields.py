@@ -6,7 +6,7 @@ have ``shape``, face fields ``shape + e_d`` along their axis d (1 = u, 2 = v,
 3 = w).  ``stagger`` and ``d`` carry the same meaning as in the reference.
 """
 from dataclasses import dataclass
-from typing import Tuple
+from typing import Optional, Tuple
 
 import torch
 
@@ -18,16 +18,26 @@ _STAGGER = {0: (0.5, 0.5, 0.5), 1: (0.0, 0.5, 0.5), 2: (0.5, 0.0, 0.5), 3: (0.5,
 
 @dataclass
 class Field:
+    """A float field; ``stagger`` defaults to the one make_field gives axis
+    ``d`` (cell centres for d = 0, face centres for d = 1, 2, 3)."""
     f: torch.Tensor
-    stagger: Tuple[float, float, float] = (0.5, 0.5, 0.5)
+    stagger: Optional[Tuple[float, float, float]] = None
     d: int = 0
+
+    def __post_init__(self):
+        if self.stagger is None:
+            self.stagger = _STAGGER[self.d]
 
 
 @dataclass
 class IntField:
     f: torch.Tensor
-    stagger: Tuple[float, float, float] = (0.5, 0.5, 0.5)
+    stagger: Optional[Tuple[float, float, float]] = None
     d: int = 0
+
+    def __post_init__(self):
+        if self.stagger is None:
+            self.stagger = _STAGGER[self.d]
 
 
 @dataclass

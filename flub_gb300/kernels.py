@@ -280,6 +280,85 @@ def extrapolate(vel, tags, phi, n_cells):
     _lib.call("flub_extrapolate", *_faces(vel, shape), *_int_faces(tags, shape), pp, *shape, int(n_cells), _stream())
 
 
+# ------------------------------------------------------------------ advection
+
+DT = 1e-2  # const_param.py dt, the time step the reference's advection kernels read
+
+
+def _vel_args(vel):
+    u = _f(vel.u)
+    shape = (u.shape[0] - 1, u.shape[1], u.shape[2])
+    return _faces(vel, shape), shape
+
+
+def _h0(shape, h0):
+    return float(h0) if h0 is not None else 1.0 / shape[0]
+
+
+def _stagger_of(q, default):
+    st = getattr(q, "stagger", None)
+    return tuple(float(x) for x in (st if st is not None else default))
+
+
+def advect_mc_stage(args_common, q_in, q_out, q_tmp, stage, dt=DT, h0=None, minmax_h=None):
+    """advect.py:57-101 _advect_mc_1 / _2 / _3 (stage 1, 2, 3) on the field
+    q_in (a Field: its stagger is used), traced by the MACGrid args_common;
+    stage 0 runs all three in one pass (q_tmp unused).  h0 defaults to 1 / nx
+    (const_param.py h0), minmax_h to h0 (what sample_minmax receives)."""
+    faces, shape = _vel_args(args_common)
+    hh = _h0(shape, h0)
+    qi, qo = _f(q_in), _f(q_out)
+    qs = tuple(qi.shape)
+    st = _stagger_of(q_in, (0.5, 0.5, 0.5))
+    qt = _ptr(_f(q_tmp), torch.float32, qs, "q_tmp") if q_tmp is not None else None
+    _lib.call("flub_advect_mc", *faces, *shape, _ptr(qi, torch.float32, qs, "q_in"), _ptr(qo, torch.float32, qs, "q_out"),
+              qt, *qs, *st, float(dt), hh, hh if minmax_h is None else float(minmax_h), int(stage), _stream())
+
+
+def advect_mc(args_common, q_in, q_out, dt=DT, h0=None, minmax_h=None):
+    """advect.py:124-128 advect_mc: MacCormack advection of q_in into q_out,
+    the three reference kernels fused into one launch (same values)."""
+    advect_mc_stage(args_common, q_in, q_out, None, 0, dt, h0, minmax_h)
+
+
+def advect_uv_mc(vel_in, vel_out, dt=DT, h0=None, minmax_h=None):
+    """advect.py:130-133 advect_uv_mc: each face array of vel_in advected by
+    vel_in into vel_out."""
+    faces, shape = _vel_args(vel_in)
+    hh = _h0(shape, h0)
+    _lib.call("flub_advect_velocity_mc", *faces, *_faces(vel_out, shape), *shape, float(dt), hh,
+              hh if minmax_h is None else float(minmax_h), _stream())
+
+
+def advect_3d(vel, qf, new_vel, new_qf, dt=DT, h0=None, minmax_h=None):
+    """advect.py:136-138 advect_3d: the scalar qf and the velocity itself."""
+    advect_mc(vel, qf, new_qf, dt, h0, minmax_h)
+    advect_uv_mc(vel, new_vel, dt, h0, minmax_h)
+
+
+def advect_phi_field(vel, phi, new_phi, dt=DT, h0=None):
+    """advect.py:39-54 advect_phi: the level set traced back by vel, tricubic
+    where the foot of the trace lies inside the grid, else h0."""
+    faces, shape = _vel_args(vel)
+    hh = _h0(shape, h0)
+    pi, po = _f(phi), _f(new_phi)
+    ps = tuple(pi.shape)
+    _lib.call("flub_advect_phi", *faces, *shape, _ptr(pi, torch.float32, ps, "phi"), _ptr(po, torch.float32, ps,
+                                                                                         "new_phi"),
+              *ps, *_stagger_of(phi, (0.5, 0.5, 0.5)), float(dt), hh, hh, _stream())
+
+
+def advect_simple(uf, vf, wf, qf, new_qf, dt, h):
+    """advect.py:24-37 advect_simple_3d (raw arrays; trilinear sample)."""
+    u, v, w, q, qn = (_f(a) for a in (uf, vf, wf, qf, new_qf))
+    shape = (u.shape[0] - 1, u.shape[1], u.shape[2])
+    qs = tuple(q.shape)
+    _lib.call("flub_advect_simple", *(_ptr(a, torch.float32, field_shape(shape, d + 1), "uvw"[d] + "f")
+                                      for d, a in enumerate((u, v, w))),
+              *shape, _ptr(q, torch.float32, qs, "qf"), _ptr(qn, torch.float32, qs, "new_qf"), *qs, float(dt),
+              float(h), _stream())
+
+
 # ------------------------------------------------------------------ wp.launch mirror
 
 class Kernel:
@@ -354,6 +433,12 @@ w_subtract_gradient_batty_3d = Kernel("w_subtract_gradient_batty_3d",
                                           wf, pf, fw, phi, wr, 3, far, h),
                                       _dim_of(0))
 set_unknown_3d = Kernel("set_unknown", set_unknown, _dim_of(0))
+# advect.py kernels: inputs=[args_common, q_in, q_out, q_tmp] / [vel, phi, new_phi] / [uf, vf, wf, qf, new_qf, dt, h]
+_advect_mc_1 = Kernel("_advect_mc_1", lambda vel, qi, qo, qt: advect_mc_stage(vel, qi, qo, qt, 1), _dim_of(1))
+_advect_mc_2 = Kernel("_advect_mc_2", lambda vel, qi, qo, qt: advect_mc_stage(vel, qi, qo, qt, 2), _dim_of(1))
+_advect_mc_3 = Kernel("_advect_mc_3", lambda vel, qi, qo, qt: advect_mc_stage(vel, qi, qo, qt, 3), _dim_of(1))
+advect_phi = Kernel("advect_phi", advect_phi_field, _dim_of(1))
+advect_simple_3d = Kernel("advect_simple_3d", advect_simple, _dim_of(3))
 
 
 def launch(kernel, dim, inputs, device=None, stream=None):

@@ -172,6 +172,43 @@ int flub_flush_unknown(int32_t *unk, int64_t n, void *stream);
 int flub_extrapolate(float *u, float *v, float *w, int32_t *tu, int32_t *tv, int32_t *tw, const float *phi, int nx,
                      int ny, int nz, int n_passes, void *stream);
 
+/* ---------------------------------------------------------------- advection */
+
+/* Velocity (u, v, w) below: MAC face arrays of the cell grid (nx, ny, nz),
+ * shapes (nx+1, ny, nz), (nx, ny+1, nz), (nx, ny, nz+1).  Positions are in grid
+ * units, samples clamp their indices to the array (utils/util.py:20-28).
+ * Element counts must stay below 2^31. */
+
+/* advect.py:57-101 _advect_mc_1 (stage 1: q_out = the tricubic sample of
+ * q_in at the RK3 foot of the trace over dt), _advect_mc_2 (stage 2: q_tmp =
+ * the sample traced over -dt), _advect_mc_3 (stage 3: q_out += (q_in - q_tmp)
+ * / 2, replaced by the stage-1 value unless strictly inside the min/max of
+ * sample_minmax, :103-122), or stage 0: all three in one pass
+ * (advect.py:124-128 advect_mc; q_tmp may be NULL).  q_in has shape
+ * (qx, qy, qz) and stagger (sx, sy, sz).  minmax_h: the divisor of
+ * sample_minmax's position (the reference passes h0, as h; 1 centres the
+ * bounds on the foot of the trace). */
+int flub_advect_mc(const float *u, const float *v, const float *w, int nx, int ny, int nz, const float *q_in,
+                   float *q_out, float *q_tmp, int qx, int qy, int qz, float sx, float sy, float sz, float dt, float h,
+                   float minmax_h, int stage, void *stream);
+
+/* advect.py:130-133 advect_uv_mc: the three face arrays advected by
+ * themselves into (u_out, v_out, w_out), each by advect_mc. */
+int flub_advect_velocity_mc(const float *u, const float *v, const float *w, float *u_out, float *v_out, float *w_out,
+                            int nx, int ny, int nz, float dt, float h, float minmax_h, void *stream);
+
+/* advect.py:39-54 advect_phi: phi (px, py, pz) with stagger (sx, sy, sz)
+ * traced back over dt; the tricubic sample where the foot lies in
+ * [0, extent) on every axis, else `outside` (the reference: h0). */
+int flub_advect_phi(const float *u, const float *v, const float *w, int nx, int ny, int nz, const float *phi,
+                    float *phi_out, int px, int py, int pz, float sx, float sy, float sz, float dt, float h,
+                    float outside, void *stream);
+
+/* advect.py:24-37 advect_simple_3d: cell-centred q traced back from the cell
+ * centre, sampled trilinearly (utils/util.py:91-96 trilerp). */
+int flub_advect_simple(const float *u, const float *v, const float *w, int nx, int ny, int nz, const float *q,
+                       float *q_out, int qx, int qy, int qz, float dt, float h, void *stream);
+
 /* ---------------------------------------------------------------- MGPCG */
 
 /* multigrid/mgpcg.py:234-490 class MGPCG.  One handle = one level hierarchy

@@ -80,6 +80,13 @@ def _declare(L):
     L.oracle_set_unknown.argtypes = [vp, vp, vp, vp, i32, i32, i32]
     L.oracle_extrapolate_axis.argtypes = [vp, vp, i32, i32, i32]
     L.oracle_flush_unknown.argtypes = [vp, i64]
+    L.oracle_advect_mc.argtypes = [vp, vp, vp, i32, i32, i32, vp, vp, vp, i32, i32, i32, vp, f32, f32, f32, i32]
+    L.oracle_advect_phi.argtypes = [vp, vp, vp, i32, i32, i32, vp, vp, i32, i32, i32, vp, f32, f32, f32]
+    L.oracle_advect_simple.argtypes = [vp, vp, vp, i32, i32, i32, vp, vp, i32, i32, i32, f32, f32]
+    L.oracle_sample_velocity.argtypes = [vp, vp, vp, i32, i32, i32, vp, vp]
+    L.oracle_backtrace.argtypes = [vp, vp, vp, i32, i32, i32, vp, f32, f32]
+    L.oracle_tricubic.argtypes = [vp, i32, i32, i32, f32, f32, f32]
+    L.oracle_tricubic.restype = f32
 
 
 REFERENCE_SCHEDULE = (-1, 3, 1.0)
@@ -259,6 +266,84 @@ def extrapolate(u, v, w, tu, tv, tw, phi, n_cells):
             extrapolate_axis(q, t)
         for t in (tu, tv, tw):
             flush_unknown(t)
+
+
+# ---------------------------------------------------------------- advection
+
+def _vel(u, v, w):
+    u, v, w = (_c(a, np.float32) for a in (u, v, w))
+    nx, ny, nz = v.shape[0], u.shape[1], u.shape[2]
+    assert u.shape == (nx + 1, ny, nz) and v.shape == (nx, ny + 1, nz) and w.shape == (nx, ny, nz + 1)
+    return u, v, w, (nx, ny, nz)
+
+
+STAGGER = {0: (0.5, 0.5, 0.5), 1: (0.0, 0.5, 0.5), 2: (0.5, 0.0, 0.5), 3: (0.5, 0.5, 0.0)}
+
+
+def advect_mc(u, v, w, q_in, stagger, dt, h, minmax_h=None, stage=0, q_out=None, q_tmp=None):
+    """advect.py:57-128: _advect_mc_1/2/3 (stage 1, 2, 3; q_out and q_tmp
+    updated in place and returned) or the whole advect_mc (stage 0: a new
+    q_out).  minmax_h: the divisor of sample_minmax (the reference's h0, the
+    default)."""
+    u, v, w, (nx, ny, nz) = _vel(u, v, w)
+    q_in = _c(q_in, np.float32)
+    q_out = np.zeros_like(q_in) if q_out is None else q_out
+    q_tmp = np.zeros_like(q_in) if q_tmp is None else q_tmp
+    for a in (q_out, q_tmp):
+        assert a.dtype == np.float32 and a.flags.c_contiguous and a.shape == q_in.shape
+    st = np.asarray(stagger, np.float32)
+    lib().oracle_advect_mc(_ptr(u), _ptr(v), _ptr(w), nx, ny, nz, _ptr(q_in), _ptr(q_out), _ptr(q_tmp), *q_in.shape,
+                           _ptr(st), dt, h, h if minmax_h is None else minmax_h, int(stage))
+    return q_out if stage != 2 else q_tmp
+
+
+def advect_velocity_mc(u, v, w, dt, h, minmax_h=None):
+    """advect.py:130-133 advect_uv_mc: the three face arrays advected by
+    themselves; returns (u_out, v_out, w_out)."""
+    return tuple(advect_mc(u, v, w, q, STAGGER[d], dt, h, minmax_h) for d, q in ((1, u), (2, v), (3, w)))
+
+
+def advect_phi(u, v, w, phi, dt, h, outside=None, stagger=(0.5, 0.5, 0.5)):
+    """advect.py:39-54 advect_phi (outside = h0 by default, as the reference)."""
+    u, v, w, (nx, ny, nz) = _vel(u, v, w)
+    phi = _c(phi, np.float32)
+    out = np.empty_like(phi)
+    st = np.asarray(stagger, np.float32)
+    lib().oracle_advect_phi(_ptr(u), _ptr(v), _ptr(w), nx, ny, nz, _ptr(phi), _ptr(out), *phi.shape, _ptr(st), dt,
+                            h, h if outside is None else outside)
+    return out
+
+
+def advect_simple(u, v, w, q, dt, h):
+    """advect.py:24-37 advect_simple_3d (trilinear, cell-centred q)."""
+    u, v, w, (nx, ny, nz) = _vel(u, v, w)
+    q = _c(q, np.float32)
+    out = np.empty_like(q)
+    lib().oracle_advect_simple(_ptr(u), _ptr(v), _ptr(w), nx, ny, nz, _ptr(q), _ptr(out), *q.shape, dt, h)
+    return out
+
+
+def sample_velocity(u, v, w, p):
+    """utils/util.py:34-88 sample_velocity_3d at one point (grid units)."""
+    u, v, w, (nx, ny, nz) = _vel(u, v, w)
+    pp = np.asarray(p, np.float32).copy()
+    out = np.empty(3, np.float32)
+    lib().oracle_sample_velocity(_ptr(u), _ptr(v), _ptr(w), nx, ny, nz, _ptr(pp), _ptr(out))
+    return out
+
+
+def backtrace(u, v, w, p, dt, h):
+    """advect.py:10-22 backtrace of one point (grid units)."""
+    u, v, w, (nx, ny, nz) = _vel(u, v, w)
+    pp = np.asarray(p, np.float32).copy()
+    lib().oracle_backtrace(_ptr(u), _ptr(v), _ptr(w), nx, ny, nz, _ptr(pp), dt, h)
+    return pp
+
+
+def tricubic(q, s, t, r):
+    """utils/util.py:148-160 _tricubic at index-space point (s, t, r)."""
+    q = _c(q, np.float32)
+    return float(lib().oracle_tricubic(_ptr(q), *q.shape, s, t, r))
 
 
 # ---------------------------------------------------------------- multigrid

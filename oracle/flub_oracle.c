@@ -440,6 +440,219 @@ void oracle_flush_unknown(int32_t *unk, int64_t n) {
         if (unk[c] == -1) unk[c] = 1;
 }
 
+/* ---------------- advection ----------------
+ * FP32, every product and sum rounded on its own in the order the reference's
+ * expressions give (this file is built with -ffp-contract=off).  Positions
+ * are in grid units (cell i spans [i, i+1)); every sample clamps its index
+ * to the array (utils/util.py:20-28 sample_3d). */
+
+typedef struct {
+    const float *q;
+    int gx, gy, gz;
+} adv_vol;
+
+static inline float adv_at(adv_vol V, int u, int v, int w) {
+    u = clampi(u, 0, V.gx - 1);
+    v = clampi(v, 0, V.gy - 1);
+    w = clampi(w, 0, V.gz - 1);
+    return V.q[((int64_t)u * V.gy + v) * V.gz + w];
+}
+
+/* floor as an int, with the argument limited to +-2^30 first (NaN -> -2^30),
+ * so that non-finite or absurd positions clamp the same way everywhere. */
+static inline int adv_ifloor(float x) { return (int)floorf(fminf(fmaxf(x, -1073741824.0f), 1073741824.0f)); }
+
+/* wp.lerp(a, b, t) = a * (1 - t) + b * t. */
+static inline float adv_lerp(float a, float b, float t) { return a * (1.0f - t) + b * t; }
+
+static inline float adv_min(float a, float b) { return a < b ? a : b; }
+static inline float adv_max(float a, float b) { return a > b ? a : b; }
+
+/* The eight corners (u0|u0+1, v0|v0+1, w0|w0+1) blended with fractions fa, fb,
+ * fc: lerp(lerp(lerp(a,b,fa), lerp(c,d,fa), fb), lerp(lerp(e,f,fa),
+ * lerp(g,h,fa), fb), fc), as utils/util.py:55-88 and :106-120 write it. */
+static float adv_tri8(adv_vol V, int u0, int v0, int w0, float fa, float fb, float fc) {
+    float a = adv_at(V, u0, v0, w0), b = adv_at(V, u0 + 1, v0, w0);
+    float c = adv_at(V, u0, v0 + 1, w0), d = adv_at(V, u0 + 1, v0 + 1, w0);
+    float e = adv_at(V, u0, v0, w0 + 1), f = adv_at(V, u0 + 1, v0, w0 + 1);
+    float g = adv_at(V, u0, v0 + 1, w0 + 1), h = adv_at(V, u0 + 1, v0 + 1, w0 + 1);
+    return adv_lerp(adv_lerp(adv_lerp(a, b, fa), adv_lerp(c, d, fa), fb),
+                    adv_lerp(adv_lerp(e, f, fa), adv_lerp(g, h, fa), fb), fc);
+}
+
+/* utils/util.py:34-88 sample_velocity_3d: the MAC velocity at p (u faces
+ * sit at (i, j+0.5, k+0.5), v faces at (i+0.5, j, k+0.5), w faces at
+ * (i+0.5, j+0.5, k)). */
+static void adv_velocity(adv_vol U, adv_vol V, adv_vol W, const float p[3], float out[3]) {
+    int iu = adv_ifloor(p[0]), iv = adv_ifloor(p[1]), iw = adv_ifloor(p[2]);
+    float fu = p[0] - (float)iu, fv = p[1] - (float)iv, fw = p[2] - (float)iw;
+    float s = p[0] - 0.5f, t = p[1] - 0.5f, r = p[2] - 0.5f;
+    int is = adv_ifloor(s), it = adv_ifloor(t), ir = adv_ifloor(r);
+    float fs = s - (float)is, ft = t - (float)it, fr = r - (float)ir;
+    out[0] = adv_tri8(U, iu, it, ir, fu, ft, fr);
+    out[1] = adv_tri8(V, is, iv, ir, fs, fv, fr);
+    out[2] = adv_tri8(W, is, it, iw, fs, ft, fw);
+}
+
+/* advect.py:10-22 backtrace: three-stage Runge-Kutta (Ralston) from p over
+ * -dt, positions in grid units (velocity / h). */
+static void adv_backtrace(adv_vol U, adv_vol V, adv_vol W, float p[3], float dt, float h) {
+    float v1[3], v2[3], v3[3], p1[3], p2[3];
+    const float c1 = 0.5f * dt / h, c2 = 0.75f * dt / h, c3 = dt / h;
+    const float k1 = 2.0f / 9.0f, k2 = 1.0f / 3.0f, k3 = 4.0f / 9.0f;
+    adv_velocity(U, V, W, p, v1);
+    for (int a = 0; a < 3; a++) p1[a] = p[a] - c1 * v1[a];
+    adv_velocity(U, V, W, p1, v2);
+    for (int a = 0; a < 3; a++) p2[a] = p[a] - c2 * v2[a];
+    adv_velocity(U, V, W, p2, v3);
+    for (int a = 0; a < 3; a++) p[a] = p[a] - c3 * ((k1 * v1[a] + k2 * v2[a]) + k3 * v3[a]);
+}
+
+/* utils/util.py:122-129 cubic: the cubic through (-1, a), (0, b), (1, c),
+ * (2, d) at s; the weights are summed left to right (wp.dot). */
+static float adv_cubic(float a, float b, float c, float d, float s) {
+    const float m13 = -1.0f / 3.0f, k16 = 1.0f / 6.0f;
+    float t0 = (m13 * s + 0.5f * s * s) - k16 * s * s * s;
+    float t1 = (1.0f - s * s) + 0.5f * (s * s * s - s);
+    float t2 = s + 0.5f * (s * s - s * s * s);
+    float t3 = k16 * (s * s * s - s);
+    return ((a * t0 + b * t1) + c * t2) + d * t3;
+}
+
+/* utils/util.py:148-160 _tricubic (with _bicubic :139-146 and _cubic
+ * :131-137): cubic along the first axis innermost, then the second, then the
+ * third, at (s, t, r) in index units. */
+static float adv_tricubic(adv_vol Q, float s, float t, float r) {
+    int iu = adv_ifloor(s), iv = adv_ifloor(t), iw = adv_ifloor(r);
+    float fu = s - (float)iu, fv = t - (float)iv, fw = r - (float)iw;
+    float qw[4];
+    for (int m = 0; m < 4; m++) {
+        float qv[4];
+        for (int n = 0; n < 4; n++) {
+            int b = iv + n - 1, c = iw + m - 1;
+            qv[n] = adv_cubic(adv_at(Q, iu - 1, b, c), adv_at(Q, iu, b, c), adv_at(Q, iu + 1, b, c),
+                              adv_at(Q, iu + 2, b, c), fu);
+        }
+        qw[m] = adv_cubic(qv[0], qv[1], qv[2], qv[3], fv);
+    }
+    return adv_cubic(qw[0], qw[1], qw[2], qw[3], fw);
+}
+
+/* utils/util.py:98-104 trilerp_stagger (the tricubic at p - stagger). */
+static inline float adv_sample_stagger(adv_vol Q, const float p[3], const float st[3]) {
+    return adv_tricubic(Q, p[0] - st[0], p[1] - st[1], p[2] - st[2]);
+}
+
+/* advect.py:103-122 sample_minmax: min and max of the eight values around
+ * floor(p / h - stagger).  The reference passes h0 while p is already in
+ * grid units, so the index is scaled by 1/h0 and clamps to the far corner of
+ * the array for p >= 1; minmax_h = h0 reproduces that, 1 gives the cell
+ * around p. */
+static void adv_minmax(adv_vol Q, const float p[3], float mh, const float st[3], float *mn, float *mx) {
+    int a = adv_ifloor(p[0] / mh - st[0]), b = adv_ifloor(p[1] / mh - st[1]), c = adv_ifloor(p[2] / mh - st[2]);
+    float v0 = adv_at(Q, a, b, c), v1 = adv_at(Q, a + 1, b, c), v2 = adv_at(Q, a, b + 1, c),
+          v3 = adv_at(Q, a + 1, b + 1, c), v4 = adv_at(Q, a, b, c + 1), v5 = adv_at(Q, a + 1, b, c + 1),
+          v6 = adv_at(Q, a, b + 1, c + 1), v7 = adv_at(Q, a + 1, b + 1, c + 1);
+    float lo0 = adv_min(adv_min(adv_min(v0, v1), v2), v3), lo1 = adv_min(adv_min(adv_min(v4, v5), v6), v7);
+    float hi0 = adv_max(adv_max(adv_max(v0, v1), v2), v3), hi1 = adv_max(adv_max(adv_max(v4, v5), v6), v7);
+    *mn = adv_min(lo0, lo1);
+    *mx = adv_max(hi0, hi1);
+}
+
+/* advect.py:57-101 _advect_mc_1 (stage 1), _advect_mc_2 (stage 2),
+ * _advect_mc_3 (stage 3) on a field q of shape (qx, qy, qz) with stagger st,
+ * advected by the MAC velocity (u, v, w) of the cell grid (nx, ny, nz);
+ * stage 0 runs the three in order (advect.py:124-128 advect_mc). */
+void oracle_advect_mc(const float *u, const float *v, const float *w, int nx, int ny, int nz, const float *q_in,
+                      float *q_out, float *q_tmp, int qx, int qy, int qz, const float *st, float dt, float h,
+                      float minmax_h, int stage) {
+    if (stage == 0) {
+        float *tmp = (float *)malloc(sizeof(float) * (size_t)qx * qy * qz);
+        oracle_advect_mc(u, v, w, nx, ny, nz, q_in, q_out, tmp, qx, qy, qz, st, dt, h, minmax_h, 1);
+        oracle_advect_mc(u, v, w, nx, ny, nz, q_in, q_out, tmp, qx, qy, qz, st, dt, h, minmax_h, 2);
+        oracle_advect_mc(u, v, w, nx, ny, nz, q_in, q_out, tmp, qx, qy, qz, st, dt, h, minmax_h, 3);
+        free(tmp);
+        return;
+    }
+    adv_vol U = {u, nx + 1, ny, nz}, V = {v, nx, ny + 1, nz}, W = {w, nx, ny, nz + 1}, Q = {q_in, qx, qy, qz};
+#pragma omp parallel for schedule(static)
+    for (int i = 0; i < qx; i++)
+        for (int j = 0; j < qy; j++)
+            for (int k = 0; k < qz; k++) {
+                int64_t f = ((int64_t)i * qy + j) * qz + k;
+                float p[3] = {(float)i + st[0], (float)j + st[1], (float)k + st[2]};
+                if (stage == 2) {
+                    adv_backtrace(U, V, W, p, -dt, h);
+                    q_tmp[f] = adv_sample_stagger(Q, p, st);
+                    continue;
+                }
+                adv_backtrace(U, V, W, p, dt, h);
+                float q_sl = adv_sample_stagger(Q, p, st);
+                if (stage == 1) {
+                    q_out[f] = q_sl;
+                    continue;
+                }
+                float q = q_out[f] + 0.5f * (q_in[f] - q_tmp[f]);
+                float mn, mx;
+                adv_minmax(Q, p, minmax_h, st, &mn, &mx);
+                q_out[f] = (mn < q && q < mx) ? q : q_sl;
+            }
+}
+
+/* advect.py:39-54 advect_phi: phi (px, py, pz) with stagger st traced back
+ * by the velocity; the tricubic sample where the foot lies inside
+ * [0, p*) on every axis, else `outside` (the reference writes h0). */
+void oracle_advect_phi(const float *u, const float *v, const float *w, int nx, int ny, int nz, const float *phi,
+                       float *phi_out, int px, int py, int pz, const float *st, float dt, float h, float outside) {
+    adv_vol U = {u, nx + 1, ny, nz}, V = {v, nx, ny + 1, nz}, W = {w, nx, ny, nz + 1}, Q = {phi, px, py, pz};
+#pragma omp parallel for schedule(static)
+    for (int i = 0; i < px; i++)
+        for (int j = 0; j < py; j++)
+            for (int k = 0; k < pz; k++) {
+                float p[3] = {(float)i + st[0], (float)j + st[1], (float)k + st[2]};
+                adv_backtrace(U, V, W, p, dt, h);
+                int in = 0.0f <= p[0] && p[0] < (float)px && 0.0f <= p[1] && p[1] < (float)py && 0.0f <= p[2] &&
+                         p[2] < (float)pz;
+                phi_out[((int64_t)i * py + j) * pz + k] = in ? adv_sample_stagger(Q, p, st) : outside;
+            }
+}
+
+/* advect.py:24-37 advect_simple_3d: a cell-centred q traced back from
+ * (i+0.5, j+0.5, k+0.5), sampled trilinearly (utils/util.py:91-96 trilerp). */
+void oracle_advect_simple(const float *u, const float *v, const float *w, int nx, int ny, int nz, const float *q,
+                          float *q_out, int qx, int qy, int qz, float dt, float h) {
+    adv_vol U = {u, nx + 1, ny, nz}, V = {v, nx, ny + 1, nz}, W = {w, nx, ny, nz + 1}, Q = {q, qx, qy, qz};
+#pragma omp parallel for schedule(static)
+    for (int i = 0; i < qx; i++)
+        for (int j = 0; j < qy; j++)
+            for (int k = 0; k < qz; k++) {
+                float p[3] = {(float)i + 0.5f, (float)j + 0.5f, (float)k + 0.5f};
+                adv_backtrace(U, V, W, p, dt, h);
+                float s = p[0] - 0.5f, t = p[1] - 0.5f, r = p[2] - 0.5f;
+                int iu = adv_ifloor(s), iv = adv_ifloor(t), iw = adv_ifloor(r);
+                q_out[((int64_t)i * qy + j) * qz + k] =
+                    adv_tri8(Q, iu, iv, iw, s - (float)iu, t - (float)iv, r - (float)iw);
+            }
+}
+
+/* Single-point probes for known-answer tests. */
+void oracle_sample_velocity(const float *u, const float *v, const float *w, int nx, int ny, int nz, const float *p,
+                            float *out) {
+    adv_vol U = {u, nx + 1, ny, nz}, V = {v, nx, ny + 1, nz}, W = {w, nx, ny, nz + 1};
+    adv_velocity(U, V, W, p, out);
+}
+
+void oracle_backtrace(const float *u, const float *v, const float *w, int nx, int ny, int nz, float *p, float dt,
+                      float h) {
+    adv_vol U = {u, nx + 1, ny, nz}, V = {v, nx, ny + 1, nz}, W = {w, nx, ny, nz + 1};
+    adv_backtrace(U, V, W, p, dt, h);
+}
+
+float oracle_tricubic(const float *q, int qx, int qy, int qz, float s, float t, float r) {
+    adv_vol Q = {q, qx, qy, qz};
+    return adv_tricubic(Q, s, t, r);
+}
+
 /* multigrid/mgpcg.py:360-370 set_tags: coarse tag levels (restrict_tag). */
 void oracle_tag_levels(int32_t **tagl, int levels, int nx, int ny, int nz) {
     for (int l = 0; l + 1 < levels; l++)
