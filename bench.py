@@ -69,7 +69,8 @@ def parse_args():
     ap.add_argument("--no-oracle-check", action="store_true",
                     help="skip the FP64 host projection that checks each variant's pressure")
     ap.add_argument("--no-e2e", action="store_true")
-    ap.add_argument("--profile-kernel", choices=["smooth", "restrict", "matvec", "solve", "project"], default=None,
+    ap.add_argument("--profile-kernel", choices=["smooth", "restrict", "matvec", "solve", "project", "advect"],
+                    default=None,
                     help="set up the 256^3 solver state and launch only this kernel 3 times (for ncu)")
     return ap.parse_args()
 
@@ -97,6 +98,19 @@ def run_profile_kernel(args):
         torch.cuda.synchronize()
         print(json.dumps({"profile_kernel": "project", "variant": args.variant, "iterations": info["iterations"],
                           "ok": bool(info["converged"])}))
+        return 0
+    if args.profile_kernel == "advect":
+        # the step's advection (water_3d.py:34-37) on the scene's velocity:
+        # advect_phi once, then advect_uv_mc (three k_advect_mc<0> launches) twice
+        vel = MACGrid(*(Field(dev(a), d=d + 1) for d, a in enumerate((scene.u, scene.v, scene.w))))
+        new_vel = MACGrid(*(Field(torch.empty_like(a.f), d=d + 1) for d, a in enumerate((vel.u, vel.v, vel.w))))
+        phi = Field(dev(scene.phi))
+        new_phi = Field(torch.empty_like(phi.f))
+        K.advect_phi_field(vel, phi, new_phi)
+        for _ in range(2):
+            K.advect_uv_mc(vel, new_vel)
+        torch.cuda.synchronize()
+        print(json.dumps({"profile_kernel": "advect", "config": args.config, "ok": True}))
         return 0
     tag = K.classify(dev(scene.phi), scene.prims, scene.h, scene.h0)
     vel = MACGrid(*(Field(dev(a), d=d + 1) for d, a in enumerate((scene.u, scene.v, scene.w))))
@@ -484,6 +498,17 @@ def run_ours(args):
                          "once, 20 B per element; the kernels gather about 280 (MacCormack) or 136 (phi) values "
                          "per element through L1, which bounds them"}
 
+    # ---- level-set redistance (redistance.py:125-136, as particles.py:267-270
+    # calls it: set_boundary = 0): _init_distance + 2 x 8 sweeps of 2 halves
+    rd_phi = torch.empty_like(phi)
+    rd_ms = time_ms(lambda: (rd_phi.copy_(phi), K.redistance(rd_phi, None, 0)))
+    copy_ms = time_ms(lambda: rd_phi.copy_(phi))
+    redistance_info = {"ms": rd_ms - copy_ms, "cells": n_cells, "launches": 33,
+                       "ms_per_half_sweep_estimate": (rd_ms - copy_ms) / 33,
+                       "note": "in place through the Python call: the init kernel writes a temporary, the 32 "
+                               "half-sweeps update it, one device copy brings it back; 256^3 FP32 phi (67 MB) "
+                               "stays in L2"}
+
     # ---- CPU baseline: the oracle on the host cores (rank 0, N = 1 only)
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu_baseline and args.cpu_baseline_steps > 0:
@@ -517,7 +542,7 @@ def run_ours(args):
                        "max_abs_div_after": div_after, "l2_flush": "inputs larger than L2 (~1.3 GB working set)",
                        "parallelism": f"replicas x{world}"},
             "roofline": roofline, "cpu_baseline": cpu, "e2e": e2e, "gpu_launches": int(launches),
-            "extrapolation": extrapolation, "advection": advection,
+            "extrapolation": extrapolation, "advection": advection, "redistance": redistance_info,
             "clocks": clocks,
         }
         print(json.dumps(out), flush=True)

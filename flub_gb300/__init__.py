@@ -11,9 +11,9 @@ loaded on first use; there is no CPU fallback.
 """
 from .fields import (DEFAULT_SHAPE, Field, IntField, MACGrid, MACGridInt, field_like, field_shape, get_uf,
                      make_field, make_mac_grid)
-from .kernels import (DT, _advect_mc_1, _advect_mc_2, _advect_mc_3, _tag_dirichlet, _tag_neumann, advect_3d,
+from .kernels import (DT, _advect_mc_1, _advect_mc_2, _advect_mc_3, _init_distance, _sweep, _tag_dirichlet, _tag_neumann, advect_3d,
                       advect_mc, advect_mc_stage, advect_phi, advect_phi_field, advect_simple, advect_simple_3d,
-                      advect_uv_mc, classify, divergence, divergence_fractional,
+                      advect_uv_mc, classify, init_distance, redistance, sweep, sweep_half, divergence, divergence_fractional,
                       divergence_fractional_3d, divergence_tag, extrapolate, extrapolate_3d, extrapolate_by_1,
                       flush_1_3d, launch, mask_with_tag, phi_prims, phi_to_fraction, phi_to_fraction_3d,
                       precompute_grid_point_phi_prims, precompute_solid_vel, scale_by_3d, set_unknown, set_unknown_3d,
@@ -34,4 +34,5 @@ __all__ = [
     "subtract_gradient_batty", "u_subtract_gradient_batty_3d", "v_subtract_gradient_batty_3d",
     "w_subtract_gradient_batty_3d", "DT", "_advect_mc_1", "_advect_mc_2", "_advect_mc_3", "advect_3d", "advect_mc",
     "advect_mc_stage", "advect_phi", "advect_phi_field", "advect_simple", "advect_simple_3d", "advect_uv_mc",
+    "_init_distance", "_sweep", "init_distance", "redistance", "sweep", "sweep_half",
 ]

@@ -67,6 +67,9 @@ SIGNATURES = {
     "flub_advect_phi": (_i32, [_vp, _vp, _vp, _i32, _i32, _i32, _vp, _vp, _i32, _i32, _i32, _f32, _f32, _f32, _f32,
                                _f32, _f32, _vp]),
     "flub_advect_simple": (_i32, [_vp, _vp, _vp, _i32, _i32, _i32, _vp, _vp, _i32, _i32, _i32, _f32, _f32, _vp]),
+    "flub_redistance_init": (_i32, [_vp, _vp, _i32, _i32, _i32, _f32, _i32, _vp]),
+    "flub_redistance_sweep": (_i32, [_vp, _i32, _i32, _i32, _i32, _i32, _i32, _i32, _f32, _vp]),
+    "flub_redistance": (_i32, [_vp, _vp, _i32, _i32, _i32, _f32, _i32, _i32, _vp]),
     "flub_mg_workspace_bytes": (_sz, [_i32, _i32, _i32, _i32, _i32]),
     "flub_mg_create": (_i32, [_i32, _i32, _i32, _i32, _i32, _vp, _sz, ctypes.POINTER(_vp)]),
     "flub_mg_destroy": (_i32, [_vp]),

@@ -11,29 +11,46 @@
 // neighbouring k, so every gather instruction of the trace and the stencils
 // touches one or two cache lines.  The kernels are bound by L1 gather
 // throughput (about 280 loads per MacCormack element), not by HBM.
+#include <cmath>
+
 #include "common.cuh"
 
 namespace flub {
+
+// MAC face arrays of the cell grid (nx, ny, nz) and their strides: u
+// (nx+1, ny, nz), v (nx, ny+1, nz), w (nx, ny, nz+1).
+struct AdvVel {
+    const float *__restrict__ u, *__restrict__ v, *__restrict__ w;
+    int nx, ny, nz;
+};
 
 struct AdvVol {
     const float *__restrict__ q;
     int gx, gy, gz;
 };
 
-struct AdvVel {
-    AdvVol u, v, w;
-};
-
 struct AdvF3 {
     float x, y, z;
 };
 
-__device__ __forceinline__ int adv_clamp(int v, int hi) { return min(max(v, 0), hi); }
+// The trace's step factors (0.5 dt)/h, (0.75 dt)/h and dt/h for +dt and -dt,
+// rounded to FP32 on the host exactly as the kernels would.
+struct AdvSteps {
+    float c1[2], c2[2], c3[2];
+};
 
-// floor as an int, with the argument limited to +-2^30 first (NaN -> -2^30),
-// so that non-finite or absurd positions clamp the same way everywhere.
-__device__ __forceinline__ int adv_ifloor(float x) {
-    return (int)floorf(fminf(fmaxf(x, -1073741824.0f), 1073741824.0f));
+// floor(x) as an int (saturating; NaN -> 0) and the fraction x - floor(x).
+__device__ __forceinline__ int adv_floor(float x) { return __float2int_rd(x); }
+__device__ __forceinline__ float adv_fract(float x) { return __fsub_rn(x, floorf(x)); }
+
+// clamp(i0, 0, hi) and clamp(i0 + 1, 0, hi), without forming i0 + 1.
+struct AdvPair {
+    int a, b;
+};
+
+__device__ __forceinline__ AdvPair adv_pair(int i0, int hi) {
+    const int a = min(max(i0, 0), hi);
+    return AdvPair{a, a + ((unsigned)i0 < (unsigned)hi ? 1 : 0)};
 }
 
 // wp.lerp(a, b, t) = a * (1 - t) + b * t.
@@ -41,41 +58,40 @@ __device__ __forceinline__ float adv_lerp(float a, float b, float t) {
     return __fadd_rn(__fmul_rn(a, __fsub_rn(1.0f, t)), __fmul_rn(b, t));
 }
 
-// The eight corners (u0|u0+1, v0|v0+1, w0|w0+1) blended as utils/util.py:55-88
-// and :106-120 write it: lerp(lerp(lerp(a,b,fa), lerp(c,d,fa), fb),
-// lerp(lerp(e,f,fa), lerp(g,h,fa), fb), fc).
-__device__ __forceinline__ float adv_tri8(const AdvVol &V, int u0, int v0, int w0, float fa, float fb, float fc) {
-    const int ua = adv_clamp(u0, V.gx - 1), ub = adv_clamp(u0 + 1, V.gx - 1);
-    const int va = adv_clamp(v0, V.gy - 1), vb = adv_clamp(v0 + 1, V.gy - 1);
-    const int wa = adv_clamp(w0, V.gz - 1), wb = adv_clamp(w0 + 1, V.gz - 1);
-    const int raa = (ua * V.gy + va) * V.gz, rba = (ub * V.gy + va) * V.gz;
-    const int rab = (ua * V.gy + vb) * V.gz, rbb = (ub * V.gy + vb) * V.gz;
-    const float *q = V.q;
-    const float a = __ldg(q + raa + wa), b = __ldg(q + rba + wa), c = __ldg(q + rab + wa), d = __ldg(q + rbb + wa);
-    const float e = __ldg(q + raa + wb), f = __ldg(q + rba + wb), g = __ldg(q + rab + wb), h = __ldg(q + rbb + wb);
+// The eight corners (x.a|x.b, y.a|y.b, z.a|z.b) of q (plane stride sp, row
+// stride sr) blended as utils/util.py:55-88 and :106-120 write it:
+// lerp(lerp(lerp(a,b,fa), lerp(c,d,fa), fb), lerp(lerp(e,f,fa), lerp(g,h,fa), fb), fc).
+__device__ __forceinline__ float adv_tri8(const float *__restrict__ q, int sp, int sr, AdvPair x, AdvPair y, AdvPair z,
+                                          float fa, float fb, float fc) {
+    const float *paa = q + (x.a * sp + y.a * sr), *pba = q + (x.b * sp + y.a * sr);
+    const float *pab = q + (x.a * sp + y.b * sr), *pbb = q + (x.b * sp + y.b * sr);
+    const float a = __ldg(paa + z.a), b = __ldg(pba + z.a), c = __ldg(pab + z.a), d = __ldg(pbb + z.a);
+    const float e = __ldg(paa + z.b), f = __ldg(pba + z.b), g = __ldg(pab + z.b), h = __ldg(pbb + z.b);
     return adv_lerp(adv_lerp(adv_lerp(a, b, fa), adv_lerp(c, d, fa), fb),
                     adv_lerp(adv_lerp(e, f, fa), adv_lerp(g, h, fa), fb), fc);
 }
 
-// utils/util.py:34-88 sample_velocity_3d.
+// utils/util.py:34-88 sample_velocity_3d.  The three components share their
+// clamped index pairs where their arrays share an extent.
 __device__ __forceinline__ AdvF3 adv_velocity(const AdvVel &M, AdvF3 p) {
-    const int iu = adv_ifloor(p.x), iv = adv_ifloor(p.y), iw = adv_ifloor(p.z);
-    const float fu = __fsub_rn(p.x, (float)iu), fv = __fsub_rn(p.y, (float)iv), fw = __fsub_rn(p.z, (float)iw);
+    const int nx = M.nx, ny = M.ny, nz = M.nz;
     const float s = __fsub_rn(p.x, 0.5f), t = __fsub_rn(p.y, 0.5f), r = __fsub_rn(p.z, 0.5f);
-    const int is = adv_ifloor(s), it = adv_ifloor(t), ir = adv_ifloor(r);
-    const float fs = __fsub_rn(s, (float)is), ft = __fsub_rn(t, (float)it), fr = __fsub_rn(r, (float)ir);
+    const float fu = adv_fract(p.x), fv = adv_fract(p.y), fw = adv_fract(p.z);
+    const float fs = adv_fract(s), ft = adv_fract(t), fr = adv_fract(r);
+    const AdvPair xu = adv_pair(adv_floor(p.x), nx), xs = adv_pair(adv_floor(s), nx - 1);
+    const AdvPair yv = adv_pair(adv_floor(p.y), ny), yt = adv_pair(adv_floor(t), ny - 1);
+    const AdvPair zw = adv_pair(adv_floor(p.z), nz), zr = adv_pair(adv_floor(r), nz - 1);
     AdvF3 o;
-    o.x = adv_tri8(M.u, iu, it, ir, fu, ft, fr);
-    o.y = adv_tri8(M.v, is, iv, ir, fs, fv, fr);
-    o.z = adv_tri8(M.w, is, it, iw, fs, ft, fw);
+    o.x = adv_tri8(M.u, ny * nz, nz, xu, yt, zr, fu, ft, fr);
+    o.y = adv_tri8(M.v, (ny + 1) * nz, nz, xs, yv, zr, fs, fv, fr);
+    o.z = adv_tri8(M.w, ny * (nz + 1), nz + 1, xs, yt, zw, fs, ft, fw);
     return o;
 }
 
-// advect.py:10-22 backtrace: three-stage Runge-Kutta from p over -dt.
-__device__ __forceinline__ AdvF3 adv_backtrace(const AdvVel &M, AdvF3 p, float dt, float h) {
-    const float c1 = __fdiv_rn(__fmul_rn(0.5f, dt), h), c2 = __fdiv_rn(__fmul_rn(0.75f, dt), h), c3 = __fdiv_rn(dt, h);
+// advect.py:10-22 backtrace from p with its first velocity sample v1 given
+// (c1, c2, c3: the step factors of the direction traced).
+__device__ __forceinline__ AdvF3 adv_backtrace_v1(const AdvVel &M, AdvF3 p, AdvF3 v1, float c1, float c2, float c3) {
     const float k1 = 2.0f / 9.0f, k2 = 1.0f / 3.0f, k3 = 4.0f / 9.0f;
-    const AdvF3 v1 = adv_velocity(M, p);
     const AdvF3 p1 = {__fsub_rn(p.x, __fmul_rn(c1, v1.x)), __fsub_rn(p.y, __fmul_rn(c1, v1.y)),
                       __fsub_rn(p.z, __fmul_rn(c1, v1.z))};
     const AdvF3 v2 = adv_velocity(M, p1);
@@ -115,29 +131,30 @@ __device__ __forceinline__ float adv_dot4(float a, float b, float c, float d, co
                      __fmul_rn(d, w.w3));
 }
 
+// clamp(i0 + a - 1, 0, hi) * stride for a = 0..3 (i0 limited to
+// [-2, hi + 2] first, which changes none of the four).
+__device__ __forceinline__ void adv_quad(int i0, int hi, int stride, int o[4]) {
+    const int c = min(max(i0, -2), hi + 2);
+#pragma unroll
+    for (int a = 0; a < 4; a++) o[a] = min(max(c + a - 1, 0), hi) * stride;
+}
+
 // utils/util.py:148-160 _tricubic (with _bicubic :139-146 and _cubic
 // :131-137) at (s, t, r): cubics along the first axis innermost, then the
 // second, then the third.
 __device__ __forceinline__ float adv_tricubic(const AdvVol &Q, float s, float t, float r) {
-    const int iu = adv_ifloor(s), iv = adv_ifloor(t), iw = adv_ifloor(r);
-    const AdvW4 wu = adv_cubic_w(__fsub_rn(s, (float)iu));
-    const AdvW4 wv = adv_cubic_w(__fsub_rn(t, (float)iv));
-    const AdvW4 ww = adv_cubic_w(__fsub_rn(r, (float)iw));
-    const int plane = Q.gy * Q.gz;
+    const AdvW4 wu = adv_cubic_w(adv_fract(s)), wv = adv_cubic_w(adv_fract(t)), ww = adv_cubic_w(adv_fract(r));
     int oi[4], oj[4], ok[4];
-#pragma unroll
-    for (int a = 0; a < 4; a++) {
-        oi[a] = adv_clamp(iu + a - 1, Q.gx - 1) * plane;
-        oj[a] = adv_clamp(iv + a - 1, Q.gy - 1) * Q.gz;
-        ok[a] = adv_clamp(iw + a - 1, Q.gz - 1);
-    }
+    adv_quad(adv_floor(s), Q.gx - 1, Q.gy * Q.gz, oi);
+    adv_quad(adv_floor(t), Q.gy - 1, Q.gz, oj);
+    adv_quad(adv_floor(r), Q.gz - 1, 1, ok);
     float qw[4];
 #pragma unroll
     for (int m = 0; m < 4; m++) {
         float qv[4];
 #pragma unroll
         for (int n = 0; n < 4; n++) {
-            const float *row = Q.q + oj[n] + ok[m];
+            const float *row = Q.q + (oj[n] + ok[m]);
             qv[n] = adv_dot4(__ldg(row + oi[0]), __ldg(row + oi[1]), __ldg(row + oi[2]), __ldg(row + oi[3]), wu);
         }
         qw[m] = adv_dot4(qv[0], qv[1], qv[2], qv[3], wv);
@@ -153,22 +170,27 @@ __device__ __forceinline__ float adv_sample_stagger(const AdvVol &Q, AdvF3 p, Ad
 __device__ __forceinline__ float adv_min(float a, float b) { return a < b ? a : b; }
 __device__ __forceinline__ float adv_max(float a, float b) { return a > b ? a : b; }
 
+// p / mh, as a multiplication when mh is a power of two (inv_mh = 1 / mh,
+// then exact and equal to the quotient), else a division.
+__device__ __forceinline__ float adv_div_mh(float p, float mh, float inv_mh) {
+    return inv_mh != 0.0f ? __fmul_rn(p, inv_mh) : __fdiv_rn(p, mh);
+}
+
 // advect.py:103-122 sample_minmax: min and max of the eight values around
 // floor(p / mh - stagger).  The reference passes h0 as mh while p is already
 // in grid units (so the corner clamps to the far end of the array for
 // p >= 1); mh = 1 gives the cell around p.
-__device__ __forceinline__ void adv_minmax(const AdvVol &Q, AdvF3 p, float mh, AdvF3 st, float &mn, float &mx) {
-    const int a = adv_ifloor(__fsub_rn(__fdiv_rn(p.x, mh), st.x));
-    const int b = adv_ifloor(__fsub_rn(__fdiv_rn(p.y, mh), st.y));
-    const int c = adv_ifloor(__fsub_rn(__fdiv_rn(p.z, mh), st.z));
-    const int ia = adv_clamp(a, Q.gx - 1), ib = adv_clamp(a + 1, Q.gx - 1);
-    const int ja = adv_clamp(b, Q.gy - 1), jb = adv_clamp(b + 1, Q.gy - 1);
-    const int ka = adv_clamp(c, Q.gz - 1), kb = adv_clamp(c + 1, Q.gz - 1);
+__device__ __forceinline__ void adv_minmax(const AdvVol &Q, AdvF3 p, float mh, float inv_mh, AdvF3 st, float &mn,
+                                           float &mx) {
+    const AdvPair x = adv_pair(adv_floor(__fsub_rn(adv_div_mh(p.x, mh, inv_mh), st.x)), Q.gx - 1);
+    const AdvPair y = adv_pair(adv_floor(__fsub_rn(adv_div_mh(p.y, mh, inv_mh), st.y)), Q.gy - 1);
+    const AdvPair z = adv_pair(adv_floor(__fsub_rn(adv_div_mh(p.z, mh, inv_mh), st.z)), Q.gz - 1);
+    const int sp = Q.gy * Q.gz, sr = Q.gz;
     const float *q = Q.q;
-    const int raa = (ia * Q.gy + ja) * Q.gz, rba = (ib * Q.gy + ja) * Q.gz;
-    const int rab = (ia * Q.gy + jb) * Q.gz, rbb = (ib * Q.gy + jb) * Q.gz;
-    const float v0 = __ldg(q + raa + ka), v1 = __ldg(q + rba + ka), v2 = __ldg(q + rab + ka), v3 = __ldg(q + rbb + ka);
-    const float v4 = __ldg(q + raa + kb), v5 = __ldg(q + rba + kb), v6 = __ldg(q + rab + kb), v7 = __ldg(q + rbb + kb);
+    const float *paa = q + (x.a * sp + y.a * sr), *pba = q + (x.b * sp + y.a * sr);
+    const float *pab = q + (x.a * sp + y.b * sr), *pbb = q + (x.b * sp + y.b * sr);
+    const float v0 = __ldg(paa + z.a), v1 = __ldg(pba + z.a), v2 = __ldg(pab + z.a), v3 = __ldg(pbb + z.a);
+    const float v4 = __ldg(paa + z.b), v5 = __ldg(pba + z.b), v6 = __ldg(pab + z.b), v7 = __ldg(pbb + z.b);
     mn = adv_min(adv_min(adv_min(adv_min(v0, v1), v2), v3), adv_min(adv_min(adv_min(v4, v5), v6), v7));
     mx = adv_max(adv_max(adv_max(adv_max(v0, v1), v2), v3), adv_max(adv_max(adv_max(v4, v5), v6), v7));
 }
@@ -179,36 +201,51 @@ __device__ __forceinline__ void adv_minmax(const AdvVol &Q, AdvF3 p, float mh, A
 // strictly between the sample_minmax bounds, else the semi-Lagrangian
 // sample), and STAGE 0: the three in one pass (stage 3 reads back exactly the
 // values stages 1 and 2 wrote, so recomputing them in registers gives the
-// same result without q_tmp).  Grid: row_grid(qx, qy, qz).
+// same result without q_tmp).  The traces over dt and -dt start with the
+// same velocity sample, taken once.  Grid: row_grid(qx, qy, qz).
 template <int STAGE>
 __global__ void __launch_bounds__(kRowThreads) k_advect_mc(const AdvVel M, const AdvVol Q, float *__restrict__ q_out,
-                                                          float *__restrict__ q_tmp, AdvF3 st, float dt, float h,
-                                                          float mh) {
+                                                          float *__restrict__ q_tmp, AdvF3 st, const AdvSteps C,
+                                                          float mh, float inv_mh) {
     const int k = blockIdx.x * blockDim.x + threadIdx.x, j = blockIdx.y, i = blockIdx.z;
     if (k >= Q.gz) return;
     const int f = (i * Q.gy + j) * Q.gz + k;
     const AdvF3 p = {__fadd_rn((float)i, st.x), __fadd_rn((float)j, st.y), __fadd_rn((float)k, st.z)};
-    if (STAGE == 2) {
-        q_tmp[f] = adv_sample_stagger(Q, adv_backtrace(M, p, -dt, h), st);
+    const AdvF3 v1 = adv_velocity(M, p);
+    if (STAGE == 1 || STAGE == 2) {
+        const int s = STAGE - 1;
+        const float q = adv_sample_stagger(Q, adv_backtrace_v1(M, p, v1, C.c1[s], C.c2[s], C.c3[s]), st);
+        (STAGE == 1 ? q_out : q_tmp)[f] = q;
         return;
     }
-    const AdvF3 pf = adv_backtrace(M, p, dt, h);
-    const float q_sl = adv_sample_stagger(Q, pf, st);
-    if (STAGE == 1) {
-        q_out[f] = q_sl;
-        return;
+    // foot over dt (pf) and over -dt (pb), and the tricubic samples there,
+    // as one loop of two so that the code is held once
+    AdvF3 pf = p, pb = p;
+    float q_sl = 0.0f, q_bk = 0.0f;
+#pragma unroll 1
+    for (int s = 0; s < (STAGE == 0 ? 2 : 1); s++) {
+        const AdvF3 e = adv_backtrace_v1(M, p, v1, s ? C.c1[1] : C.c1[0], s ? C.c2[1] : C.c2[0], s ? C.c3[1] : C.c3[0]);
+        const float q = adv_sample_stagger(Q, e, st);
+        if (s == 0) {
+            pf = e;
+            q_sl = q;
+        } else {
+            pb = e;
+            q_bk = q;
+        }
     }
+    (void)pb;
     float qo, qt;
     if (STAGE == 3) {
         qo = q_out[f];
         qt = q_tmp[f];
     } else {
         qo = q_sl;
-        qt = adv_sample_stagger(Q, adv_backtrace(M, p, -dt, h), st);
+        qt = q_bk;
     }
     const float q = __fadd_rn(qo, __fmul_rn(0.5f, __fsub_rn(__ldg(Q.q + f), qt)));
     float mn, mx;
-    adv_minmax(Q, pf, mh, st, mn, mx);
+    adv_minmax(Q, pf, mh, inv_mh, st, mn, mx);
     q_out[f] = (mn < q && q < mx) ? q : q_sl;
 }
 
@@ -216,11 +253,11 @@ __global__ void __launch_bounds__(kRowThreads) k_advect_mc(const AdvVel M, const
 // where it lies inside [0, extent) on every axis, else `outside` (the
 // reference writes h0).  Grid: row_grid(px, py, pz).
 __global__ void __launch_bounds__(kRowThreads) k_advect_phi(const AdvVel M, const AdvVol Q, float *__restrict__ out,
-                                                           AdvF3 st, float dt, float h, float outside) {
+                                                           AdvF3 st, const AdvSteps C, float outside) {
     const int k = blockIdx.x * blockDim.x + threadIdx.x, j = blockIdx.y, i = blockIdx.z;
     if (k >= Q.gz) return;
     const AdvF3 p0 = {__fadd_rn((float)i, st.x), __fadd_rn((float)j, st.y), __fadd_rn((float)k, st.z)};
-    const AdvF3 p = adv_backtrace(M, p0, dt, h);
+    const AdvF3 p = adv_backtrace_v1(M, p0, adv_velocity(M, p0), C.c1[0], C.c2[0], C.c3[0]);
     const bool in = 0.0f <= p.x && p.x < (float)Q.gx && 0.0f <= p.y && p.y < (float)Q.gy && 0.0f <= p.z &&
                     p.z < (float)Q.gz;
     out[(i * Q.gy + j) * Q.gz + k] = in ? adv_sample_stagger(Q, p, st) : outside;
@@ -230,23 +267,42 @@ __global__ void __launch_bounds__(kRowThreads) k_advect_phi(const AdvVel M, cons
 // (i+0.5, j+0.5, k+0.5) and sampled trilinearly (utils/util.py:91-96
 // trilerp).  Grid: row_grid(qx, qy, qz).
 __global__ void __launch_bounds__(kRowThreads) k_advect_simple(const AdvVel M, const AdvVol Q, float *__restrict__ out,
-                                                              float dt, float h) {
+                                                              const AdvSteps C) {
     const int k = blockIdx.x * blockDim.x + threadIdx.x, j = blockIdx.y, i = blockIdx.z;
     if (k >= Q.gz) return;
     const AdvF3 p0 = {__fadd_rn((float)i, 0.5f), __fadd_rn((float)j, 0.5f), __fadd_rn((float)k, 0.5f)};
-    const AdvF3 p = adv_backtrace(M, p0, dt, h);
+    const AdvF3 p = adv_backtrace_v1(M, p0, adv_velocity(M, p0), C.c1[0], C.c2[0], C.c3[0]);
     const float s = __fsub_rn(p.x, 0.5f), t = __fsub_rn(p.y, 0.5f), r = __fsub_rn(p.z, 0.5f);
-    const int iu = adv_ifloor(s), iv = adv_ifloor(t), iw = adv_ifloor(r);
     out[(i * Q.gy + j) * Q.gz + k] =
-        adv_tri8(Q, iu, iv, iw, __fsub_rn(s, (float)iu), __fsub_rn(t, (float)iv), __fsub_rn(r, (float)iw));
+        adv_tri8(Q.q, Q.gy * Q.gz, Q.gz, adv_pair(adv_floor(s), Q.gx - 1), adv_pair(adv_floor(t), Q.gy - 1),
+                 adv_pair(adv_floor(r), Q.gz - 1), adv_fract(s), adv_fract(t), adv_fract(r));
 }
 
 static inline AdvVel make_vel(const float *u, const float *v, const float *w, int nx, int ny, int nz) {
-    AdvVel M;
-    M.u = AdvVol{u, nx + 1, ny, nz};
-    M.v = AdvVol{v, nx, ny + 1, nz};
-    M.w = AdvVol{w, nx, ny, nz + 1};
-    return M;
+    return AdvVel{u, v, w, nx, ny, nz};
+}
+
+// The step factors of advect.py:16-21 for +dt (index 0) and -dt (index 1),
+// each product and quotient rounded to FP32 as in the kernels.
+static AdvSteps make_steps(float dt, float h) {
+    AdvSteps C;
+    for (int s = 0; s < 2; s++) {
+        const float d = s ? -dt : dt;
+        volatile float half = 0.5f * d, three_q = 0.75f * d;
+        volatile float c1 = half / h, c2 = three_q / h, c3 = d / h;
+        C.c1[s] = c1;
+        C.c2[s] = c2;
+        C.c3[s] = c3;
+    }
+    return C;
+}
+
+// 1 / mh when mh is a power of two (so that p * (1 / mh) == p / mh), else 0.
+static float pow2_inverse(float mh) {
+    int e = 0;
+    const float m = std::frexp(mh, &e);
+    if (std::fabs(m) != 0.5f || e < -120 || e > 120) return 0.0f;
+    return std::ldexp(m > 0 ? 1.0f : -1.0f, 1 - e);
 }
 
 // Element counts stay below 2^31 so that the kernels index with int.
@@ -258,11 +314,13 @@ static int launch_mc(const AdvVel &M, const float *q_in, float *q_out, float *q_
                      float dt, float h, float mh, int stage, cudaStream_t s) {
     const AdvVol Q{q_in, qx, qy, qz};
     const dim3 g = row_grid(qx, qy, qz);
+    const AdvSteps C = make_steps(dt, h);
+    const float inv = pow2_inverse(mh);
     switch (stage) {
-        case 0: k_advect_mc<0><<<g, kRowThreads, 0, s>>>(M, Q, q_out, q_tmp, st, dt, h, mh); break;
-        case 1: k_advect_mc<1><<<g, kRowThreads, 0, s>>>(M, Q, q_out, q_tmp, st, dt, h, mh); break;
-        case 2: k_advect_mc<2><<<g, kRowThreads, 0, s>>>(M, Q, q_out, q_tmp, st, dt, h, mh); break;
-        default: k_advect_mc<3><<<g, kRowThreads, 0, s>>>(M, Q, q_out, q_tmp, st, dt, h, mh); break;
+        case 0: k_advect_mc<0><<<g, kRowThreads, 0, s>>>(M, Q, q_out, q_tmp, st, C, mh, inv); break;
+        case 1: k_advect_mc<1><<<g, kRowThreads, 0, s>>>(M, Q, q_out, q_tmp, st, C, mh, inv); break;
+        case 2: k_advect_mc<2><<<g, kRowThreads, 0, s>>>(M, Q, q_out, q_tmp, st, C, mh, inv); break;
+        default: k_advect_mc<3><<<g, kRowThreads, 0, s>>>(M, Q, q_out, q_tmp, st, C, mh, inv); break;
     }
     FLUB_CHECK_LAUNCH();
     return FLUB_OK;
@@ -316,7 +374,8 @@ int flub_advect_phi(const float *u, const float *v, const float *w, int nx, int 
     FLUB_REQUIRE(adv_shape_ok(px, py, pz), "flub_advect_phi: bad field shape %dx%dx%d", px, py, pz);
     FLUB_REQUIRE(h > 0.0f, "flub_advect_phi: h must be > 0");
     k_advect_phi<<<row_grid(px, py, pz), kRowThreads, 0, as_stream(stream)>>>(
-        make_vel(u, v, w, nx, ny, nz), AdvVol{phi, px, py, pz}, phi_out, AdvF3{sx, sy, sz}, dt, h, outside);
+        make_vel(u, v, w, nx, ny, nz), AdvVol{phi, px, py, pz}, phi_out, AdvF3{sx, sy, sz}, make_steps(dt, h),
+        outside);
     FLUB_CHECK_LAUNCH();
     return FLUB_OK;
 }
@@ -328,8 +387,8 @@ int flub_advect_simple(const float *u, const float *v, const float *w, int nx, i
     FLUB_REQUIRE(adv_shape_ok(nx + 1, ny + 1, nz + 1), "flub_advect_simple: bad velocity grid %dx%dx%d", nx, ny, nz);
     FLUB_REQUIRE(adv_shape_ok(qx, qy, qz), "flub_advect_simple: bad field shape %dx%dx%d", qx, qy, qz);
     FLUB_REQUIRE(h > 0.0f, "flub_advect_simple: h must be > 0");
-    k_advect_simple<<<row_grid(qx, qy, qz), kRowThreads, 0, as_stream(stream)>>>(make_vel(u, v, w, nx, ny, nz),
-                                                                                 AdvVol{q, qx, qy, qz}, q_out, dt, h);
+    k_advect_simple<<<row_grid(qx, qy, qz), kRowThreads, 0, as_stream(stream)>>>(
+        make_vel(u, v, w, nx, ny, nz), AdvVol{q, qx, qy, qz}, q_out, make_steps(dt, h));
     FLUB_CHECK_LAUNCH();
     return FLUB_OK;
 }

@@ -359,6 +359,45 @@ def advect_simple(uf, vf, wf, qf, new_qf, dt, h):
               float(h), _stream())
 
 
+# ------------------------------------------------------------------ level-set redistance
+
+def init_distance(phi, h, set_boundary=1, out=None):
+    """redistance.py:66-119 _init_distance.  Every cell reads the values from
+    before the call; with out=None phi is updated (through a temporary)."""
+    pf = _f(phi)
+    shape = tuple(pf.shape)
+    dst = torch.empty_like(pf) if out is None else _f(out)
+    _lib.call("flub_redistance_init", _ptr(pf, torch.float32, shape, "phi"), _ptr(dst, torch.float32, shape, "out"),
+              *shape, float(h), int(bool(set_boundary)), _stream())
+    if out is None:
+        pf.copy_(dst)
+
+
+def sweep_half(phi, incx, incy, incz, odd, h):
+    """redistance.py:58-63 _sweep: one red-black half of a sweep, in place."""
+    pf = _f(phi)
+    _lib.call("flub_redistance_sweep", _ptr(pf, torch.float32, name="phi"), *pf.shape, int(incx), int(incy),
+              int(incz), int(odd), float(h), _stream())
+
+
+def sweep(phi, h, incx, incy, incz):
+    """redistance.py:121-123 sweep: both halves."""
+    for odd in (0, 1):
+        sweep_half(phi, incx, incy, incz, odd, h)
+
+
+def redistance(phi, h=None, set_boundary=1, n_rounds=2):
+    """redistance.py:125-136 redistance(phi, h=h0, set_boundary=1), in place
+    (h defaults to 1 / nx, const_param.py h0)."""
+    pf = _f(phi)
+    shape = tuple(pf.shape)
+    hh = float(h) if h is not None else 1.0 / shape[0]
+    tmp = torch.empty_like(pf)
+    _lib.call("flub_redistance", _ptr(pf, torch.float32, shape, "phi"), _ptr(tmp, torch.float32, shape, "tmp"),
+              *shape, hh, int(bool(set_boundary)), int(n_rounds), _stream())
+    pf.copy_(tmp)
+
+
 # ------------------------------------------------------------------ wp.launch mirror
 
 class Kernel:
@@ -439,6 +478,9 @@ _advect_mc_2 = Kernel("_advect_mc_2", lambda vel, qi, qo, qt: advect_mc_stage(ve
 _advect_mc_3 = Kernel("_advect_mc_3", lambda vel, qi, qo, qt: advect_mc_stage(vel, qi, qo, qt, 3), _dim_of(1))
 advect_phi = Kernel("advect_phi", advect_phi_field, _dim_of(1))
 advect_simple_3d = Kernel("advect_simple_3d", advect_simple, _dim_of(3))
+# redistance.py kernels: inputs=[phi, h, set_boundary] / [phi, incx, incy, incz, odd, h]
+_init_distance = Kernel("_init_distance", lambda phi, h, sb: init_distance(phi, h, sb), _dim_of(0))
+_sweep = Kernel("_sweep", sweep_half, _dim_of(0))
 
 
 def launch(kernel, dim, inputs, device=None, stream=None):

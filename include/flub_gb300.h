@@ -209,6 +209,27 @@ int flub_advect_phi(const float *u, const float *v, const float *w, int nx, int 
 int flub_advect_simple(const float *u, const float *v, const float *w, int nx, int ny, int nz, const float *q,
                        float *q_out, int qx, int qy, int qz, float dt, float h, void *stream);
 
+/* ---------------------------------------------------------------- redistance */
+
+/* redistance.py:66-119 _init_distance on phi (nx, ny, nz) into out: cells
+ * next to a sign change get +-h times the smallest face fraction
+ * (utils/util.py:403-412), other cells +-2; boundary cells keep phi unless
+ * set_boundary.  Every cell reads the values from before the call (the
+ * reference rewrites phi in place inside one launch, a data race). */
+int flub_redistance_init(const float *phi, float *out, int nx, int ny, int nz, float h, int set_boundary,
+                         void *stream);
+
+/* redistance.py:58-63 _sweep(phi, incx, incy, incz, odd, h), in place: one
+ * red-black half of a fast sweep in direction (incx, incy, incz) = +-1. */
+int flub_redistance_sweep(float *phi, int nx, int ny, int nz, int incx, int incy, int incz, int odd, float h,
+                          void *stream);
+
+/* redistance.py:125-136 redistance: _init_distance from phi into phi_out,
+ * then n_rounds (the reference: 2) rounds of the eight sweep directions on
+ * phi_out. */
+int flub_redistance(const float *phi, float *phi_out, int nx, int ny, int nz, float h, int set_boundary, int n_rounds,
+                    void *stream);
+
 /* ---------------------------------------------------------------- MGPCG */
 
 /* multigrid/mgpcg.py:234-490 class MGPCG.  One handle = one level hierarchy

@@ -87,6 +87,9 @@ def _declare(L):
     L.oracle_backtrace.argtypes = [vp, vp, vp, i32, i32, i32, vp, f32, f32]
     L.oracle_tricubic.argtypes = [vp, i32, i32, i32, f32, f32, f32]
     L.oracle_tricubic.restype = f32
+    L.oracle_redistance_init.argtypes = [vp, vp, i32, i32, i32, f32, i32]
+    L.oracle_redistance_sweep.argtypes = [vp, i32, i32, i32, i32, i32, i32, i32, f32]
+    L.oracle_redistance.argtypes = [vp, i32, i32, i32, f32, i32, i32]
 
 
 REFERENCE_SCHEDULE = (-1, 3, 1.0)
@@ -344,6 +347,34 @@ def tricubic(q, s, t, r):
     """utils/util.py:148-160 _tricubic at index-space point (s, t, r)."""
     q = _c(q, np.float32)
     return float(lib().oracle_tricubic(_ptr(q), *q.shape, s, t, r))
+
+
+# ---------------------------------------------------------------- redistance
+
+REDISTANCE_DIRECTIONS = ((1, 1, -1), (-1, 1, -1), (-1, -1, -1), (1, -1, -1),
+                         (1, 1, 1), (-1, 1, 1), (-1, -1, 1), (1, -1, 1))
+
+
+def redistance_init(phi, h, set_boundary=1):
+    """redistance.py:66-119 _init_distance (every cell reads the values from
+    before the launch); returns a new array."""
+    phi = _c(phi, np.float32)
+    out = np.empty_like(phi)
+    lib().oracle_redistance_init(_ptr(phi), _ptr(out), *phi.shape, h, int(set_boundary))
+    return out
+
+
+def redistance_sweep(phi, incx, incy, incz, odd, h):
+    """redistance.py:58-63 _sweep, in place."""
+    assert phi.dtype == np.float32 and phi.flags.c_contiguous
+    lib().oracle_redistance_sweep(_ptr(phi), *phi.shape, incx, incy, incz, int(odd), h)
+
+
+def redistance(phi, h, set_boundary=1, n_rounds=2):
+    """redistance.py:125-136 redistance; returns a new array."""
+    out = _c(phi, np.float32).copy()
+    lib().oracle_redistance(_ptr(out), *out.shape, h, int(set_boundary), int(n_rounds))
+    return out
 
 
 # ---------------------------------------------------------------- multigrid

@@ -451,16 +451,27 @@ typedef struct {
     int gx, gy, gz;
 } adv_vol;
 
-static inline float adv_at(adv_vol V, int u, int v, int w) {
-    u = clampi(u, 0, V.gx - 1);
-    v = clampi(v, 0, V.gy - 1);
-    w = clampi(w, 0, V.gz - 1);
-    return V.q[((int64_t)u * V.gy + v) * V.gz + w];
+static inline int64_t adv_clamp64(int64_t v, int64_t hi) { return v < 0 ? 0 : (v > hi ? hi : v); }
+
+/* Indices are int64 so that an index +- 2 never overflows. */
+static inline float adv_at(adv_vol V, int64_t u, int64_t v, int64_t w) {
+    u = adv_clamp64(u, V.gx - 1);
+    v = adv_clamp64(v, V.gy - 1);
+    w = adv_clamp64(w, V.gz - 1);
+    return V.q[(u * V.gy + v) * V.gz + w];
 }
 
-/* floor as an int, with the argument limited to +-2^30 first (NaN -> -2^30),
- * so that non-finite or absurd positions clamp the same way everywhere. */
-static inline int adv_ifloor(float x) { return (int)floorf(fminf(fmaxf(x, -1073741824.0f), 1073741824.0f)); }
+/* floor(x) as an int, saturating at the int range, NaN -> 0 (what a CUDA
+ * float-to-int conversion gives), and the fraction x - floor(x) (equal to the
+ * reference's x - float(int(floor(x))) wherever the int is exact). */
+static inline int adv_ifloor(float x) {
+    if (isnan(x)) return 0;
+    float f = floorf(x);
+    if (f >= 2147483648.0f) return INT32_MAX;
+    if (f < -2147483648.0f) return INT32_MIN;
+    return (int)f;
+}
+static inline float adv_fract(float x) { return x - floorf(x); }
 
 /* wp.lerp(a, b, t) = a * (1 - t) + b * t. */
 static inline float adv_lerp(float a, float b, float t) { return a * (1.0f - t) + b * t; }
@@ -471,7 +482,7 @@ static inline float adv_max(float a, float b) { return a > b ? a : b; }
 /* The eight corners (u0|u0+1, v0|v0+1, w0|w0+1) blended with fractions fa, fb,
  * fc: lerp(lerp(lerp(a,b,fa), lerp(c,d,fa), fb), lerp(lerp(e,f,fa),
  * lerp(g,h,fa), fb), fc), as utils/util.py:55-88 and :106-120 write it. */
-static float adv_tri8(adv_vol V, int u0, int v0, int w0, float fa, float fb, float fc) {
+static float adv_tri8(adv_vol V, int64_t u0, int64_t v0, int64_t w0, float fa, float fb, float fc) {
     float a = adv_at(V, u0, v0, w0), b = adv_at(V, u0 + 1, v0, w0);
     float c = adv_at(V, u0, v0 + 1, w0), d = adv_at(V, u0 + 1, v0 + 1, w0);
     float e = adv_at(V, u0, v0, w0 + 1), f = adv_at(V, u0 + 1, v0, w0 + 1);
@@ -485,10 +496,10 @@ static float adv_tri8(adv_vol V, int u0, int v0, int w0, float fa, float fb, flo
  * (i+0.5, j+0.5, k)). */
 static void adv_velocity(adv_vol U, adv_vol V, adv_vol W, const float p[3], float out[3]) {
     int iu = adv_ifloor(p[0]), iv = adv_ifloor(p[1]), iw = adv_ifloor(p[2]);
-    float fu = p[0] - (float)iu, fv = p[1] - (float)iv, fw = p[2] - (float)iw;
+    float fu = adv_fract(p[0]), fv = adv_fract(p[1]), fw = adv_fract(p[2]);
     float s = p[0] - 0.5f, t = p[1] - 0.5f, r = p[2] - 0.5f;
     int is = adv_ifloor(s), it = adv_ifloor(t), ir = adv_ifloor(r);
-    float fs = s - (float)is, ft = t - (float)it, fr = r - (float)ir;
+    float fs = adv_fract(s), ft = adv_fract(t), fr = adv_fract(r);
     out[0] = adv_tri8(U, iu, it, ir, fu, ft, fr);
     out[1] = adv_tri8(V, is, iv, ir, fs, fv, fr);
     out[2] = adv_tri8(W, is, it, iw, fs, ft, fw);
@@ -523,13 +534,13 @@ static float adv_cubic(float a, float b, float c, float d, float s) {
  * :131-137): cubic along the first axis innermost, then the second, then the
  * third, at (s, t, r) in index units. */
 static float adv_tricubic(adv_vol Q, float s, float t, float r) {
-    int iu = adv_ifloor(s), iv = adv_ifloor(t), iw = adv_ifloor(r);
-    float fu = s - (float)iu, fv = t - (float)iv, fw = r - (float)iw;
+    int64_t iu = adv_ifloor(s), iv = adv_ifloor(t), iw = adv_ifloor(r);
+    float fu = adv_fract(s), fv = adv_fract(t), fw = adv_fract(r);
     float qw[4];
     for (int m = 0; m < 4; m++) {
         float qv[4];
         for (int n = 0; n < 4; n++) {
-            int b = iv + n - 1, c = iw + m - 1;
+            int64_t b = iv + n - 1, c = iw + m - 1;
             qv[n] = adv_cubic(adv_at(Q, iu - 1, b, c), adv_at(Q, iu, b, c), adv_at(Q, iu + 1, b, c),
                               adv_at(Q, iu + 2, b, c), fu);
         }
@@ -549,7 +560,7 @@ static inline float adv_sample_stagger(adv_vol Q, const float p[3], const float 
  * the array for p >= 1; minmax_h = h0 reproduces that, 1 gives the cell
  * around p. */
 static void adv_minmax(adv_vol Q, const float p[3], float mh, const float st[3], float *mn, float *mx) {
-    int a = adv_ifloor(p[0] / mh - st[0]), b = adv_ifloor(p[1] / mh - st[1]), c = adv_ifloor(p[2] / mh - st[2]);
+    int64_t a = adv_ifloor(p[0] / mh - st[0]), b = adv_ifloor(p[1] / mh - st[1]), c = adv_ifloor(p[2] / mh - st[2]);
     float v0 = adv_at(Q, a, b, c), v1 = adv_at(Q, a + 1, b, c), v2 = adv_at(Q, a, b + 1, c),
           v3 = adv_at(Q, a + 1, b + 1, c), v4 = adv_at(Q, a, b, c + 1), v5 = adv_at(Q, a + 1, b, c + 1),
           v6 = adv_at(Q, a, b + 1, c + 1), v7 = adv_at(Q, a + 1, b + 1, c + 1);
@@ -629,9 +640,8 @@ void oracle_advect_simple(const float *u, const float *v, const float *w, int nx
                 float p[3] = {(float)i + 0.5f, (float)j + 0.5f, (float)k + 0.5f};
                 adv_backtrace(U, V, W, p, dt, h);
                 float s = p[0] - 0.5f, t = p[1] - 0.5f, r = p[2] - 0.5f;
-                int iu = adv_ifloor(s), iv = adv_ifloor(t), iw = adv_ifloor(r);
                 q_out[((int64_t)i * qy + j) * qz + k] =
-                    adv_tri8(Q, iu, iv, iw, s - (float)iu, t - (float)iv, r - (float)iw);
+                    adv_tri8(Q, adv_ifloor(s), adv_ifloor(t), adv_ifloor(r), adv_fract(s), adv_fract(t), adv_fract(r));
             }
 }
 
@@ -651,6 +661,127 @@ void oracle_backtrace(const float *u, const float *v, const float *w, int nx, in
 float oracle_tricubic(const float *q, int qx, int qy, int qz, float s, float t, float r) {
     adv_vol Q = {q, qx, qy, qz};
     return adv_tricubic(Q, s, t, r);
+}
+
+/* ---------------- level-set redistance ----------------
+ * FP32 in the reference's operation order; x ** 2.0 is x * x; wp.min / wp.max
+ * of two values are a < b ? a : b and a > b ? a : b; a vector's min / max
+ * scans its components in order. */
+
+static inline float rd_min(float a, float b) { return a < b ? a : b; }
+static inline float rd_max(float a, float b) { return a > b ? a : b; }
+
+/* redistance.py:66-119 _init_distance.  The reference rewrites phi in place
+ * inside one launch, so a cell can read neighbours another thread has already
+ * rewritten; here every cell reads the values from before the launch (phi) and
+ * the results go to out.  Neighbours outside the grid read 0.5 h (the clamped
+ * sample is replaced on each boundary side).  The neighbour test keeps the
+ * reference's precedence: (!boundary && left) || right || bottom || ... */
+void oracle_redistance_init(const float *phi, float *out, int nx, int ny, int nz, float h, int set_boundary) {
+#pragma omp parallel for schedule(static)
+    for (int i = 0; i < nx; i++)
+        for (int j = 0; j < ny; j++)
+            for (int k = 0; k < nz; k++) {
+                const float hb = 0.5f * h;
+                float pl = i > 0 ? phi[IX(i - 1, j, k)] : hb, pr = i < nx - 1 ? phi[IX(i + 1, j, k)] : hb;
+                float pb = j > 0 ? phi[IX(i, j - 1, k)] : hb, pt = j < ny - 1 ? phi[IX(i, j + 1, k)] : hb;
+                float pf = k > 0 ? phi[IX(i, j, k - 1)] : hb, pn = k < nz - 1 ? phi[IX(i, j, k + 1)] : hb;
+                float pc = phi[IX(i, j, k)];
+                int bnd = i == 0 || i == nx - 1 || j == 0 || j == ny - 1 || k == 0 || k == nz - 1;
+                float v = pc;
+                if (bnd && !set_boundary) {
+                    v = pc;
+                } else if (pc > 0.0f) {
+                    if ((!bnd && pl < 0.0f) || pr < 0.0f || pb < 0.0f || pt < 0.0f || pf < 0.0f || pn < 0.0f) {
+                        float f[6] = {1.0f - frac_fluid(pc, pl), 1.0f - frac_fluid(pc, pr), 1.0f - frac_fluid(pc, pb),
+                                      1.0f - frac_fluid(pc, pt), 1.0f - frac_fluid(pc, pf), 1.0f - frac_fluid(pc, pn)};
+                        float m = f[0];
+                        for (int a = 1; a < 6; a++) m = rd_min(m, f[a]);
+                        v = h * m;
+                    } else {
+                        v = 2.0f;
+                    }
+                } else if (pc < 0.0f) {
+                    if ((!bnd && pl > 0.0f) || pr > 0.0f || pb > 0.0f || pt > 0.0f || pf > 0.0f || pn > 0.0f) {
+                        float f[6] = {frac_fluid(pc, pl), frac_fluid(pc, pr), frac_fluid(pc, pb),
+                                      frac_fluid(pc, pt), frac_fluid(pc, pf), frac_fluid(pc, pn)};
+                        float m = f[0];
+                        for (int a = 1; a < 6; a++) m = rd_min(m, f[a]);
+                        v = -h * m;
+                    } else {
+                        v = -2.0f;
+                    }
+                }
+                out[IX(i, j, k)] = v;
+            }
+}
+
+/* redistance.py:7-55 update at cell (i, j, k) for sweep direction
+ * (incx, incy, incz): the upwind-sorted neighbour values, the 1-, 2- or
+ * 3-neighbour Eikonal solution, kept if smaller than |phi|. */
+static void rd_update(float *phi, int nx, int ny, int nz, int i, int j, int k, int incx, int incy, int incz, float h) {
+    int bnd = i == 0 || i == nx - 1 || j == 0 || j == ny - 1 || k == 0 || k == nz - 1;
+    float pc = phi[IX(i, j, k)];
+    if (!(fabsf(pc) > h) || bnd) return;
+    float phii = phi[IX(i - incx, j, k)], phij = phi[IX(i, j - incy, k)], phik = phi[IX(i, j, k - incz)];
+    float phiii = phi[IX(i + incx, j, k)], phijj = phi[IX(i, j + incy, k)], phikk = phi[IX(i, j, k + incz)];
+    float sgn = 1.0f;
+    if (phii < 0.0f) {
+        phii = -rd_max(phii, phiii);
+        phij = -rd_max(phij, phijj);
+        phik = -rd_max(phik, phikk);
+        sgn = -1.0f;
+    } else {
+        phii = rd_min(phii, phiii);
+        phij = rd_min(phij, phijj);
+        phik = rd_min(phik, phikk);
+    }
+    float phi0 = rd_min(rd_min(phii, phij), phik);
+    float phi2 = rd_max(rd_max(phii, phij), phik);
+    float phi1 = (((phii + phij) + phik) - phi0) - phi2;
+    float d = phi0 + h;
+    if (d > phi1) {
+        float e = phi0 - phi1;
+        d = 0.5f * ((phi0 + phi1) + sqrtf((2.0f * h) * h - e * e));
+        if (d > phi2) {
+            float s = (phi0 + phi1) + phi2;
+            float term = s * s - 3.0f * (((phi0 * phi0 + phi1 * phi1) + phi2 * phi2) - h * h);
+            d = (1.0f / 3.0f) * (((phi0 + phi1) + phi2) + sqrtf(rd_max(0.0f, term)));
+        }
+    }
+    phi[IX(i, j, k)] = sgn * rd_min(d, fabsf(pc));
+}
+
+/* redistance.py:58-63 _sweep: the reference's thread (a, b, c) with
+ * (a + b + c) % 2 == odd updates the cell (a, b, c) mirrored on every axis
+ * whose increment is negative.  A cell reads only its six neighbours, all of
+ * the other parity, so the cells of one launch can be visited in any order. */
+void oracle_redistance_sweep(float *phi, int nx, int ny, int nz, int incx, int incy, int incz, int odd, float h) {
+#pragma omp parallel for schedule(static)
+    for (int a = 0; a < nx; a++)
+        for (int b = 0; b < ny; b++)
+            for (int c = 0; c < nz; c++) {
+                if ((a + b + c) % 2 != odd) continue;
+                int i = incx < 0 ? nx - 1 - a : a, j = incy < 0 ? ny - 1 - b : b, k = incz < 0 ? nz - 1 - c : c;
+                rd_update(phi, nx, ny, nz, i, j, k, incx, incy, incz, h);
+            }
+}
+
+/* redistance.py:121-136 redistance: _init_distance, then n_rounds times the
+ * eight sweep directions, each as two launches (odd = 0, 1). */
+static const int RD_DIRS[8][3] = {{1, 1, -1}, {-1, 1, -1}, {-1, -1, -1}, {1, -1, -1},
+                                  {1, 1, 1},  {-1, 1, 1},  {-1, -1, 1},  {1, -1, 1}};
+
+void oracle_redistance(float *phi, int nx, int ny, int nz, float h, int set_boundary, int n_rounds) {
+    size_t n = (size_t)nx * ny * nz;
+    float *tmp = (float *)malloc(n * sizeof(float));
+    oracle_redistance_init(phi, tmp, nx, ny, nz, h, set_boundary);
+    memcpy(phi, tmp, n * sizeof(float));
+    free(tmp);
+    for (int r = 0; r < n_rounds; r++)
+        for (int s = 0; s < 8; s++)
+            for (int odd = 0; odd < 2; odd++)
+                oracle_redistance_sweep(phi, nx, ny, nz, RD_DIRS[s][0], RD_DIRS[s][1], RD_DIRS[s][2], odd, h);
 }
 
 /* multigrid/mgpcg.py:360-370 set_tags: coarse tag levels (restrict_tag). */

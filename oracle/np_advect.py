@@ -8,7 +8,8 @@ advect_uv_mc); utils/util.py:20-28 (sample_3d), :34-88 (sample_velocity_3d),
 :91-120 (trilerp, trilerp_stagger, _trilerp), :122-160 (cubic, _cubic,
 _bicubic, _tricubic).  Every operation is a float32 NumPy operation (rounded
 on its own; NumPy does not contract a*b+c), with wp.lerp(a, b, t) =
-a*(1-t) + b*t.  Indices: floor of the position limited to +-2^30.
+a*(1-t) + b*t.  Indices: floor of the position, saturating at the int32
+range (NaN -> 0); fractions x - floor(x).
 """
 import numpy as np
 
@@ -16,7 +17,14 @@ F = np.float32
 
 
 def _ifloor(x):
-    return np.floor(np.fmin(np.fmax(x, F(-2.0 ** 30)), F(2.0 ** 30))).astype(np.int64)
+    """floor as an integer, saturating at the int32 range, NaN -> 0."""
+    f = np.floor(x).astype(np.float64)
+    f = np.where(np.isnan(f), 0.0, np.clip(f, -2.0 ** 31, 2.0 ** 31 - 1))
+    return f.astype(np.int64)
+
+
+def _fract(x):
+    return x - np.floor(x)
 
 
 def _at(q, a, b, c):
@@ -40,10 +48,10 @@ def sample_velocity(u, v, w, p):
     """utils/util.py:34-88 at points p = (x, y, z) (float32 arrays)."""
     x, y, z = p
     iu, iv, iw = _ifloor(x), _ifloor(y), _ifloor(z)
-    fu, fv, fw = x - iu.astype(F), y - iv.astype(F), z - iw.astype(F)
+    fu, fv, fw = _fract(x), _fract(y), _fract(z)
     s, t, r = x - F(0.5), y - F(0.5), z - F(0.5)
     i_s, i_t, i_r = _ifloor(s), _ifloor(t), _ifloor(r)
-    fs, ft, fr = s - i_s.astype(F), t - i_t.astype(F), r - i_r.astype(F)
+    fs, ft, fr = _fract(s), _fract(t), _fract(r)
     return (_tri8(u, iu, i_t, i_r, fu, ft, fr), _tri8(v, i_s, iv, i_r, fs, fv, fr), _tri8(w, i_s, i_t, iw, fs, ft, fw))
 
 
@@ -74,7 +82,7 @@ def _cubic(a, b, c, d, s):
 def tricubic(q, s, t, r):
     """utils/util.py:148-160 _tricubic at index-space points (s, t, r)."""
     iu, iv, iw = _ifloor(s), _ifloor(t), _ifloor(r)
-    fu, fv, fw = s - iu.astype(F), t - iv.astype(F), r - iw.astype(F)
+    fu, fv, fw = _fract(s), _fract(t), _fract(r)
     qw = []
     for m in range(4):
         qv = []
@@ -131,4 +139,4 @@ def advect_simple(u, v, w, q, dt, h):
     p = backtrace(u, v, w, _grid_points(q.shape, (0.5, 0.5, 0.5)), dt, h)
     s, t, r = (p[a] - F(0.5) for a in range(3))
     iu, iv, iw = _ifloor(s), _ifloor(t), _ifloor(r)
-    return _tri8(q, iu, iv, iw, s - iu.astype(F), t - iv.astype(F), r - iw.astype(F))
+    return _tri8(q, iu, iv, iw, _fract(s), _fract(t), _fract(r))

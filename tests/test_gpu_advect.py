@@ -151,3 +151,23 @@ def test_advect_rejects_aliasing_and_bad_args():
         advect_uv_mc(vel, vel)
     with pytest.raises(FlubError):
         advect_mc(vel, q, Field(torch.zeros(n, device="cuda")), h0=0.0)
+
+
+@pytest.mark.parametrize("scale", [1e7, 1e30])
+def test_advect_far_outside_and_nan_bit_exact(scale):
+    """Traces that leave the grid by millions of cells (or saturate the index
+    range), and a NaN velocity component: the same values as the oracle."""
+    n = (12, 10, 14)
+    vel = _vel_np(n, 1.0, 19)
+    vel[0][3, 4, 5] = scale
+    vel[1][6, 2, 7] = -scale
+    vel[2][5, 5, 5] = np.nan
+    q = np.random.default_rng(20).standard_normal(n).astype(F)
+    h = 1.0 / 12
+    ref = O.advect_mc(*vel, q, O.STAGGER[0], 0.01, h)
+    out = torch.zeros(n, device="cuda")
+    advect_mc(_mac(vel), Field(dev(q)), Field(out))
+    got = host(out)
+    assert np.array_equal(np.isnan(got), np.isnan(ref))
+    assert np.array_equal(got[~np.isnan(ref)], ref[~np.isnan(ref)])
+    assert np.isnan(ref).any()

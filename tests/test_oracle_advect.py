@@ -165,3 +165,16 @@ def test_advect_simple_shifts_linear_fields():
     s = dt / h
     want = lin(i + 0.5 - s * U[0], j + 0.5 - s * U[1], k + 0.5 - s * U[2])
     np.testing.assert_allclose(out[2:-2, 2:-2, 2:-2], want[2:-2, 2:-2, 2:-2], atol=2e-5)
+
+
+def test_c_oracle_matches_numpy_far_outside_and_nan():
+    n = (8, 9, 10)
+    u, v, w = _vel(n, 1.0, 40)
+    u[3, 4, 5] = 1e30
+    v[2, 2, 2] = -1e7
+    w[4, 4, 4] = np.nan
+    q = np.random.default_rng(41).standard_normal(n).astype(F)
+    c = O.advect_mc(u, v, w, q, O.STAGGER[0], 0.01, 1.0 / 8)
+    py = NA.advect_mc(u, v, w, q, O.STAGGER[0], 0.01, 1.0 / 8)
+    assert np.array_equal(np.isnan(c), np.isnan(py)) and np.isnan(c).any()
+    assert np.array_equal(c[~np.isnan(c)], py[~np.isnan(py)])
