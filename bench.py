@@ -383,37 +383,76 @@ def run_ours(args):
     ms_per_step = elapsed / args.steps
     value = job_ms_per_projection(elapsed, args.steps, world)
 
-    # ---- end to end through the public API with host buffers
+    # ---- end to end through the public API with host buffers.  Every step
+    # copies its inputs from pinned host memory and reads its results back; the
+    # steps are pipelined over two device input sets: step n+1's inputs go up
+    # on a copy stream while step n solves, step n's velocity comes back on a
+    # second copy stream while step n+1 solves, and the pressure comes back on
+    # the compute stream right after its solve (the handle reuses that buffer).
     e2e = None
     if not args.no_e2e:
         pin = lambda a: torch.from_numpy(np.ascontiguousarray(a)).pin_memory()
         h_in = [pin(scene.phi)] + [pin(a) for a in (scene.u, scene.v, scene.w, scene.ur, scene.vr, scene.wr)]
-        h_out = [torch.empty_like(t).pin_memory() for t in h_in[1:4]] + [torch.empty(scene.shape).pin_memory()]
-        d_in = [phi, vel.u.f, vel.v.f, vel.w.f, velr.u.f, velr.v.f, velr.w.f]
-        d_out = [vel.u.f, vel.v.f, vel.w.f, proj.p.f]
+        sets = [[phi, vel.u.f, vel.v.f, vel.w.f, velr.u.f, velr.v.f, velr.w.f],
+                [torch.empty_like(t) for t in (phi, vel.u.f, vel.v.f, vel.w.f, velr.u.f, velr.v.f, velr.w.f)]]
+        h_out = [[torch.empty(t.shape).pin_memory() for t in sets[0][1:4]] + [torch.empty(scene.shape).pin_memory()]
+                 for _ in range(2)]
+        s_up, s_down = torch.cuda.Stream(), torch.cuda.Stream()
+        up_done = [torch.cuda.Event(), torch.cuda.Event()]
+        set_free = [torch.cuda.Event(), torch.cuda.Event()]
+        solved = torch.cuda.Event()
+        for ev in set_free:
+            ev.record(stream)
 
-        def step_e2e():
-            for h, d in zip(h_in, d_in):
-                d.copy_(h, non_blocking=True)
-            proj.project(vel, velr, phi, scene.prims, sync=False, warm_start=warm.get(id(proj)), **solve_kw)
-            for h, d in zip(h_out, d_out):
-                h.copy_(d, non_blocking=True)
+        def upload(n):
+            b = n % 2
+            with torch.cuda.stream(s_up):
+                s_up.wait_event(set_free[b])
+                for h, d in zip(h_in, sets[b]):
+                    d.copy_(h, non_blocking=True)
+                up_done[b].record(s_up)
 
-        for _ in range(max(args.warmup, 1)):
-            step_e2e()
+        def solve_and_download(n):
+            b = n % 2
+            d = sets[b]
+            stream.wait_event(up_done[b])
+            v_b = MACGrid(*(Field(t, d=k + 1) for k, t in enumerate(d[1:4])))
+            vr_b = MACGrid(*(Field(t, d=k + 1) for k, t in enumerate(d[4:7])))
+            proj.project(v_b, vr_b, d[0], scene.prims, sync=False, warm_start=warm.get(id(proj)), **solve_kw)
+            h_out[b][3].copy_(proj.p.f, non_blocking=True)
+            solved.record(stream)
+            with torch.cuda.stream(s_down):
+                s_down.wait_event(solved)
+                for h, t in zip(h_out[b][:3], d[1:4]):
+                    h.copy_(t, non_blocking=True)
+                set_free[b].record(s_down)
+
+        def run_e2e(k, start_event=None):
+            if start_event is not None:
+                s_up.wait_event(start_event)
+            upload(0)
+            for n in range(k):
+                if n + 1 < k:
+                    upload(n + 1)
+                solve_and_download(n)
+            stream.wait_stream(s_down)
+
+        run_e2e(max(args.warmup, 1))
         torch.cuda.synchronize()
         if world > 1:
             dist.barrier()
         e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
         e0.record(stream)
-        for _ in range(args.steps):
-            step_e2e()
+        run_e2e(args.steps, e0)
         e1.record(stream)
         torch.cuda.synchronize()
         et = max_over_ranks(e0.elapsed_time(e1), world, "cuda")
         e2e = {"value": job_ms_per_projection(et, args.steps, world), "unit": UNIT,
                "h2d_bytes_per_step": int(sum(t.numel() * t.element_size() for t in h_in)),
-               "d2h_bytes_per_step": int(sum(t.numel() * t.element_size() for t in h_out))}
+               "d2h_bytes_per_step": int(sum(t.numel() * t.element_size() for t in h_out[0])),
+               "pipelining": "two device input sets; uploads of step n+1 and the velocity read-back of step n "
+                             "overlap the solves on two copy streams; the first upload and the last read-back "
+                             "are inside the timed region"}
 
     # ---- roofline of the dominant kernel of the plain path: the level-0
     # red-black half-sweep (timed on the plain handle's level-0 buffers)
