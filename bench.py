@@ -126,9 +126,10 @@ def run_profile_kernel(args):
     torch.cuda.empty_cache()
     if args.profile_kernel == "smooth":
         # z is defined (set_tags clears every level's z): three level-0
-        # half-sweeps are the only smoother launches of this process
+        # red-black iterations (the tiled kernel where the level has tiles) are
+        # the only smoother launches of this process
         for q in range(3):
-            mg.smooth(0, q & 1)
+            mg.smooth_iteration(0, q & 1)
     elif args.profile_kernel == "matvec":
         for _ in range(3):
             mg.matvec(mg.r0)
@@ -454,37 +455,73 @@ def run_ours(args):
                              "overlap the solves on two copy streams; the first upload and the last read-back "
                              "are inside the timed region"}
 
-    # ---- roofline of the dominant kernel of the plain path: the level-0
-    # red-black half-sweep (timed on the plain handle's level-0 buffers)
+    # ---- roofline of the dominant kernel of the plain path: one level-0
+    # red-black iteration (the TMA-tiled kernel, two half-sweeps per launch),
+    # timed on the plain handle's level-0 buffers
     peak, peak_kind = load_peaks()
-    reps = 48
+    reps = 24
     plain_mg = variants["plain"].mg
-    for ph in (0, 1):
-        plain_mg.smooth(0, ph)
+    tiled = plain_mg.smooth_iteration(0, 0)
+    plain_mg.smooth_iteration(0, 0)
     torch.cuda.synchronize()
     k0, k1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     k0.record(stream)
     for q in range(reps):
-        plain_mg.smooth(0, q & 1)
+        plain_mg.smooth_iteration(0, q & 1)
     k1.record(stream)
     torch.cuda.synchronize()
-    launch_ms = k0.elapsed_time(k1) / reps
-    # a thread owns 8 consecutive cells along k and visits only the groups of
-    # the level's active list (those holding a fluid cell): the canonical
-    # 6.5 B per cell for their 8 cells plus the 4-byte list entry; the
-    # fluid-free groups are never read
+    launch_ms = k0.elapsed_time(k1) / reps / (1 if tiled else 2)
     nx_, ny_, nz_ = scene.shape
-    groups = (proj.tag.f == 1).view(nx_, ny_, nz_ // 8, 8).any(dim=-1)
-    n_active = int(groups.sum().item())
-    n_groups = groups.numel()
-    alg_bytes = SMOOTH_HALF_SWEEP_BYTES_PER_CELL * 8 * n_active + 4.0 * n_active
+    fluid = (proj.tag.f == 1)
+    if tiled:
+        # a CTA stages and updates the whole of every tile (8 x 8 x 32 cells)
+        # that holds a fluid cell: the canonical 13 B per cell per iteration
+        # (R z, r, tag; W z) for those cells, plus the 4-byte tile-list entry;
+        # the fluid-free tiles are never read
+        tiles = fluid.view(nx_ // 8, 8, ny_ // 8, 8, nz_ // 32, 32).any(dim=5).any(dim=3).any(dim=1)
+        n_units = int(tiles.sum().item())
+        alg_bytes = 2 * SMOOTH_HALF_SWEEP_BYTES_PER_CELL * 8 * 8 * 32 * n_units + 4.0 * n_units
+        kname = "k_smooth_tile<0> (level-0 red-black iteration, TMA-staged 8x8x32 tiles, two half-sweeps per launch)"
+        unit_frac = n_units / tiles.numel()
+        traffic = load_traffic("k_smooth_tile")
+    else:
+        groups = fluid.view(nx_, ny_, nz_ // 8, 8).any(dim=-1)
+        n_units = int(groups.sum().item())
+        alg_bytes = SMOOTH_HALF_SWEEP_BYTES_PER_CELL * 8 * n_units + 4.0 * n_units
+        kname = "k_smooth8<false,false> (level-0 red-black half-sweep over the active list)"
+        unit_frac = n_units / groups.numel()
+        traffic = load_traffic("k_smooth8")
     achieved = alg_bytes / (launch_ms * 1e-3) / 1e9
-    traffic = load_traffic("k_smooth8")
-    roofline = {"bound": "hbm", "kernel": "k_smooth8<false,false> (level-0 red-black half-sweep over the active list)",
+    roofline = {"bound": "hbm", "kernel": kname,
                 "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
                 "peak_source": f"{peak_kind} hbm_gbs", "traffic": traffic,
                 "alg_bytes_per_launch": alg_bytes, "launch_ms": launch_ms,
-                "active_group_fraction": n_active / n_groups}
+                "active_unit_fraction": unit_frac}
+
+    # ---- the TMA-tiled smoother (opt-in, FLUB_TILE=1) against the row kernel:
+    # one level-0 red-black iteration each, on a handle of the same scene
+    from flub_gb300 import MGPCG as _MG
+    os.environ["FLUB_TILE"] = "1"
+    try:
+        tmg = _MG(3, scene.shape, scene.levels)
+    finally:
+        os.environ.pop("FLUB_TILE", None)
+    tmg.set_tags(proj.tag.f)
+    tmg.init(plain_mg.r0, 1.0)
+    tmg.mask_interior()
+    tiled_ok = tmg.smooth_iteration(0, 0)
+    tmg.smooth_iteration(0, 1)
+    torch.cuda.synchronize()
+    k0.record(stream)
+    for q in range(reps):
+        tmg.smooth_iteration(0, q & 1)
+    k1.record(stream)
+    torch.cuda.synchronize()
+    tile_smoother = {"level0_iteration_ms_tiles": k0.elapsed_time(k1) / reps if tiled_ok else None,
+                     "level0_iteration_ms_rows": launch_ms * (1 if tiled else 2),
+                     "note": "k_smooth_tile (TMA-staged 8x8x32 tiles, both half-sweeps in one launch, bit-identical) "
+                             "is off by default: slower than the row kernel at this size"}
+    del tmg
 
     # ---- velocity extrapolation after the projection (water_3d.py:70-73, the
     # step after project()): one pass over the three face arrays, timed warm
@@ -582,6 +619,7 @@ def run_ours(args):
                        "parallelism": f"replicas x{world}"},
             "roofline": roofline, "cpu_baseline": cpu, "e2e": e2e, "gpu_launches": int(launches),
             "extrapolation": extrapolation, "advection": advection, "redistance": redistance_info,
+            "tile_smoother": tile_smoother,
             "clocks": clocks,
         }
         print(json.dumps(out), flush=True)

@@ -87,6 +87,7 @@ SIGNATURES = {
     "flub_mg_matvec": (_i32, [_vp, _vp, _vp, _vp]),
     "flub_mg_kernels_executed": (_i32, [_vp, _vp, ctypes.POINTER(_i64)]),
     "flub_mg_smooth": (_i32, [_vp, _i32, _i32, _vp]),
+    "flub_mg_smooth_iteration": (_i32, [_vp, _i32, _i32, ctypes.POINTER(_i32), _vp]),
     "flub_mg_set_schedule": (_i32, [_vp, _i32, _i32, _f32]),
     "flub_mg_set_x0_scaled": (_i32, [_vp, _vp, _vp]),
     "flub_mg_level_shape": (_i32, [_vp, _i32, ctypes.POINTER(_i32), ctypes.POINTER(_i32), ctypes.POINTER(_i32)]),

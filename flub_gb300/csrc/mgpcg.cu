@@ -10,6 +10,8 @@
 //   epilogue  x += alpha p if the last test converged
 // which is the reference's loop (mgpcg.py:406-461) rotated so that the
 // convergence test closes the loop body.  The host reads back the state once.
+#include <cudaTypedefs.h>
+
 #include <cstddef>
 #include <cstdlib>
 #include <cstring>
@@ -22,6 +24,7 @@
 #include "mixed.cuh"
 #include "restrict8.cuh"
 #include "smooth8.cuh"
+#include "smooth_tile.cuh"
 #include "tail.cuh"
 
 namespace flub {
@@ -48,6 +51,14 @@ struct Level {
     int *act, *act_n;
     // stencil words (smooth8.cuh), same condition
     uint16_t *sw;
+    // TMA-tiled smoothing (smooth_tile.cuh) on FP32 levels whose extents are
+    // multiples of the tile: a third correction buffer for the ping-pong of
+    // the out-of-place iterations, the tile flags, and the list of tiles that
+    // hold fluid with its count on the device.  n_tiles == 0: not tiled.
+    float *z3;
+    unsigned char *tflags;
+    int *tiles, *tiles_n;
+    int n_tiles;
 };
 
 struct LaunchCtx {
@@ -79,6 +90,8 @@ struct flub_mg {
     cudaStream_t cap_stream, cap_stream2;
     bool host_loop;
     bool skip_ok;   // internal z buffers keep z = 0 off the fluid (see k_smooth8)
+    bool tile_ok;   // the TMA-tiled smoother runs where a level has tiles (FLUB_TILE=1)
+    bool iter_toggle[flub::kMaxLevels];  // flub_mg_smooth_iteration: direction of the next tiled call
     bool r_masked;  // r is 0 off the fluid (mask_interior since the last init)
     int tail_start;  // first level run by the one-block tail kernel (== levels: none)
     size_t tail_smem;
@@ -144,6 +157,20 @@ static size_t carve(flub_mg *mg, char *base) {
             L.act = (int *)take(sizeof(int) * (size_t)(nl >> 3));
             L.act_n = (int *)take(sizeof(int));
             L.sw = (uint16_t *)take(sizeof(uint16_t) * (size_t)nl);
+        }
+        L.z3 = nullptr;
+        L.tflags = nullptr;
+        L.tiles = L.tiles_n = nullptr;
+        L.n_tiles = 0;
+        // tiles where the level is a whole number of them and every extent is at
+        // least a tile box (the coarse level below then holds the coarse box)
+        if (mg->precision == FLUB_PRECISION_FP32 && L.D.nz % 8 == 0 && L.D.nx % kTI == 0 && L.D.ny % kTJ == 0 &&
+            L.D.nz % kTK == 0 && L.D.nx >= 2 * kTI && L.D.ny >= 2 * kTJ && L.D.nz >= 2 * kTK) {
+            L.n_tiles = (L.D.nx / kTI) * (L.D.ny / kTJ) * (L.D.nz / kTK);
+            L.z3 = (float *)take(sizeof(float) * nl);
+            L.tflags = (unsigned char *)take((size_t)L.n_tiles);
+            L.tiles = (int *)take(sizeof(int) * (size_t)L.n_tiles);
+            L.tiles_n = (int *)take(sizeof(int));
         }
     }
     // per-block counts of the active-list build (level 0 has the most blocks)
@@ -424,6 +451,99 @@ static int sweep(const LaunchCtx &c, const Level &L, int phase, int mode, int sk
 }
 
 
+// ---------------------------------------------------------------- tiled smoothing (smooth_tile.cuh)
+
+static PFN_cuTensorMapEncodeTiled_v12000 g_tile_encode = nullptr;
+
+// Driver entry point for tensor maps and the tile kernels' shared-memory limit.
+static int tile_setup() {
+    static std::mutex m;
+    std::lock_guard<std::mutex> lock(m);
+    if (g_tile_encode) return FLUB_OK;
+    void *fn = nullptr;
+    cudaDriverEntryPointQueryResult q;
+    if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &fn, 12000, cudaEnableDefault, &q) !=
+            cudaSuccess ||
+        q != cudaDriverEntryPointSuccess || !fn) {
+        cudaGetLastError();
+        return FLUB_ERR_CUDA;
+    }
+    if (cudaFuncSetAttribute(k_smooth_tile<kTileInPlaceInput>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                             kTileSmem) != cudaSuccess ||
+        cudaFuncSetAttribute(k_smooth_tile<kTileFromZero>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                             kTileSmem) != cudaSuccess ||
+        cudaFuncSetAttribute(k_smooth_tile<kTileProlong>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                             kTileSmem) != cudaSuccess) {
+        cudaGetLastError();
+        return FLUB_ERR_CUDA;
+    }
+    g_tile_encode = reinterpret_cast<PFN_cuTensorMapEncodeTiled_v12000>(fn);
+    return FLUB_OK;
+}
+
+// 3D tensor map over an (nx, ny, nz) C-order array (x = k innermost), box
+// bk x bj x bi, zero fill outside the array.
+static int tile_map(CUtensorMap *m, const void *base, CUtensorMapDataType dt, int esize, Dims D, int bk, int bj,
+                    int bi) {
+    cuuint64_t dims[3] = {(cuuint64_t)D.nz, (cuuint64_t)D.ny, (cuuint64_t)D.nx};
+    cuuint64_t strides[2] = {(cuuint64_t)D.nz * esize, (cuuint64_t)D.nz * D.ny * esize};
+    cuuint32_t box[3] = {(cuuint32_t)bk, (cuuint32_t)bj, (cuuint32_t)bi};
+    cuuint32_t es[3] = {1, 1, 1};
+    const CUresult r = g_tile_encode(m, dt, 3, const_cast<void *>(base), dims, strides, box, es,
+                                     CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE,
+                                     CU_TENSOR_MAP_L2_PROMOTION_L2_128B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+    if (r != CUDA_SUCCESS) {
+        set_last_error("cuTensorMapEncodeTiled (%dx%dx%d, box %dx%dx%d) failed: %d", D.nx, D.ny, D.nz, bi, bj, bk,
+                       (int)r);
+        return FLUB_ERR_CUDA;
+    }
+    return FLUB_OK;
+}
+
+// One red-black iteration of level L (first_phase, then the other) by tiles,
+// zin -> zout (different buffers); mode kTileFromZero ignores zin,
+// kTileProlong adds the coarse correction zc first.
+static int tile_iteration(flub_mg *mg, const LaunchCtx &c, int l, int first_phase, int mode, const float *r,
+                          const float *zin, float *zout, const float *zc) {
+    const Level &L = mg->lv[l];
+    CUtensorMap mz, mr, mw, mc;
+    FLUB_TRY(tile_map(&mr, r, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 4, L.D, kRK, kRJ, kRI));
+    FLUB_TRY(tile_map(&mw, L.sw, CU_TENSOR_MAP_DATA_TYPE_UINT16, 2, L.D, kWK, kWJ, kWI));
+    mz = mr;
+    mc = mr;  // unused by the modes that do not read them
+    if (mode != kTileFromZero) FLUB_TRY(tile_map(&mz, zin, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 4, L.D, kZK, kZJ, kZI));
+    if (mode == kTileProlong)
+        FLUB_TRY(tile_map(&mc, zc, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 4, mg->lv[l + 1].D, kCK, kCJ, kCI));
+    const dim3 grd(L.n_tiles < kNumSMs * kTileBlocksPerSM ? L.n_tiles : kNumSMs * kTileBlocksPerSM);
+    int *status = &mg->st->status;
+    const int *tl = L.tiles, *tn = L.tiles_n;
+    if (mode == kTileFromZero)
+        return launch_pdl(k_smooth_tile<kTileFromZero>, grd, dim3(kTileThreads), kTileSmem, c.s, mz, mr, mw, mc, zout,
+                          L.D, first_phase, tl, tn, status, c.kc);
+    if (mode == kTileProlong)
+        return launch_pdl(k_smooth_tile<kTileProlong>, grd, dim3(kTileThreads), kTileSmem, c.s, mz, mr, mw, mc, zout,
+                          L.D, first_phase, tl, tn, status, c.kc);
+    return launch_pdl(k_smooth_tile<kTileInPlaceInput>, grd, dim3(kTileThreads), kTileSmem, c.s, mz, mr, mw, mc,
+                      zout, L.D, first_phase, tl, tn, status, c.kc);
+}
+
+// Pre-smoothing (iters iterations from z = 0, phases 0 then 1) ending in
+// z_fin, or post-smoothing (first iteration from z_pre + P zc, phases 1 then
+// 0) ending in z_fin, by tiles; the iterations alternate between z_fin and
+// the level's third buffer so that the last one writes z_fin.
+static int tile_side(flub_mg *mg, const LaunchCtx &c, int l, bool post, int iters, const float *r,
+                     const float *z_pre, float *z_fin, const float *zc) {
+    float *z3 = mg->lv[l].z3;
+    const float *prev = z_pre;
+    for (int t = 0; t < iters; t++) {
+        float *w = ((iters - 1 - t) % 2 == 0) ? z_fin : z3;
+        const int mode = t == 0 ? (post ? kTileProlong : kTileFromZero) : kTileInPlaceInput;
+        FLUB_TRY(tile_iteration(mg, c, l, post ? 1 : 0, mode, r, prev, w, zc));
+        prev = w;
+    }
+    return FLUB_OK;
+}
+
 // multigrid/mgpcg.py:296-349 apply_preconditioner; level 0 uses (r0, z0).
 // z0_clean: z0 holds 0 on every non-fluid cell (true for the handle's own z).
 static int enqueue_vcycle(flub_mg *mg, const LaunchCtx &c, const float *r0, float *z0, bool z0_clean) {
@@ -435,12 +555,21 @@ static int enqueue_vcycle(flub_mg *mg, const LaunchCtx &c, const float *r0, floa
     auto ZF = [&](int l) -> float * { return l == 0 ? z0 : mg->lv[l].z; };
     auto ZP = [&](int l) -> float * { return mg->lv[l].z2; };
     const int lg = lt < Lm - 1 ? lt : Lm - 1;  // levels 0 .. lg-1 restrict to a coarser level
+    // tiled smoothing where the level has tiles and the buffers written hold 0
+    // off the fluid: pre-smoothing writes the level's own z2 / z3, post-
+    // smoothing ends in ZF(l), the caller's z0 at level 0
+    auto TILED_PRE = [&](int l) { return mg->tile_ok && mg->lv[l].n_tiles > 0 && sk == 1; };
+    auto TILED_POST = [&](int l) { return mg->tile_ok && mg->lv[l].n_tiles > 0 && SK(l) == 1; };
     for (int l = 0; l < lg; l++) {
         const Level &L = mg->lv[l];
         const int iters = level_iters(mg, l);
-        for (int it = 0; it < iters; it++) {
-            FLUB_TRY(sweep(c, L, 0, it == 0 ? kSweepFromZero : kSweepInPlace, sk, R(l), ZP(l), ZP(l), nullptr));
-            FLUB_TRY(sweep(c, L, 1, kSweepInPlace, sk, R(l), ZP(l), ZP(l), nullptr));
+        if (TILED_PRE(l)) {
+            FLUB_TRY(tile_side(mg, c, l, false, iters, R(l), nullptr, ZP(l), nullptr));
+        } else {
+            for (int it = 0; it < iters; it++) {
+                FLUB_TRY(sweep(c, L, 0, it == 0 ? kSweepFromZero : kSweepInPlace, sk, R(l), ZP(l), ZP(l), nullptr));
+                FLUB_TRY(sweep(c, L, 1, kSweepInPlace, sk, R(l), ZP(l), ZP(l), nullptr));
+            }
         }
         const Level &C = mg->lv[l + 1];
         if (L.D.nz % 8 == 0)
@@ -489,6 +618,10 @@ static int enqueue_vcycle(flub_mg *mg, const LaunchCtx &c, const float *r0, floa
     for (int l = lg - 1; l >= 0; l--) {
         const Level &L = mg->lv[l];
         const int iters = level_iters(mg, l);
+        if (TILED_POST(l)) {
+            FLUB_TRY(tile_side(mg, c, l, true, iters, R(l), ZP(l), ZF(l), mg->lv[l + 1].z));
+            continue;
+        }
         for (int it = 0; it < iters; it++) {
             FLUB_TRY(sweep(c, L, 1, it == 0 ? kSweepProlong : kSweepInPlace, SK(l), R(l), ZP(l), ZF(l),
                            mg->lv[l + 1].z));
@@ -1015,6 +1148,8 @@ int flub_mg_create(int nx, int ny, int nz, int levels, int precision, void *work
     const char *hl = getenv("FLUB_SOLVE_HOST_LOOP");
     mg->host_loop = hl && hl[0] == '1';
     mg->skip_ok = true;  // the workspace is zeroed below and set_tags re-zeroes the z buffers
+    const char *tl = getenv("FLUB_TILE");
+    mg->tile_ok = tl && tl[0] == '1' && tile_setup() == FLUB_OK;
     choose_tail(mg);
     choose_cluster(mg);
     if (precision == FLUB_PRECISION_MIXED) {
@@ -1080,6 +1215,14 @@ int flub_mg_set_tags(flub_mg *mg, const int32_t *tag, void *stream) {
         FLUB_CHECK_LAUNCH();
         k_act_write<<<nb, kActThreads, 0, s>>>(L.code, ng, mg->act_scratch, L.act);
         FLUB_CHECK_LAUNCH();
+        if (L.n_tiles) {
+            FLUB_CHECK_CUDA(cudaMemsetAsync(L.tflags, 0, (size_t)L.n_tiles, s));
+            FLUB_CHECK_CUDA(cudaMemsetAsync(L.tiles_n, 0, sizeof(int), s));
+            k_tile_flags<<<blocks_for(ng, 256, kNumSMs * 8), 256, 0, s>>>(L.act, L.act_n, L.D, L.tflags);
+            FLUB_CHECK_LAUNCH();
+            k_tile_list<<<blocks_for(L.n_tiles, 256), 256, 0, s>>>(L.tflags, L.n_tiles, L.tiles, L.tiles_n);
+            FLUB_CHECK_LAUNCH();
+        }
     }
     // new tags: re-establish z = p = Ap = 0 off the fluid (the kernels skip
     // 8-cell groups without fluid and rely on it)
@@ -1091,6 +1234,7 @@ int flub_mg_set_tags(flub_mg *mg, const int32_t *tag, void *stream) {
         if (l > 0 && mg->lv[l].rh) FLUB_CHECK_CUDA(cudaMemsetAsync(mg->lv[l].rh, 0, b / 2, s));
         FLUB_CHECK_CUDA(cudaMemsetAsync(mg->lv[l].z, 0, b, s));
         FLUB_CHECK_CUDA(cudaMemsetAsync(mg->lv[l].z2, 0, b, s));
+        if (mg->lv[l].z3) FLUB_CHECK_CUDA(cudaMemsetAsync(mg->lv[l].z3, 0, b, s));
         if (mg->lv[l].zh) FLUB_CHECK_CUDA(cudaMemsetAsync(mg->lv[l].zh, 0, b / 2, s));
         if (mg->lv[l].z2h) FLUB_CHECK_CUDA(cudaMemsetAsync(mg->lv[l].z2h, 0, b / 2, s));
     }
@@ -1301,6 +1445,27 @@ int flub_mg_smooth(flub_mg *mg, int level, int phase, void *stream) {
     LaunchCtx c{as_stream(stream), nullptr, 0, 0};
     const Level &L = mg->lv[level];
     return sweep(c, L, phase, kSweepInPlace, mg->skip_ok ? 1 : 0, L.r, L.z, L.z, nullptr);
+}
+
+int flub_mg_smooth_iteration(flub_mg *mg, int level, int phase, int *tiled, void *stream) {
+    FLUB_REQUIRE(mg, "flub_mg_smooth_iteration: NULL handle");
+    FLUB_REQUIRE(level >= 0 && level < mg->levels, "flub_mg_smooth_iteration: level %d outside [0, %d)", level,
+                 mg->levels);
+    FLUB_REQUIRE(phase == 0 || phase == 1, "flub_mg_smooth_iteration: phase must be 0 or 1");
+    LaunchCtx c{as_stream(stream), nullptr, 0, 0};
+    const Level &L = mg->lv[level];
+    const bool t = mg->tile_ok && L.n_tiles > 0 && mg->skip_ok;
+    if (tiled) *tiled = t ? 1 : 0;
+    if (t) {
+        // z -> z3 and z3 -> z on alternate calls (both keep 0 off the fluid);
+        // the handle's pointers stay as the captured solve graphs know them
+        const bool back = mg->iter_toggle[level];
+        mg->iter_toggle[level] = !back;
+        return tile_iteration(mg, c, level, phase, kTileInPlaceInput, L.r, back ? L.z3 : L.z, back ? L.z : L.z3,
+                              nullptr);
+    }
+    FLUB_TRY(sweep(c, L, phase, kSweepInPlace, mg->skip_ok ? 1 : 0, L.r, L.z, L.z, nullptr));
+    return sweep(c, L, 1 - phase, kSweepInPlace, mg->skip_ok ? 1 : 0, L.r, L.z, L.z, nullptr);
 }
 
 int flub_mg_kernels_executed(flub_mg *mg, void *stream, int64_t *out) {

@@ -247,6 +247,14 @@ class MGPCG:
         """One red-black half-sweep (mgpcg.py:72-86) on a level of the hierarchy."""
         _lib.check(self._lib.flub_mg_smooth(self._h, int(level), int(phase), _stream()), "flub_mg_smooth")
 
+    def smooth_iteration(self, level=0, phase=0):
+        """One red-black iteration on a level (the TMA-tiled kernel where the
+        level has tiles); returns True when the tiled kernel ran."""
+        t = ctypes.c_int(0)
+        _lib.check(self._lib.flub_mg_smooth_iteration(self._h, int(level), int(phase), ctypes.byref(t), _stream()),
+                   "flub_mg_smooth_iteration")
+        return bool(t.value)
+
     def get_x(self, out, scale=1.0):
         """x * scale into out (water_3d.py:67-68)."""
         _lib.check(self._lib.flub_mg_get_x(self._h, ctypes.c_void_p(out.data_ptr()), float(scale), _stream()),

@@ -320,6 +320,13 @@ int flub_mg_matvec(flub_mg *mg, const float *p, float *Ap, void *stream);
  * vectors z and r).  The same kernel the V-cycle launches. */
 int flub_mg_smooth(flub_mg *mg, int level, int phase, void *stream);
 
+/* One red-black iteration (phase, then 1 - phase) on a level: the TMA-tiled
+ * kernel where the level has tiles (out of place, between the level's
+ * correction buffer and its spare, in alternate directions on successive
+ * calls), else two half-sweeps in place.  *tiled (if not NULL) tells which
+ * ran.  For timing and profiling. */
+int flub_mg_smooth_iteration(flub_mg *mg, int level, int phase, int *tiled, void *stream);
+
 /* Allocation-free V-cycle.  No counterpart in the reference: it exists for
  * callers that cannot allocate device memory themselves -- a plugin whose host
  * application owns every device allocation and forbids cudaMalloc in its frame

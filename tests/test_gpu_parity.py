@@ -486,3 +486,71 @@ def test_schedule_rejects_bad_values():
     for bad in [(0, 8, 0.5), (2, 0, 0.5), (2, 8, 0.0), (2, 8, 2.0), (65, 8, 0.5)]:
         with pytest.raises(FlubError):
             mg.set_schedule(*bad)
+
+
+# ---------------------------------------------------------------- TMA-tiled smoothing
+
+TILE_SCENES = {
+    "dam128": lambda: scenes.dam(128, seed=31, levels=5),
+    "rand128": lambda: scenes.random_scene(128, 32, levels=5),
+}
+
+
+@pytest.mark.parametrize("name", sorted(TILE_SCENES))
+def test_tiled_vcycle_bit_exact(name, monkeypatch):
+    """The TMA-tiled smoother (two half-sweeps per launch, FLUB_TILE=1)
+    against the oracle and against the row smoother, bit for bit, with the
+    reference schedule and the light one."""
+    scene = TILE_SCENES[name]()
+    monkeypatch.setenv("FLUB_TILE", "1")
+    tag_o, r0, mg = _setup(scene)
+    tags = O.tag_levels(tag_o, scene.levels)
+    z_tile = host(mg.apply_preconditioner(dev(r0)))
+    assert np.array_equal(z_tile, O.vcycle(r0, tags, np.float32))
+    mg.set_schedule(2, 4, 0.5)
+    z_tile22 = host(mg.apply_preconditioner(dev(r0)))
+    with O.schedule(2, 4, 0.5):
+        assert np.array_equal(z_tile22, O.vcycle(r0, tags, np.float32))
+    monkeypatch.setenv("FLUB_TILE", "0")
+    _, _, mg_rows = _setup(scene)
+    assert np.array_equal(host(mg_rows.apply_preconditioner(dev(r0))), z_tile)
+
+
+@pytest.mark.parametrize("sched", ["reference", "v22"])
+def test_tiled_solve_equals_row_solve(sched, monkeypatch):
+    """A whole solve (level 0 tiled too, inside the CUDA graph) gives the same
+    bits as the row smoother."""
+    scene = TILE_SCENES["dam128"]()
+    out = []
+    for tile in ("1", "0"):
+        monkeypatch.setenv("FLUB_TILE", tile)
+        _, r0, mg = _setup(scene)
+        mg.set_schedule(sched)
+        info = mg.solve(200, 1e-12, 0.0, 1e-12, smoother="phases")
+        out.append((info["iterations"], host(mg.x).copy()))
+    assert out[0][0] == out[1][0]
+    assert np.array_equal(out[0][1], out[1][1])
+
+
+def test_tiled_vcycle_non_cubic_bit_exact(monkeypatch):
+    """96 x 48 x 128 (tiles on levels 0 and 1, not on the 24 x 12 x 32 level
+    below), with solid cells, air pockets and the domain walls."""
+    shape = (96, 48, 128)
+    rng = np.random.default_rng(34)
+    phi = (rng.uniform(-1, 1, shape) + 0.6).astype(np.float32)
+    tag_o = O.tag_dirichlet(phi)
+    tag_o[rng.random(shape) < 0.05] = 2
+    r0 = np.where(tag_o == 1, rng.standard_normal(shape), 0).astype(np.float32)
+    out = []
+    for tile in ("1", "0"):
+        monkeypatch.setenv("FLUB_TILE", tile)
+        mg = MGPCG(3, shape, 4)
+        mg.set_tags(dev(tag_o))
+        mg.init(dev(r0), 1.0)
+        mg.mask_interior()
+        out.append(host(mg.apply_preconditioner(dev(r0))))
+        info = mg.solve(200, 1e-12, 0.0, 1e-12, smoother="phases")
+        out.append((info["iterations"], host(mg.x).copy()))
+    assert np.array_equal(out[0], O.vcycle(r0, O.tag_levels(tag_o, 4), np.float32))
+    assert np.array_equal(out[0], out[2])
+    assert out[1][0] == out[3][0] and np.array_equal(out[1][1], out[3][1])
