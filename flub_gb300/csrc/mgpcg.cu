@@ -164,7 +164,8 @@ static size_t carve(flub_mg *mg, char *base) {
         L.n_tiles = 0;
         // tiles where the level is a whole number of them and every extent is at
         // least a tile box (the coarse level below then holds the coarse box)
-        if (mg->precision == FLUB_PRECISION_FP32 && L.D.nz % 8 == 0 && L.D.nx % kTI == 0 && L.D.ny % kTJ == 0 &&
+        if (mg->tile_ok && mg->precision == FLUB_PRECISION_FP32 && L.D.nz % 8 == 0 && L.D.nx % kTI == 0 &&
+            L.D.ny % kTJ == 0 &&
             L.D.nz % kTK == 0 && L.D.nx >= 2 * kTI && L.D.ny >= 2 * kTJ && L.D.nz >= 2 * kTK) {
             L.n_tiles = (L.D.nx / kTI) * (L.D.ny / kTJ) * (L.D.nz / kTK);
             L.z3 = (float *)take(sizeof(float) * nl);
@@ -1116,6 +1117,8 @@ int flub_mg_create(int nx, int ny, int nz, int levels, int precision, void *work
     reference_schedule(mg);
     mg->nx = nx; mg->ny = ny; mg->nz = nz; mg->levels = levels; mg->precision = precision;
     mg->n = (int64_t)nx * ny * nz;
+    const char *tl = getenv("FLUB_TILE");
+    mg->tile_ok = tl && tl[0] == '1' && tile_setup() == FLUB_OK;  // decides the tile buffers carved below
     const size_t need = carve(mg, nullptr);
     if (workspace) {
         if (workspace_bytes < need || ((uintptr_t)workspace & 255)) {
@@ -1148,8 +1151,6 @@ int flub_mg_create(int nx, int ny, int nz, int levels, int precision, void *work
     const char *hl = getenv("FLUB_SOLVE_HOST_LOOP");
     mg->host_loop = hl && hl[0] == '1';
     mg->skip_ok = true;  // the workspace is zeroed below and set_tags re-zeroes the z buffers
-    const char *tl = getenv("FLUB_TILE");
-    mg->tile_ok = tl && tl[0] == '1' && tile_setup() == FLUB_OK;
     choose_tail(mg);
     choose_cluster(mg);
     if (precision == FLUB_PRECISION_MIXED) {

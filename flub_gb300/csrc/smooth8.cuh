@@ -139,11 +139,17 @@ __global__ void __launch_bounds__(256, 6) k_smooth8(TO *zout, const TI *zin, con
     const int lane = threadIdx.x & 31;
     const int total = 2 * (act ? *act_n : (int)(D.n() >> 3));
     const int stride = gridDim.x * blockDim.x;
-    for (int base = blockIdx.x * blockDim.x + (threadIdx.x & ~31); base < total; base += stride) {
+    // list entry of this lane's next group, fetched one grid-stride step ahead
+    // so that the list read is off the critical path of the loads it feeds
+    const int base0 = blockIdx.x * blockDim.x + (threadIdx.x & ~31);
+    int g_next = (base0 + lane < total) ? (act ? __ldg(act + ((base0 + lane) >> 1)) : ((base0 + lane) >> 1)) : 0;
+    for (int base = base0; base < total; base += stride) {
         const int t = base + lane;
         const bool valid = t < total;  // both lanes of a pair agree (total is even)
         const int h = t & 1;           // half: cells 4h .. 4h + 3 of the group
-        const int g = valid ? (act ? __ldg(act + (t >> 1)) : (t >> 1)) : 0;
+        const int g = valid ? g_next : 0;
+        const int tn = t + stride;
+        g_next = tn < total ? (act ? __ldg(act + (tn >> 1)) : (tn >> 1)) : 0;
         int i, j, kg;
         group_ijk(g, D, i, j, kg);
         const int k0 = kg << 3;
