@@ -69,6 +69,7 @@ def parse_args():
     ap.add_argument("--no-oracle-check", action="store_true",
                     help="skip the FP64 host projection that checks each variant's pressure")
     ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--no-scale512", action="store_true", help="skip the 512^3 dam-break timings")
     ap.add_argument("--profile-kernel", choices=["smooth", "restrict", "matvec", "solve", "project", "advect"],
                     default=None,
                     help="set up the 256^3 solver state and launch only this kernel 3 times (for ncu)")
@@ -595,6 +596,52 @@ def run_ours(args):
                                "half-sweeps update it, one device copy brings it back; 256^3 FP32 phi (67 MB) "
                                "stays in L2"}
 
+    # ---- the 512^3 dam break (the 256^3 scene scaled up, generated on the
+    # device): ms per solve of plain FP32 (reference schedule), plain-v22 and
+    # learned+mixed-v22, each to relative residual 1e-6; the pressures of the
+    # light variants against the plain one (an FP64 host solve at 512^3 would
+    # take minutes)
+    scale512 = None
+    if rank == 0 and not args.no_scale512:
+        del variants
+        torch.cuda.empty_cache()
+        s5 = scenes.dam_device(512, 2, "cuda")
+        v5_0 = [a.clone() for a in (s5.u, s5.v, s5.w)]
+        v5 = MACGrid(*(Field(a, d=d + 1) for d, a in enumerate((s5.u, s5.v, s5.w))))
+        vr5 = MACGrid(*(Field(a, d=d + 1) for d, a in enumerate((s5.ur, s5.vr, s5.wr))))
+        scale512 = {"scene": "dam512 (device-generated, same layout as dam256)", "cells": s5.n_cells,
+                    "levels": s5.levels}
+        p_plain = None
+        for name in ("plain", "plain-v22", "learned+mixed-v22"):
+            prec, sched, use_net = VARIANT_SETUP[name]
+            if use_net and net is None:
+                continue
+            pj = Projection(s5.shape, s5.levels, precision=prec, schedule=sched)
+            ws5 = learned.WarmStart(net) if use_net else None
+            times = []
+            for rep in range(4):
+                for a, b in zip((v5.u.f, v5.v.f, v5.w.f), v5_0):
+                    a.copy_(b)
+                e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+                e0.record(stream)
+                pj.project(v5, vr5, s5.phi, s5.prims, sync=False, warm_start=ws5, **solve_kw)
+                e1.record(stream)
+                torch.cuda.synchronize()
+                if rep:
+                    times.append(e0.elapsed_time(e1))
+            inf = pj.mg.info()
+            entry = {"ms_per_solve": statistics.median(times), "iterations": inf["iterations"],
+                     "converged": bool(inf["converged"]), "max_abs_div_after": pj.max_abs_div(v5, vr5)}
+            if p_plain is None:
+                p_plain = pj.p.f.detach().double().clone()
+            else:
+                entry["pressure_rel_l2_vs_plain"] = float((pj.p.f.double() - p_plain).norm() / p_plain.norm())
+            scale512[name] = entry
+            del pj, ws5
+            torch.cuda.empty_cache()
+        del s5, v5, vr5, v5_0, p_plain
+        torch.cuda.empty_cache()
+
     # ---- CPU baseline: the oracle on the host cores (rank 0, N = 1 only)
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu_baseline and args.cpu_baseline_steps > 0:
@@ -629,7 +676,7 @@ def run_ours(args):
                        "parallelism": f"replicas x{world}"},
             "roofline": roofline, "cpu_baseline": cpu, "e2e": e2e, "gpu_launches": int(launches),
             "extrapolation": extrapolation, "advection": advection, "redistance": redistance_info,
-            "tile_smoother": tile_smoother,
+            "tile_smoother": tile_smoother, "dam512": scale512,
             "clocks": clocks,
         }
         print(json.dumps(out), flush=True)

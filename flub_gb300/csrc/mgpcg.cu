@@ -482,6 +482,14 @@ static int tile_setup() {
     return FLUB_OK;
 }
 
+// The tiled smoother is used (and its buffers carved) when FLUB_TILE=1 and the
+// driver provides tensor maps; flub_mg_workspace_bytes and flub_mg_create
+// must agree on it.
+static bool tile_requested() {
+    const char *tl = getenv("FLUB_TILE");
+    return tl && tl[0] == '1' && tile_setup() == FLUB_OK;
+}
+
 // 3D tensor map over an (nx, ny, nz) C-order array (x = k innermost), box
 // bk x bj x bi, zero fill outside the array.
 static int tile_map(CUtensorMap *m, const void *base, CUtensorMapDataType dt, int esize, Dims D, int bk, int bj,
@@ -1104,6 +1112,7 @@ size_t flub_mg_workspace_bytes(int nx, int ny, int nz, int levels, int precision
     reference_schedule(&tmp);
     tmp.nx = nx; tmp.ny = ny; tmp.nz = nz; tmp.levels = levels; tmp.precision = precision;
     tmp.n = (int64_t)nx * ny * nz;
+    tmp.tile_ok = tile_requested();
     return carve(&tmp, nullptr);
 }
 
@@ -1117,8 +1126,7 @@ int flub_mg_create(int nx, int ny, int nz, int levels, int precision, void *work
     reference_schedule(mg);
     mg->nx = nx; mg->ny = ny; mg->nz = nz; mg->levels = levels; mg->precision = precision;
     mg->n = (int64_t)nx * ny * nz;
-    const char *tl = getenv("FLUB_TILE");
-    mg->tile_ok = tl && tl[0] == '1' && tile_setup() == FLUB_OK;  // decides the tile buffers carved below
+    mg->tile_ok = tile_requested();  // decides the tile buffers carved below
     const size_t need = carve(mg, nullptr);
     if (workspace) {
         if (workspace_bytes < need || ((uintptr_t)workspace & 255)) {

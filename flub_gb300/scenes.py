@@ -264,6 +264,26 @@ def random_scene_device(n, seed, device, levels=None):
                  make_prims(objs), u, v, w, *zeros, seed=seed)
 
 
+def dam_device(n, seed, device, levels=None, g=9.8, dt=1.0 / 60.0):
+    """dam() built with torch on ``device`` (phi and faces are device tensors;
+    the faces from fourier_faces_device), for sizes whose host generation
+    would take minutes (512^3)."""
+    import torch
+    shape = (n, n, n)
+    h = 1.0 / n
+    c = [((torch.arange(n, dtype=torch.float64, device=device) + 0.5) * h) for _ in range(3)]
+    x, y, z = c[0][:, None, None], c[1][None, :, None], c[2][None, None, :]
+    box_phi = torch.maximum(x - 0.35, y - 0.55).expand(shape)
+    sph = torch.sqrt((x - 0.7) ** 2 + (y - 0.3) ** 2 + (z - 0.5) ** 2) - 0.08
+    phi = torch.minimum(box_phi, sph).float().contiguous()
+    del box_phi, sph
+    prims = make_prims([dict(geometry=GEOM_BOX, x=(0.6, 0.05, 0.45), radius=0.05)])
+    u, v, w = fourier_faces_device(shape, seed, device)
+    v -= float(np.float32(g * dt))
+    zeros = [torch.zeros_like(a) for a in (u, v, w)]
+    return Scene(f"dam{n}", shape, levels or _default_levels(n), phi, prims, u, v, w, *zeros, seed=seed)
+
+
 CONFIGS = {
     "box64": lambda seed=0: box(64, seed),
     "sphere128": lambda seed=1: sphere(128, seed),
