@@ -596,6 +596,47 @@ def run_ours(args):
                                "half-sweeps update it, one device copy brings it back; 256^3 FP32 phi (67 MB) "
                                "stays in L2"}
 
+    # ---- U-Net training throughput: forward + backward + Adam on a batch of 4
+    # random 64^3 scenes (the shape the warm start runs at), its conv FLOPs
+    # counted as 2 * 27 * (cin0 + cin1) * cout per output voxel per layer, x3
+    # for forward + the two backward convolutions
+    unet_training = None
+    if net is not None:
+        from flub_gb300.unet import LAYERS, UNet3D as _U
+        tnet = _U(seed=1)
+        gen = torch.Generator(device="cuda").manual_seed(5)
+        B, G = 4, 64
+        div_b = torch.randn((B, G, G, G), generator=gen, device="cuda")
+        tag_b = torch.ones((B, G, G, G), dtype=torch.int32, device="cuda")
+        tag_b[:, :, G // 2:, :] = 0
+        x_b = torch.randn((B, G, G, G), generator=gen, device="cuda")
+        for _ in range(3):
+            tnet.zero_grad()
+            tnet.loss_and_grad(div_b, tag_b, x_b)
+            tnet.adam_step()
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        n_it = 10
+        for _ in range(n_it):
+            tnet.zero_grad()
+            tnet.loss_and_grad(div_b, tag_b, x_b)
+            tnet.adam_step()
+        e1.record(stream)
+        torch.cuda.synchronize()
+        t_ms = e0.elapsed_time(e1) / n_it
+        flops_voxel = sum(2 * 27 * (c0 + c1) * co / 8 ** lv for _, c0, c1, co, lv in LAYERS)
+        flops = 3 * flops_voxel * G ** 3 * B
+        peaks = json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json"))) if os.path.exists(
+            os.path.join(ROOT, "MEASURED_PEAKS.json")) else {}
+        sustained = peaks.get("bf16_tflops_sustained", 1700.0)
+        unet_training = {"batch": B, "grid": G, "ms_per_step": t_ms, "samples_per_s": B / (t_ms * 1e-3),
+                         "conv_flops_per_step": flops, "achieved_tflops": flops / (t_ms * 1e-3) / 1e12,
+                         "frac_of_sustained_bf16": flops / (t_ms * 1e-3) / 1e12 / sustained,
+                         "note": "conv FLOPs only; the 16-64-channel convolutions are skinny GEMMs "
+                                 "(N = 16..64) whose per-tap operand loads bound them, far from the tensor peak"}
+        del tnet, div_b, tag_b, x_b
+
     # ---- the 512^3 dam break (the 256^3 scene scaled up, generated on the
     # device): ms per solve of plain FP32 (reference schedule), plain-v22 and
     # learned+mixed-v22, each to relative residual 1e-6; the pressures of the
@@ -634,6 +675,22 @@ def run_ours(args):
                      "converged": bool(inf["converged"]), "max_abs_div_after": pj.max_abs_div(v5, vr5)}
             if p_plain is None:
                 p_plain = pj.p.f.detach().double().clone()
+                # the level-0 half-sweep at 512^3 (8x the groups of the 256^3 launch)
+                for ph in (0, 1):
+                    pj.mg.smooth(0, ph)
+                torch.cuda.synchronize()
+                e0.record(stream)
+                for q in range(24):
+                    pj.mg.smooth(0, q & 1)
+                e1.record(stream)
+                torch.cuda.synchronize()
+                sweep_ms = e0.elapsed_time(e1) / 24
+                f5 = (pj.tag.f == 1).view(512, 512, 64, 8).any(dim=-1)
+                na = int(f5.sum().item())
+                ab = SMOOTH_HALF_SWEEP_BYTES_PER_CELL * 8 * na + 4.0 * na
+                scale512["k_smooth8_level0"] = {"launch_ms": sweep_ms, "active_groups": na, "alg_bytes": ab,
+                                                "achieved_GBps": ab / (sweep_ms * 1e-3) / 1e9,
+                                                "frac_of_measured_peak": ab / (sweep_ms * 1e-3) / 1e9 / peak}
             else:
                 entry["pressure_rel_l2_vs_plain"] = float((pj.p.f.double() - p_plain).norm() / p_plain.norm())
             scale512[name] = entry
@@ -676,7 +733,7 @@ def run_ours(args):
                        "parallelism": f"replicas x{world}"},
             "roofline": roofline, "cpu_baseline": cpu, "e2e": e2e, "gpu_launches": int(launches),
             "extrapolation": extrapolation, "advection": advection, "redistance": redistance_info,
-            "tile_smoother": tile_smoother, "dam512": scale512,
+            "tile_smoother": tile_smoother, "dam512": scale512, "unet_training": unet_training,
             "clocks": clocks,
         }
         print(json.dumps(out), flush=True)

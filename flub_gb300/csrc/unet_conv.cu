@@ -43,6 +43,9 @@ struct ConvGeom {
     int cout;
     int cin0, cin1;  // cin1 = 0: one source
     int relu;
+    // forward kernel's pipeline stage: activation tile (128 voxels x max cin)
+    // then weight tile, rounded to 1 KB so that every tile stays 1 KB aligned
+    int a_bytes, stage_bytes;
 };
 
 __device__ __forceinline__ uint32_t smem_u32(const void *p) {
@@ -122,7 +125,7 @@ __global__ void __launch_bounds__(kConvThreads, 1)
     extern __shared__ unsigned char conv_smem_raw[];
     unsigned char *smem = reinterpret_cast<unsigned char *>(
         (reinterpret_cast<uintptr_t>(conv_smem_raw) + 1023) & ~static_cast<uintptr_t>(1023));
-    uint64_t *full = reinterpret_cast<uint64_t *>(smem + kConvStages * kConvStage);
+    uint64_t *full = reinterpret_cast<uint64_t *>(smem + kConvStages * g.stage_bytes);
     uint64_t *empty = full + kConvStages;
     uint64_t *done = empty + kConvStages;
     uint32_t *tmem_slot = reinterpret_cast<uint32_t *>(done + 1);
@@ -175,7 +178,7 @@ __global__ void __launch_bounds__(kConvThreads, 1)
             const uint32_t bytes = (uint32_t)(128 * cin * 2 + COUT * cin * 2);
             const uint32_t fb = smem_u32(&full[s]);
             asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(fb), "r"(bytes) : "memory");
-            const uint32_t a = smem_u32(smem + s * kConvStage), w = a + kConvATile;
+            const uint32_t a = smem_u32(smem + s * g.stage_bytes), w = a + g.a_bytes;
             tma_load_5d(a, src ? &mx1 : &mx0, 0, z0 + dz, y0 + dy, x + dx, b, fb);
             tma_load_2d(w, src ? &mw1 : &mw0, 0, tap * COUT, fb);
         }
@@ -192,7 +195,7 @@ __global__ void __launch_bounds__(kConvThreads, 1)
             }
             asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
             const int cin = (it / 27) ? g.cin1 : g.cin0;
-            const uint32_t a = smem_u32(smem + s * kConvStage), w = a + kConvATile;
+            const uint32_t a = smem_u32(smem + s * g.stage_bytes), w = a + g.a_bytes;
             for (int kk = 0; kk < cin / 16; kk++) {
                 const uint64_t ad = sw_desc(a + kk * 32, cin * 2), bd = sw_desc(w + kk * 32, cin * 2);
                 const uint32_t acc = (it > 0 || kk > 0) ? 1u : 0u;
@@ -485,7 +488,10 @@ static int launch_conv(const CUtensorMap &mx0, const CUtensorMap &mw0, const CUt
         attr_set = true;
     }
     const unsigned tiles = (unsigned)((int64_t)g.B * g.NX * (g.NY / g.nyb) * (g.NZ / g.nzb));
-    k_conv3d_tc<COUT><<<tiles, kConvThreads, kConvSmem, s>>>(mx0, mw0, mx1, mw1, g, bias, y);
+    // shared memory sized for this layer's channels: the 16- and 32-channel
+    // layers fit several CTAs per SM, whose pipelines then overlap
+    const size_t smem = (size_t)kConvStages * g.stage_bytes + 1024 + 256;
+    k_conv3d_tc<COUT><<<tiles, kConvThreads, smem, s>>>(mx0, mw0, mx1, mw1, g, bias, y);
     FLUB_CHECK_LAUNCH();
     return FLUB_OK;
 }
@@ -517,6 +523,11 @@ extern "C" int flub_conv3d_bf16(const void *x0, int cin0, const void *w0, const 
     g.cin0 = cin0;
     g.cin1 = x1 ? cin1 : 0;
     g.relu = relu ? 1 : 0;
+    {
+        const int cmax = g.cin1 > g.cin0 ? g.cin1 : g.cin0;
+        g.a_bytes = 128 * cmax * 2;
+        g.stage_bytes = (g.a_bytes + cout * cmax * 2 + 1023) & ~1023;
+    }
     int st = get_encode();
     if (st) return st;
     CUtensorMap mx0, mw0, mx1, mw1;
@@ -572,6 +583,7 @@ extern "C" int flub_conv3d_wgrad(const void *x, int cin, const void *dy, int cou
     FLUB_REQUIRE(aligned16(x) && aligned16(dy), "flub_conv3d_wgrad: pointers must be 16-byte aligned");
     ConvGeom g;
     g.B = B; g.NX = NX; g.NY = NY; g.NZ = NZ;
+    g.a_bytes = g.stage_bytes = 0;  // the forward kernel's stage layout; unused here
     g.nzb = NZ < 128 ? NZ : 128;
     FLUB_REQUIRE(128 % g.nzb == 0 && NZ % g.nzb == 0, "flub_conv3d_wgrad: NZ=%d must divide 128 or be a multiple of 128",
                  NZ);
