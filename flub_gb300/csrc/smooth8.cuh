@@ -106,6 +106,34 @@ __device__ __forceinline__ float coarse_at(const TC *__restrict__ p, float scale
     return __fmul_rn(St<TC>::ld_ro(p), scale);
 }
 
+// One cell's red-black update (multigrid/mgpcg.py:72-86 in the reference's
+// order) from its stencil word w, its value xc, its six neighbours (i+, i-,
+// j+, j-, k+, k-) and its residual r: xc + (r + L z) / d, or 0 for a cell that
+// is not fluid or has no non-solid neighbour.  kFromZero: z was 0 before the
+// sweep (then r / d).
+template <bool kFromZero>
+__device__ __forceinline__ float smooth_cell(uint32_t w, float xc, float xip, float xim, float xjp, float xjm,
+                                             float xkp, float xkm, float r) {
+    if (sw_code(w, 0) != kCodeFluid) return 0.0f;
+    int d = 0;
+    float tp, tm, ret = 0.0f;
+    uint32_t cn;
+    tp = 0.0f; tm = 0.0f;
+    cn = sw_code(w, 1); if (cn != kCodeSolid) { tp = __fsub_rn(cn == kCodeAir ? 0.0f : xip, xc); d++; }
+    cn = sw_code(w, 2); if (cn != kCodeSolid) { tm = __fsub_rn(cn == kCodeAir ? 0.0f : xim, xc); d++; }
+    ret = __fadd_rn(ret, __fadd_rn(tp, tm));
+    tp = 0.0f; tm = 0.0f;
+    cn = sw_code(w, 3); if (cn != kCodeSolid) { tp = __fsub_rn(cn == kCodeAir ? 0.0f : xjp, xc); d++; }
+    cn = sw_code(w, 4); if (cn != kCodeSolid) { tm = __fsub_rn(cn == kCodeAir ? 0.0f : xjm, xc); d++; }
+    ret = __fadd_rn(ret, __fadd_rn(tp, tm));
+    tp = 0.0f; tm = 0.0f;
+    cn = sw_code(w, 5); if (cn != kCodeSolid) { tp = __fsub_rn(cn == kCodeAir ? 0.0f : xkp, xc); d++; }
+    cn = sw_code(w, 6); if (cn != kCodeSolid) { tm = __fsub_rn(cn == kCodeAir ? 0.0f : xkm, xc); d++; }
+    ret = __fadd_rn(ret, __fadd_rn(tp, tm));
+    if (d == 0) return 0.0f;
+    return kFromZero ? __fdiv_rn(r, (float)d) : __fadd_rn(xc, __fdiv_rn(__fadd_rn(r, ret), (float)d));
+}
+
 // One half-sweep over the 8-cell groups; a pair of adjacent lanes shares a
 // group, each lane owning 4 consecutive cells (its "half") -- 4-wide vector
 // loads per row and about half the registers of one lane per group, so twice
@@ -213,44 +241,38 @@ __global__ void __launch_bounds__(256, 6) k_smooth8(TO *zout, const TI *zin, con
         if (!valid) continue;
 
         float out[4];
+        if constexpr (!kProlong) {
+            // the two cells of the active colour are mm = b0 and mm = b0 + 2 (4h is
+            // even): each gets one update body, its operands picked by selects, so
+            // no lane runs the bodies of the other colour
+            const uint32_t wa = b0 ? (wd.x >> 16) : (wd.x & 0xffffu), wb = b0 ? (wd.y >> 16) : (wd.y & 0xffffu);
+            const float za = smooth_cell<kFromZero>(wa, b0 ? zc0[1] : zc0[0], b0 ? zip[1] : zip[0],
+                                                    b0 ? zim[1] : zim[0], b0 ? zjp[1] : zjp[0], b0 ? zjm[1] : zjm[0],
+                                                    b0 ? zc0[2] : zc0[1], b0 ? zc0[0] : zkm, b0 ? rr[1] : rr[0]);
+            const float zb = smooth_cell<kFromZero>(wb, b0 ? zc0[3] : zc0[2], b0 ? zip[3] : zip[2],
+                                                    b0 ? zim[3] : zim[2], b0 ? zjp[3] : zjp[2], b0 ? zjm[3] : zjm[2],
+                                                    b0 ? zkp : zc0[3], b0 ? zc0[2] : zc0[1], b0 ? rr[3] : rr[2]);
+            // the other colour passes through (0 off the fluid)
 #pragma unroll
-        for (int mm = 0; mm < 4; mm++) {
-            const int m = 4 * h + mm;  // cell index in the group (parity of m == parity of mm)
-            const uint32_t w = (mm & 1) ? ((mm < 2 ? wd.x : wd.y) >> 16) : ((mm < 2 ? wd.x : wd.y) & 0xffffu);
-            const uint32_t cm = sw_code(w, 0);
-            out[mm] = cm == kCodeFluid ? zc0[mm] : 0.0f;
-            if ((m & 1) != b0) continue;
-            float zn = 0.0f;
-            if (cm == kCodeFluid) {
-                const float xc = zc0[mm];
-                int d = 0;
-                float tp, tm, ret = 0.0f;
-                uint32_t cn;
-                // axis i
-                tp = 0.0f; tm = 0.0f;
-                cn = sw_code(w, 1); if (cn != kCodeSolid) { tp = __fsub_rn(cn == kCodeAir ? 0.0f : zip[mm], xc); d++; }
-                cn = sw_code(w, 2); if (cn != kCodeSolid) { tm = __fsub_rn(cn == kCodeAir ? 0.0f : zim[mm], xc); d++; }
-                ret = __fadd_rn(ret, __fadd_rn(tp, tm));
-                // axis j
-                tp = 0.0f; tm = 0.0f;
-                cn = sw_code(w, 3); if (cn != kCodeSolid) { tp = __fsub_rn(cn == kCodeAir ? 0.0f : zjp[mm], xc); d++; }
-                cn = sw_code(w, 4); if (cn != kCodeSolid) { tm = __fsub_rn(cn == kCodeAir ? 0.0f : zjm[mm], xc); d++; }
-                ret = __fadd_rn(ret, __fadd_rn(tp, tm));
-                // axis k
-                tp = 0.0f; tm = 0.0f;
-                cn = sw_code(w, 5);
-                if (cn != kCodeSolid) { tp = __fsub_rn(cn == kCodeAir ? 0.0f : (mm < 3 ? zc0[mm + 1] : zkp), xc); d++; }
-                cn = sw_code(w, 6);
-                if (cn != kCodeSolid) { tm = __fsub_rn(cn == kCodeAir ? 0.0f : (mm > 0 ? zc0[mm - 1] : zkm), xc); d++; }
-                ret = __fadd_rn(ret, __fadd_rn(tp, tm));
-                if (d != 0) {
-                    if (kFromZero)
-                        zn = __fdiv_rn(rr[mm], (float)d);  // 0 + (r + L 0) / d, L 0 = 0
-                    else
-                        zn = __fadd_rn(xc, __fdiv_rn(__fadd_rn(rr[mm], ret), (float)d));
-                }
+            for (int mm = 0; mm < 4; mm++) {
+                const uint32_t w = (mm & 1) ? ((mm < 2 ? wd.x : wd.y) >> 16) : ((mm < 2 ? wd.x : wd.y) & 0xffffu);
+                out[mm] = sw_code(w, 0) == kCodeFluid ? zc0[mm] : 0.0f;
             }
-            out[mm] = zn;
+            out[0] = b0 ? out[0] : za;
+            out[1] = b0 ? za : out[1];
+            out[2] = b0 ? out[2] : zb;
+            out[3] = b0 ? zb : out[3];
+        } else {
+            // (the prolongation variant keeps the per-cell form, which needs fewer
+            // live registers)
+#pragma unroll
+            for (int mm = 0; mm < 4; mm++) {
+                const uint32_t w = (mm & 1) ? ((mm < 2 ? wd.x : wd.y) >> 16) : ((mm < 2 ? wd.x : wd.y) & 0xffffu);
+                out[mm] = sw_code(w, 0) == kCodeFluid ? zc0[mm] : 0.0f;
+                if ((mm & 1) != b0) continue;  // 4h is even: cell 4h + mm has the parity of mm
+                out[mm] = smooth_cell<kFromZero>(w, zc0[mm], zip[mm], zim[mm], zjp[mm], zjm[mm],
+                                                 mm < 3 ? zc0[mm + 1] : zkp, mm > 0 ? zc0[mm - 1] : zkm, rr[mm]);
+            }
         }
         St<TO>::st4(zout + ch, out);
     }
