@@ -87,8 +87,7 @@ __global__ void __launch_bounds__(kRedThreads) k8_matvec_pap(MgState *st, const 
         Row8 pc;
         lap_row8(p, code, sw, D, g, a, pc);
         store_row8(Ap + (g << 3), a);
-#pragma unroll
-        for (int m = 0; m < 8; m++) s = fma((double)pc.v[m], (double)a[m], s);
+        s += dot8_ff(pc.v, a);
     }
     double total;
     if (finish_partials(s, partials, &st->ticket, red, &total) && threadIdx.x == 0) {
@@ -130,8 +129,7 @@ __global__ void __launch_bounds__(kRedThreads) k8_update_r_rr(MgState *st, float
             for (int m = 0; m < 8; m++) rv.v[m] = __fmaf_rn(-a, av.v[m], rv.v[m]);
             store_row8(r + (g << 3), rv.v);
         }
-#pragma unroll
-        for (int m = 0; m < 8; m++) s = fma((double)rv.v[m], (double)rv.v[m], s);
+        s += dot8_ff(rv.v, rv.v);
     }
     double total;
     if (finish_partials(s, partials, &st->ticket, red, &total) && threadIdx.x == 0) {
@@ -159,8 +157,7 @@ __global__ void __launch_bounds__(kRedThreads) k8_dot_rr0(MgState *st, const flo
         if (skip && !ga && !group_has_fluid(load_codes8(code + (g << 3)))) continue;
         Row8 rv;
         load_row8(r + (g << 3), rv);
-#pragma unroll
-        for (int m = 0; m < 8; m++) s = fma((double)rv.v[m], (double)rv.v[m], s);
+        s += dot8_ff(rv.v, rv.v);
     }
     double total;
     if (finish_partials(s, partials, &st->ticket, red, &total) && threadIdx.x == 0) {
@@ -193,8 +190,7 @@ __global__ void __launch_bounds__(kRedThreads) k8_dot_zr(MgState *st, const floa
             for (int m = 0; m < 8; m++) zv.v[m] = __fmul_rn(zv.v[m], zs);
         }
         load_row8(r + (g << 3), rv);
-#pragma unroll
-        for (int m = 0; m < 8; m++) s = fma((double)zv.v[m], (double)rv.v[m], s);
+        s += dot8_ff(zv.v, rv.v);
         if (kInit) store_row8(p + (g << 3), zv.v);
     }
     double total;
@@ -283,12 +279,11 @@ __global__ void __launch_bounds__(kRedThreads) k8_x0_gamma(MgState *st, const fl
         Row8 dc, bv;
         lap_row8(d, code, sw, D, g, ld, dc);
         load_row8(b + (g << 3), bv);
+        float dm[8];
 #pragma unroll
-        for (int m = 0; m < 8; m++) {
-            if (code_at(cc, m) != kCodeFluid) continue;
-            s_ld = fma((double)dc.v[m], (double)ld[m], s_ld);
-            s_b = fma((double)dc.v[m], (double)bv.v[m], s_b);
-        }
+        for (int m = 0; m < 8; m++) dm[m] = code_at(cc, m) == kCodeFluid ? dc.v[m] : 0.0f;
+        s_ld += dot8_ff(dm, ld);
+        s_b += dot8_ff(dm, bv.v);
     }
     const double bb = block_sum(s_b, red);
     __syncthreads();

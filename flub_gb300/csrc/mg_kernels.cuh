@@ -45,6 +45,29 @@ struct Dims {
     __host__ __device__ int64_t n() const { return (int64_t)nx * ny * nz; }
 };
 
+// Sum of x[m] * y[m] over the 8 cells of a group, returned as a double.  Each
+// product is split exactly into p + e with an FMA (Dekker), and the running
+// sum is kept as an unevaluated pair (hi, lo) by two-sum (Knuth), all in FP32
+// arithmetic; the pair is converted once.  The result agrees with an FP64
+// accumulation of the exact products to about 2^-44 of sum |x y|, while the
+// FP64 unit, which this GPU runs at a small fraction of the FP32 rate, sees
+// one add per group instead of eight fused multiply-adds and sixteen
+// conversions.
+__device__ __forceinline__ double dot8_ff(const float *x, const float *y) {
+    float hi = 0.0f, lo = 0.0f;
+#pragma unroll
+    for (int m = 0; m < 8; m++) {
+        const float p = __fmul_rn(x[m], y[m]);
+        const float e = __fmaf_rn(x[m], y[m], -p);
+        const float t = __fadd_rn(hi, p);
+        const float bp = __fsub_rn(t, hi);
+        const float err = __fadd_rn(__fsub_rn(hi, __fsub_rn(t, bp)), __fsub_rn(p, bp));
+        hi = t;
+        lo = __fadd_rn(lo, __fadd_rn(err, e));
+    }
+    return (double)hi + (double)lo;
+}
+
 // Entry of every solver kernel.  Programmatic dependent launch: let the next
 // kernel of the stream start launching now, then wait until the previous one
 // has completed and its writes are visible (both are no-ops for a launch

@@ -130,8 +130,7 @@ __global__ void __launch_bounds__(kRedThreads) k8_update_r_rr_mixed(MgState *st,
         }
         St<float>::st8(r + (g << 3), rv);
         St<__half>::st8(rh + (g << 3), hv);
-#pragma unroll
-        for (int m = 0; m < 8; m++) s = fma((double)rv[m], (double)rv[m], s);
+        s += dot8_ff(rv, rv);
     }
     double total;
     if (finish_partials(s, partials, &st->ticket, red, &total) && threadIdx.x == 0) {
@@ -164,11 +163,8 @@ __global__ void __launch_bounds__(kRedThreads) k8_dot_zr_flex(MgState *st, const
         for (int m = 0; m < 8; m++) zv[m] = __fmul_rn(zv[m], zs);
         St<float>::ld8_ro(r + (g << 3), rv);
         St<float>::ld8_ro(r_old + (g << 3), ov);
-#pragma unroll
-        for (int m = 0; m < 8; m++) {
-            s = fma((double)zv[m], (double)rv[m], s);
-            so = fma((double)zv[m], (double)ov[m], so);
-        }
+        s += dot8_ff(zv, rv);
+        so += dot8_ff(zv, ov);
     }
     const double bo = block_sum(so, red);
     __syncthreads();
