@@ -8,11 +8,16 @@
 
 namespace flub {
 
-// Update of one face between cells lo and hi (mirrors the reference's branch
-// order: solid on either side, else fluid on either side, else 0).
-__device__ __forceinline__ float grad_face(float uf, float urf, float plo, float phi_, int tlo, int thi) {
-    if (tlo == 2 || thi == 2) return urf;
-    if (tlo == 1 || thi == 1) return __fsub_rn(uf, __fsub_rn(phi_, plo));
+// Update of face f between cells lo and hi (mirrors the reference's branch
+// order: solid on either side, else fluid on either side, else 0).  Each
+// branch reads only what it uses: a face between two air cells (most of a
+// water scene) reads its two tags and writes 0.  ps: pressure scale.
+__device__ __forceinline__ float grad_face(const float *__restrict__ uf, const float *__restrict__ urf,
+                                          const float *__restrict__ p, float ps, int64_t f, int64_t clo, int64_t chi,
+                                          int tlo, int thi) {
+    if (tlo == 2 || thi == 2) return __ldg(&urf[f]);
+    if (tlo == 1 || thi == 1)
+        return __fsub_rn(uf[f], __fsub_rn(__fmul_rn(__ldg(&p[chi]), ps), __fmul_rn(__ldg(&p[clo]), ps)));
     return 0.0f;
 }
 
@@ -32,8 +37,7 @@ __global__ void __launch_bounds__(kRowThreads) k_subtract_gradient_axis(float *_
         if (0 < ii && ii < nd) {
             const int64_t chi = ((int64_t)i * ny + j) * nz + k;
             const int64_t clo = chi - (d == 1 ? (int64_t)ny * nz : (d == 2 ? (int64_t)nz : 1));
-            uf[f] = grad_face(uf[f], __ldg(&urf[f]), __ldg(&p[clo]), __ldg(&p[chi]), __ldg(&tag[clo]),
-                              __ldg(&tag[chi]));
+            uf[f] = grad_face(uf, urf, p, 1.0f, f, clo, chi, __ldg(&tag[clo]), __ldg(&tag[chi]));
         } else {
             uf[f] = 0.0f;
         }
@@ -57,24 +61,21 @@ __global__ void __launch_bounds__(kRowThreads) k_subtract_gradient_all(float *__
         if (j < ny && k < nz) {  // u face (i, j, k), i in [0, nx]
             const int64_t f = ((int64_t)i * ny + j) * nz + k;
             if (0 < i && i < nx)
-                u[f] = grad_face(u[f], __ldg(&ur[f]), __fmul_rn(__ldg(&p[c - si]), ps), __fmul_rn(__ldg(&p[c]), ps),
-                                 __ldg(&tag[c - si]), __ldg(&tag[c]));
+                u[f] = grad_face(u, ur, p, ps, f, c - si, c, __ldg(&tag[c - si]), __ldg(&tag[c]));
             else
                 u[f] = 0.0f;
         }
         if (i < nx && k < nz) {  // v face (i, j, k), j in [0, ny]
             const int64_t f = ((int64_t)i * ey + j) * nz + k;
             if (0 < j && j < ny)
-                v[f] = grad_face(v[f], __ldg(&vr[f]), __fmul_rn(__ldg(&p[c - sj]), ps), __fmul_rn(__ldg(&p[c]), ps),
-                                 __ldg(&tag[c - sj]), __ldg(&tag[c]));
+                v[f] = grad_face(v, vr, p, ps, f, c - sj, c, __ldg(&tag[c - sj]), __ldg(&tag[c]));
             else
                 v[f] = 0.0f;
         }
         if (i < nx && j < ny) {  // w face (i, j, k), k in [0, nz]
             const int64_t f = ((int64_t)i * ny + j) * ez + k;
             if (0 < k && k < nz)
-                w[f] = grad_face(w[f], __ldg(&wr[f]), __fmul_rn(__ldg(&p[c - 1]), ps), __fmul_rn(__ldg(&p[c]), ps),
-                                 __ldg(&tag[c - 1]), __ldg(&tag[c]));
+                w[f] = grad_face(w, wr, p, ps, f, c - 1, c, __ldg(&tag[c - 1]), __ldg(&tag[c]));
             else
                 w[f] = 0.0f;
         }

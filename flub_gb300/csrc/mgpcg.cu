@@ -253,7 +253,10 @@ static size_t cluster_layout(const flub_mg *mg, int lc, int C, ClusterParams *P)
     // block 0 takes over the <= 16^3 levels when their schedule is long (the
     // reference's 6 << l sweeps, hundreds of barriers); a light schedule has
     // too few sweeps there to pay for the hand-off
-    const bool want_tail = mg->sched_nu < 0 || mg->sched_nu >= 4;
+    // (FLUB_CLUSTER_TAIL=1 / 0 overrides the rule; both give the same bits)
+    const char *ct = getenv("FLUB_CLUSTER_TAIL");
+    const bool want_tail =
+        ct && (ct[0] == '0' || ct[0] == '1') ? ct[0] == '1' : (mg->sched_nu < 0 || mg->sched_nu >= 4);
     int lt = mg->levels;  // first level run by block 0 alone (== levels: none)
     for (int l = lc; l < mg->levels; l++) {
         const Dims D{mg->nx >> l, mg->ny >> l, mg->nz >> l};
