@@ -584,7 +584,7 @@ static int enqueue_vcycle(flub_mg *mg, const LaunchCtx &c, const float *r0, floa
         }
         const Level &C = mg->lv[l + 1];
         if (L.D.nz % 8 == 0)
-            FLUB_TRY(launch_pdl(k_restrict8<float, float, float>, dim3(blocks_for(C.D.n() >> 2, 256, kNumSMs * 8)),
+            FLUB_TRY(launch_pdl(k_restrict8<float, float, float>, dim3(blocks_for(C.D.n(), 256, kNumSMs * 4)),
                                 dim3(256), 0, c.s, R(l), (const float *)ZP(l), (const uint8_t *)L.code,
                                 (const uint16_t *)L.sw, C.r,
                                 (const uint8_t *)C.code, C.D, mg->sched_rscale, (const int *)C.act,
@@ -693,7 +693,7 @@ static int enqueue_vcycle_mixed(flub_mg *mg, const LaunchCtx &c, float *z0, bool
                                                             1.0f));
         }
         const Level &C = mg->lv[l + 1];
-        FLUB_TRY(launch_pdl(k_restrict8<__half, __half, __half>, dim3(blocks_for(C.D.n() >> 2, 256, kNumSMs * 8)),
+        FLUB_TRY(launch_pdl(k_restrict8<__half, __half, __half>, dim3(blocks_for(C.D.n(), 256, kNumSMs * 4)),
                             dim3(256), 0, c.s, (const __half *)L.rh, (const __half *)L.z2h, (const uint8_t *)L.code,
                             (const uint16_t *)L.sw, C.rh, (const uint8_t *)C.code, C.D, 0.125f * mg->sched_rscale, (const int *)C.act,
                             (const int *)C.act_n, c.kc));

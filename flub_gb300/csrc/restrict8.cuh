@@ -1,5 +1,5 @@
 // Residual + restriction (multigrid/mgpcg.py:94-101, written as a gather) on
-// groups of 8 fine cells: one thread produces 4 consecutive coarse cells
+// groups of 8 fine cells: four lanes produce 4 consecutive coarse cells
 // (I, J, K0..K0+3) from the four fine rows (2I + ii, 2J + jj), k = 2 K0 .. 2 K0
 // + 7, each one 8-cell group read with vector loads.  Per coarse cell the 8
 // children are summed in the reference's order (ii, jj, kk), kk fastest, with
@@ -68,61 +68,74 @@ __device__ __forceinline__ void residual_row8(const TR *__restrict__ r, const TZ
     }
 }
 
-// Coarse level C (fine = 2C).  Items: with a coarse active list, 2 per listed
-// coarse group (its two halves of 4 cells); the coarse cells outside the list
-// are not fluid and keep r_c = 0 (cleared at set_tags, never written
-// otherwise).  Without a list, every half-group of the coarse grid.
+// Coarse level C (fine = 2C).  Work items: the coarse half-groups of 4 cells
+// (I, J, 4 K4 .. 4 K4 + 3): with a coarse active list, the 2 halves of every
+// listed coarse group (the coarse cells outside the list are not fluid and keep
+// r_c = 0, cleared at set_tags and never written otherwise); without one, every
+// half-group.  Four adjacent lanes share an item, lane q = 2 ii + jj computing
+// the residual of fine row (2I + ii, 2J + jj) -- a quarter of the registers
+// and four times the lanes of one thread per item, to hide memory latency.
+// The 8 children of each coarse cell are then summed in the reference's order
+// (ii, jj, kk), kk fastest, from values broadcast by shuffles; the first
+// lane of the four stores the 4 coarse values.
 // out_scale: restriction scale (times 1/8 between FP16 levels at 8^-l).
+// Grid: one-dimensional, grid-stride by warps (all lanes of a warp run the same
+// iterations, so the shuffles see every lane).
 template <typename TRI, typename TZI, typename TRO>
-__global__ void __launch_bounds__(256) k_restrict8(const TRI *__restrict__ rf, const TZI *__restrict__ zf,
-                                                   const uint8_t *__restrict__ cf, const uint16_t *__restrict__ swf,
-                                                   TRO *__restrict__ rc,
-                                                   const uint8_t *__restrict__ cc, Dims C, float out_scale,
-                                                   const int *__restrict__ act, const int *__restrict__ act_n,
-                                                   unsigned long long *kc) {
+__global__ void __launch_bounds__(256, 4) k_restrict8(const TRI *__restrict__ rf, const TZI *__restrict__ zf,
+                                                      const uint8_t *__restrict__ cf, const uint16_t *__restrict__ swf,
+                                                      TRO *__restrict__ rc,
+                                                      const uint8_t *__restrict__ cc, Dims C, float out_scale,
+                                                      const int *__restrict__ act, const int *__restrict__ act_n,
+                                                      unsigned long long *kc) {
     count_kernel(kc);
     const Dims F{2 * C.nx, 2 * C.ny, 2 * C.nz};
     const int nh = (int)(C.n() >> 2);  // coarse half-groups of 4 cells
-    const int total = act ? 2 * *act_n : nh;
+    const int items = act ? 2 * *act_n : nh;
+    const int total = 4 * items;
     const int fz8 = F.nz >> 3;
-    for (int t = blockIdx.x * blockDim.x + threadIdx.x; t < total; t += gridDim.x * blockDim.x) {
-        const int h = act ? 2 * __ldg(act + (t >> 1)) + (t & 1) : t;  // half-group index
-        const int q0 = h << 2;                                         // first coarse cell
-        const uint32_t codes4 = __ldg(reinterpret_cast<const uint32_t *>(cc + q0));
-        float s[4];
-        if ((codes4 & 0x02020202u) == 0u) {
-            // no fluid coarse cell among the 4
+    const int lane = threadIdx.x & 31, q = lane & 3;
+    const int stride = gridDim.x * blockDim.x;
+    for (int base = blockIdx.x * blockDim.x + (threadIdx.x & ~31); base < total; base += stride) {
+        const int t = base + lane;
+        const bool valid = t < total;  // the 4 lanes of an item agree (total is a multiple of 4)
+        const int it = t >> 2;
+        const int h = valid ? (act ? 2 * __ldg(act + (it >> 1)) + (it & 1) : it) : 0;  // half-group index
+        const int q0 = h << 2;                                                          // first coarse cell
+        const uint32_t codes4 = valid ? __ldg(reinterpret_cast<const uint32_t *>(cc + q0)) : 0u;
+        const bool any = (codes4 & 0x02020202u) != 0u;  // a fluid coarse cell among the 4
+        float v[8];
 #pragma unroll
-            for (int m = 0; m < 4; m++) s[m] = 0.0f;
-        } else {
+        for (int m = 0; m < 8; m++) v[m] = 0.0f;
+        if (any) {
             // (I, J, K4) of the half-group: the coarse grid read as 4-cell groups
             int I, J, K4;
             group_ijk(h, Dims{C.nx, C.ny, C.nz << 1}, I, J, K4);  // C.nz / 4 half-groups per row
-            bool first[4] = {true, true, true, true};
+            const int g = ((2 * I + (q >> 1)) * F.ny + 2 * J + (q & 1)) * fz8 + K4;  // fine group at k = 8 K4
+            residual_row8(rf, zf, cf, swf, F, g, v);
+        }
+        // coarse cell m gets (v[2m], v[2m + 1]) of lanes q = 0..3 in turn
+        float s[4];
+        const int src = lane & ~3;
 #pragma unroll
-            for (int m = 0; m < 4; m++) s[m] = 0.0f;
+        for (int m = 0; m < 4; m++) {
 #pragma unroll
-            for (int ii = 0; ii < 2; ii++)
-#pragma unroll
-                for (int jj = 0; jj < 2; jj++) {
-                    const int g = ((2 * I + ii) * F.ny + 2 * J + jj) * fz8 + K4;  // fine group at k = 8 K4
-                    float v[8];
-                    residual_row8(rf, zf, cf, swf, F, g, v);
-#pragma unroll
-                    for (int m = 0; m < 4; m++) {
-#pragma unroll
-                        for (int kk = 0; kk < 2; kk++) {
-                            const float x = v[2 * m + kk];
-                            s[m] = first[m] ? x : __fadd_rn(s[m], x);
-                            first[m] = false;
-                        }
-                    }
-                }
+            for (int u = 0; u < 4; u++) {
+                const float a = __shfl_sync(0xffffffffu, v[2 * m], src + u);
+                const float b = __shfl_sync(0xffffffffu, v[2 * m + 1], src + u);
+                s[m] = u == 0 ? __fadd_rn(a, b) : __fadd_rn(__fadd_rn(s[m], a), b);
+            }
+        }
+        if (!valid || q != 0) continue;
+        if (any) {
 #pragma unroll
             for (int m = 0; m < 4; m++) {
                 const uint8_t cm = (uint8_t)((codes4 >> (8 * m)) & 0xffu);
                 s[m] = cm == kCodeFluid ? __fmul_rn(s[m], out_scale) : 0.0f;
             }
+        } else {
+#pragma unroll
+            for (int m = 0; m < 4; m++) s[m] = 0.0f;
         }
         St<TRO>::st4(rc + q0, s);
     }
