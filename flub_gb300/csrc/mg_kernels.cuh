@@ -40,6 +40,17 @@ __device__ __forceinline__ float fp16_residual_scale(double rtr, int64_t n) {
     return ldexpf(1.0f, -e);
 }
 
+// fp16_residual_scale evaluated once per block by thread 0 and shared: the
+// FP64 divide and square root cost tens of FP64 instructions, which at this
+// GPU's FP64 rate dominate a streaming kernel when every thread repeats them.
+// Every thread of the block must reach the call.
+__device__ __forceinline__ float block_fp16_residual_scale(double rtr, int64_t n) {
+    __shared__ float s_hs;
+    if (threadIdx.x == 0) s_hs = fp16_residual_scale(rtr, n);
+    __syncthreads();
+    return s_hs;
+}
+
 struct Dims {
     int nx, ny, nz;
     __host__ __device__ int64_t n() const { return (int64_t)nx * ny * nz; }

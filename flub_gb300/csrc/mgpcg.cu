@@ -1071,33 +1071,67 @@ __global__ void __launch_bounds__(256) k_restrict_vec(const float *__restrict__ 
 // weights 3/4 and 1/4 per axis.  Coarse fluid cells contribute their value,
 // air cells 0 (Dirichlet), solid and out-of-domain cells are left out and
 // the remaining weights renormalised.
-__global__ void __launch_bounds__(256) k_prolong_trilinear(const float *__restrict__ xc,
-                                                           const uint8_t *__restrict__ cc, Dims C,
-                                                           const uint8_t *__restrict__ cf, float *__restrict__ xf,
-                                                           Dims F) {
-    const int64_t n = F.n();
-    for (int64_t c = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; c < n; c += (int64_t)gridDim.x * blockDim.x) {
-        if (cf[c] != kCodeFluid) {
-            xf[c] = 0.0f;
-            continue;
+// One thread per coarse cell (I, J, K) writes the 2 x 2 x 2 fine cells it
+// covers (every level is half its parent on each axis).  The 27 coarse
+// neighbours are loaded once into registers as a weight flag (inside the
+// domain and not solid) and a value (0 unless fluid); each fine fluid cell
+// accumulates its 8 corners in a fixed order (the coarse cell itself first,
+// then the corners towards the fine cell, z fastest), w by adds and s by
+// fmaf, and stores s / w.  A left-out corner adds 0 to w and fmaf(wt, 0, s)
+// to s, which leave both unchanged (s starts at +0 and never becomes -0).
+// Grid: row_grid(C.nx, C.ny, C.nz).
+__global__ void __launch_bounds__(kRowThreads) k_prolong_trilinear(const float *__restrict__ xc,
+                                                                    const uint8_t *__restrict__ cc, Dims C,
+                                                                    const uint8_t *__restrict__ cf,
+                                                                    float *__restrict__ xf) {
+    const int K = blockIdx.x * blockDim.x + threadIdx.x, J = blockIdx.y, I = blockIdx.z;
+    if (K >= C.nz) return;
+    const int fy = 2 * C.ny, fz = 2 * C.nz;
+    int64_t frow[4];
+    uint16_t fcode[4];
+    bool any = false;
+#pragma unroll
+    for (int r = 0; r < 4; r++) {
+        frow[r] = ((int64_t)(2 * I + (r >> 1)) * fy + 2 * J + (r & 1)) * fz + 2 * K;
+        fcode[r] = __ldg(reinterpret_cast<const uint16_t *>(cf + frow[r]));
+        any |= (fcode[r] & 0xff) == kCodeFluid || (fcode[r] >> 8) == kCodeFluid;
+    }
+    if (!any) {
+#pragma unroll
+        for (int r = 0; r < 4; r++) *reinterpret_cast<float2 *>(xf + frow[r]) = make_float2(0.0f, 0.0f);
+        return;
+    }
+    float val[27];
+    bool ok[27];
+#pragma unroll
+    for (int q = 0; q < 27; q++) {
+        const int ii = I + q / 9 - 1, jj = J + (q / 3) % 3 - 1, kk = K + q % 3 - 1;
+        const bool in = ii >= 0 && ii < C.nx && jj >= 0 && jj < C.ny && kk >= 0 && kk < C.nz;
+        const int64_t cq = ((int64_t)ii * C.ny + jj) * C.nz + kk;
+        const uint8_t code = in ? __ldg(cc + cq) : kCodeSolid;
+        ok[q] = code != kCodeSolid;
+        val[q] = code == kCodeFluid ? __ldg(xc + cq) : 0.0f;
+    }
+#pragma unroll
+    for (int r = 0; r < 4; r++) {
+        float out[2];
+#pragma unroll
+        for (int ek = 0; ek < 2; ek++) {
+            const int ei = r >> 1, ej = r & 1;
+            const int oi = ei ? 1 : -1, oj = ej ? 1 : -1, ok3 = ek ? 1 : -1;
+            float s = 0.0f, w = 0.0f;
+#pragma unroll
+            for (int m = 0; m < 8; m++) {
+                const int a = (m >> 2) ? oi : 0, bq = ((m >> 1) & 1) ? oj : 0, e = (m & 1) ? ok3 : 0;
+                const int q = (a + 1) * 9 + (bq + 1) * 3 + (e + 1);
+                const float wt = (a ? 0.25f : 0.75f) * (bq ? 0.25f : 0.75f) * (e ? 0.25f : 0.75f);
+                w += ok[q] ? wt : 0.0f;
+                s = fmaf(wt, val[q], s);
+            }
+            const uint8_t fc = ek ? (uint8_t)(fcode[r] >> 8) : (uint8_t)(fcode[r] & 0xff);
+            out[ek] = fc != kCodeFluid ? 0.0f : (w > 0.0f ? s / w : 0.0f);
         }
-        int i, j, k;
-        unflatten(c, F, i, j, k);
-        const int I = i >> 1, J = j >> 1, K = k >> 1;
-        const int oi = (i & 1) ? 1 : -1, oj = (j & 1) ? 1 : -1, ok = (k & 1) ? 1 : -1;
-        float s = 0.0f, w = 0.0f;
-        for (int m = 0; m < 8; m++) {
-            const int a = (m >> 2) ? oi : 0, bq = ((m >> 1) & 1) ? oj : 0, e = (m & 1) ? ok : 0;
-            const int ii = I + a, jj = J + bq, kk = K + e;
-            if (ii < 0 || ii >= C.nx || jj < 0 || jj >= C.ny || kk < 0 || kk >= C.nz) continue;
-            const int64_t q = ((int64_t)ii * C.ny + jj) * C.nz + kk;
-            const uint8_t code = cc[q];
-            if (code == kCodeSolid) continue;
-            const float wt = (a ? 0.25f : 0.75f) * (bq ? 0.25f : 0.75f) * (e ? 0.25f : 0.75f);
-            w += wt;
-            if (code == kCodeFluid) s = fmaf(wt, xc[q], s);
-        }
-        xf[c] = w > 0.0f ? s / w : 0.0f;
+        *reinterpret_cast<float2 *>(xf + frow[r]) = make_float2(out[0], out[1]);
     }
 }
 
@@ -1415,8 +1449,8 @@ int flub_mg_prolong_vector(flub_mg *mg, int level, const float *coarse, float *f
     FLUB_REQUIRE(level >= 1 && level < mg->levels, "flub_mg_prolong_vector: level %d outside [1, %d)", level,
                  mg->levels);
     const Level &C = mg->lv[level], &F = mg->lv[level - 1];
-    k_prolong_trilinear<<<blocks_for(F.D.n(), 256), 256, 0, as_stream(stream)>>>(coarse, C.code, C.D, F.code, fine,
-                                                                                 F.D);
+    k_prolong_trilinear<<<row_grid(C.D.nx, C.D.ny, C.D.nz), kRowThreads, 0, as_stream(stream)>>>(coarse, C.code,
+                                                                                                 C.D, F.code, fine);
     FLUB_CHECK_LAUNCH();
     return FLUB_OK;
 }

@@ -76,7 +76,7 @@ __global__ void __launch_bounds__(256) k_restrict_t(const TRI *__restrict__ rf, 
 __global__ void __launch_bounds__(256) k8_to_half(MgState *st, const float *__restrict__ r, __half *__restrict__ rh,
                                                   int64_t n, unsigned long long *kc) {
     count_kernel(kc);
-    const float hs = st ? fp16_residual_scale(st->rtr0, n) : 1.0f;
+    const float hs = st ? block_fp16_residual_scale(threadIdx.x == 0 ? st->rtr0 : 0.0, n) : 1.0f;
     if (st && (blockIdx.x | threadIdx.x) == 0) st->zscale = 1.0f / hs;
     const int ng = (int)(n >> 3);
     // every group: afterwards rh = r / zscale everywhere (0 off the fluid when r is masked)
@@ -113,7 +113,7 @@ __global__ void __launch_bounds__(kRedThreads) k8_update_r_rr_mixed(MgState *st,
     const int *ga = skip ? act : nullptr;
     // scale of the FP16 copy from the previous residual norm (st->rtr is only
     // overwritten by the last block, after every block has read it)
-    const float hs = fp16_residual_scale(st->rtr, n);
+    const float hs = block_fp16_residual_scale(threadIdx.x == 0 ? st->rtr : 0.0, n);
     if ((blockIdx.x | threadIdx.x) == 0) st->zscale = 1.0f / hs;
     const int ng = (int)(n >> 3);
     double s = 0.0;

@@ -96,6 +96,40 @@ __global__ void __launch_bounds__(256) k_pool2(const __nv_bfloat16 *__restrict__
     }
 }
 
+// The same pool for C % 8 == 0: thread t of coarse row (b, i, j) averages
+// channels 8 c8 .. 8 c8 + 7 of coarse voxel k = t / (C / 8) from its 8 fine
+// voxels (16-byte loads), summing them in k_pool2's order.
+// Grid: (ceil((NZ / 2) * (C / 8) / 128), NY / 2, B * (NX / 2)), 128 threads.
+__global__ void __launch_bounds__(128) k_pool2_v8(const uint4 *__restrict__ x, uint4 *__restrict__ y, int NX, int NY,
+                                                  int NZ, int C8) {
+    const int t = blockIdx.x * blockDim.x + threadIdx.x;
+    const int cx = NX >> 1, cy = NY >> 1, cz = NZ >> 1;
+    if (t >= cz * C8) return;
+    const int k = t / C8, c8 = t - k * C8;
+    const int j = blockIdx.y, bi = blockIdx.z;
+    const int b = bi / cx, i = bi - b * cx;
+    float s[8];
+#pragma unroll
+    for (int m = 0; m < 8; m++) s[m] = 0.0f;
+#pragma unroll
+    for (int d = 0; d < 8; d++) {
+        const int64_t f = (((int64_t)b * NX + 2 * i + (d >> 2)) * NY + 2 * j + ((d >> 1) & 1)) * NZ + 2 * k + (d & 1);
+        const uint4 u = __ldg(x + f * C8 + c8);
+        const __nv_bfloat162 *h = reinterpret_cast<const __nv_bfloat162 *>(&u);
+#pragma unroll
+        for (int q = 0; q < 4; q++) {
+            const float2 p = __bfloat1622float2(h[q]);
+            s[2 * q] += p.x;
+            s[2 * q + 1] += p.y;
+        }
+    }
+    uint4 o;
+    __nv_bfloat162 *oh = reinterpret_cast<__nv_bfloat162 *>(&o);
+#pragma unroll
+    for (int q = 0; q < 4; q++) oh[q] = __floats2bfloat162_rn(s[2 * q] * 0.125f, s[2 * q + 1] * 0.125f);
+    y[(((int64_t)bi * cy + j) * cz + k) * C8 + c8] = o;
+}
+
 // Gradient of the pool: dx (+)= dy / 8.
 __global__ void __launch_bounds__(256) k_pool2_bwd(const __nv_bfloat16 *__restrict__ dy, __nv_bfloat16 *dx, int B,
                                                    int NX, int NY, int NZ, int C, int accumulate) {
@@ -128,6 +162,25 @@ __global__ void __launch_bounds__(256) k_up2(const __nv_bfloat16 *__restrict__ x
         const int64_t cv = (((int64_t)b * (NX / 2) + i / 2) * (NY / 2) + j / 2) * (NZ / 2) + k / 2;
         y[q] = x[cv * C + c];
     }
+}
+
+// The same upsample for C % 8 == 0: thread t of fine row (b, i, j) copies
+// channels 8 c8 .. 8 c8 + 7 of coarse voxel K into fine voxels 2K and 2K + 1
+// (one 16-byte load, two 16-byte stores), with t = K * (C / 8) + c8.
+// Grid: (ceil((NZ / 2) * (C / 8) / 128), NY, B * NX), 128 threads.
+__global__ void __launch_bounds__(128) k_up2_v8(const uint4 *__restrict__ x, uint4 *__restrict__ y, int NX, int NY,
+                                                int NZ, int C8) {
+    const int t = blockIdx.x * blockDim.x + threadIdx.x;
+    const int cz = NZ >> 1;
+    if (t >= cz * C8) return;
+    const int K = t / C8, c8 = t - K * C8;
+    const int j = blockIdx.y, bi = blockIdx.z;
+    const int b = bi / NX, i = bi - b * NX;
+    const int64_t crow = ((int64_t)b * (NX >> 1) + (i >> 1)) * (NY >> 1) + (j >> 1);
+    const uint4 v = __ldg(x + (crow * cz + K) * C8 + c8);
+    const int64_t f = (((int64_t)bi * NY + j) * NZ + 2 * K) * C8 + c8;
+    y[f] = v;
+    y[f + C8] = v;
 }
 
 // Gradient of the upsample: dx_coarse = sum of the 8 fine gradients.
@@ -329,8 +382,16 @@ int flub_unet_input(const float *div, const int32_t *tag, int B, int64_t ncell, 
 
 int flub_pool2_bf16(const void *x, void *y, int B, int NX, int NY, int NZ, int C, void *stream) {
     FLUB_REQUIRE(x && y && NX % 2 == 0 && NY % 2 == 0 && NZ % 2 == 0, "flub_pool2_bf16: bad arguments");
-    k_pool2<<<nb((int64_t)B * NX * NY * NZ * C / 8), 256, 0, as_stream(stream)>>>(
-        static_cast<const __nv_bfloat16 *>(x), static_cast<__nv_bfloat16 *>(y), B, NX, NY, NZ, C);
+    const bool v8 = C % 8 == 0 && (int64_t)B * (NX / 2) <= 65535 && NY / 2 <= 65535 &&
+                    ((uintptr_t)x | (uintptr_t)y) % 16 == 0;
+    if (v8) {
+        const int C8 = C / 8, units = (NZ / 2) * C8;
+        k_pool2_v8<<<dim3((unsigned)((units + 127) / 128), (unsigned)(NY / 2), (unsigned)(B * (NX / 2))), 128, 0,
+                     as_stream(stream)>>>(static_cast<const uint4 *>(x), static_cast<uint4 *>(y), NX, NY, NZ, C8);
+    } else {
+        k_pool2<<<nb((int64_t)B * NX * NY * NZ * C / 8), 256, 0, as_stream(stream)>>>(
+            static_cast<const __nv_bfloat16 *>(x), static_cast<__nv_bfloat16 *>(y), B, NX, NY, NZ, C);
+    }
     FLUB_CHECK_LAUNCH();
     return FLUB_OK;
 }
@@ -345,8 +406,16 @@ int flub_pool2_bwd_bf16(const void *dy, void *dx, int B, int NX, int NY, int NZ,
 
 int flub_up2_bf16(const void *x, void *y, int B, int NX, int NY, int NZ, int C, void *stream) {
     FLUB_REQUIRE(x && y, "flub_up2_bf16: bad arguments");
-    k_up2<<<nb((int64_t)B * NX * NY * NZ * C), 256, 0, as_stream(stream)>>>(
-        static_cast<const __nv_bfloat16 *>(x), static_cast<__nv_bfloat16 *>(y), B, NX, NY, NZ, C);
+    const bool v8 = C % 8 == 0 && NZ % 2 == 0 && (int64_t)B * NX <= 65535 && NY <= 65535 &&
+                    ((uintptr_t)x | (uintptr_t)y) % 16 == 0;
+    if (v8) {
+        const int C8 = C / 8, units = (NZ / 2) * C8;
+        k_up2_v8<<<dim3((unsigned)((units + 127) / 128), (unsigned)NY, (unsigned)(B * NX)), 128, 0,
+                   as_stream(stream)>>>(static_cast<const uint4 *>(x), static_cast<uint4 *>(y), NX, NY, NZ, C8);
+    } else {
+        k_up2<<<nb((int64_t)B * NX * NY * NZ * C), 256, 0, as_stream(stream)>>>(
+            static_cast<const __nv_bfloat16 *>(x), static_cast<__nv_bfloat16 *>(y), B, NX, NY, NZ, C);
+    }
     FLUB_CHECK_LAUNCH();
     return FLUB_OK;
 }

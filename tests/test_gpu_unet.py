@@ -115,6 +115,18 @@ def test_pool_up_relu_head_ops():
     pr = R.pool2(x.double())
     assert float((U.pool2(xd).double().cpu() - pr).abs().max()) <= 2.0 ** -8 * float(pr.abs().max())
     assert torch.equal(U.up2(xd).cpu(), R.up2(x))
+    # the 8 children summed in FP32 in (di, dj, dk) order, then / 8, rounded to BF16
+    xf, s = x.float(), 0.0
+    for d in range(8):
+        s = s + xf[:, d >> 2::2, (d >> 1) & 1::2, d & 1::2, :]
+    assert torch.equal(U.pool2(xd).cpu(), (s * 0.125).to(BF16))
+    # a channel count that is not a multiple of 8 (element-wise kernels)
+    x12 = _bf(_rand((1, 4, 6, 2, 12), g))
+    assert torch.equal(U.up2(x12.to(_dev())).cpu(), R.up2(x12))
+    s12 = 0.0
+    for d in range(8):
+        s12 = s12 + x12.float()[:, d >> 2::2, (d >> 1) & 1::2, d & 1::2, :]
+    assert torch.equal(U.pool2(x12.to(_dev())).cpu(), (s12 * 0.125).to(BF16))
     # gradients
     dyc = _bf(_rand((2, 2, 3, 4, 32), g))
     dx = torch.zeros_like(xd)
@@ -279,6 +291,32 @@ def test_learned_pipeline_small():
         assert r["err_warm"] <= 1e-3 and r["err_cold"] <= 1e-3, r
 
 
+def _prolong_ref(xc, tc, tf):
+    """Cell-centred trilinear prolongation (tags: 0 air, 1 fluid, 2 solid):
+    fine fluid cell 2I + e takes weights 3/4 (cell I) and 1/4 (cell I - 1 for
+    e = 0, I + 1 for e = 1) per axis over the coarse cells inside the domain
+    that are not solid, renormalised; air contributes 0."""
+    out = np.zeros(tf.shape)
+    for i, j, k in zip(*np.nonzero(tf == 1)):
+        s = w = 0.0
+        for a in (0, 1):
+            for b in (0, 1):
+                for e in (0, 1):
+                    ii = i // 2 + (a * (1 if i & 1 else -1))
+                    jj = j // 2 + (b * (1 if j & 1 else -1))
+                    kk = k // 2 + (e * (1 if k & 1 else -1))
+                    if not (0 <= ii < tc.shape[0] and 0 <= jj < tc.shape[1] and 0 <= kk < tc.shape[2]):
+                        continue
+                    if tc[ii, jj, kk] == 2:
+                        continue
+                    wt = (0.25 if a else 0.75) * (0.25 if b else 0.75) * (0.25 if e else 0.75)
+                    w += wt
+                    if tc[ii, jj, kk] == 1:
+                        s += wt * xc[ii, jj, kk]
+        out[i, j, k] = s / w if w > 0 else 0.0
+    return out
+
+
 def test_warm_start_support_kernels_match_reference_formulas():
     """Level tags, restriction, trilinear prolongation and the device-scaled
     guess against plain float64 restatements on the CPU."""
@@ -314,6 +352,10 @@ def test_warm_start_support_kernels_match_reference_formulas():
     i = np.arange(32)
     exact = 1.0 + 0.5 * ((i + 0.5) / 2 - 0.5)
     assert np.allclose(f[1:-1, 5, 5], exact[1:-1], atol=1e-6)
+    # with solid, air and fluid cells: the renormalised weights of a float64 restatement
+    c1 = np.random.default_rng(8).standard_normal(t1.shape).astype(np.float32)
+    got = mg.prolong_vector(1, torch.as_tensor(c1).to(dev)).cpu().double().numpy()
+    assert np.allclose(got, _prolong_ref(c1.astype(np.float64), t1, t0), rtol=0, atol=1e-6 * np.abs(c1).max())
     # scaled guess: gamma = (d . b) / (d . L d)
     g = torch.Generator(device=dev).manual_seed(1)
     d = torch.randn(sc.shape, generator=g, device=dev) * (tagf == 1)
