@@ -70,7 +70,8 @@ def parse_args():
                     help="skip the FP64 host projection that checks each variant's pressure")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-scale512", action="store_true", help="skip the 512^3 dam-break timings")
-    ap.add_argument("--profile-kernel", choices=["smooth", "restrict", "matvec", "solve", "project", "advect"],
+    ap.add_argument("--profile-kernel",
+                    choices=["smooth", "restrict", "matvec", "solve", "project", "advect", "warmstart"],
                     default=None,
                     help="set up the 256^3 solver state and launch only this kernel 3 times (for ncu)")
     return ap.parse_args()
@@ -147,6 +148,12 @@ def run_profile_kernel(args):
     elif args.profile_kernel == "solve":
         # two CG iterations (with FLUB_SOLVE_HOST_LOOP=1 every kernel is a separate launch)
         mg.solve(2, 1e-12, 0.0, 1e-12, smoother="phases")
+    elif args.profile_kernel == "warmstart":
+        # the network's guess for this right-hand side, twice, eagerly (each
+        # pass: restriction to 64^3, ten convolutions, prolongation to 256^3)
+        ws = learned.WarmStart(UNet3D.load(learned.WEIGHTS))
+        for _ in range(2):
+            ws.guess(mg)
     else:
         for _ in range(3):
             mg.apply_preconditioner()

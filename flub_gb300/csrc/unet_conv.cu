@@ -242,6 +242,225 @@ __global__ void __launch_bounds__(kConvThreads, 1)
     if (warp == 0) asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(kCols));
 }
 
+// ---------------------------------------------------------------- halo-plane forward kernel
+//
+// The same convolution for NZ % 8 == 0 and NY % 16 == 0 when the layer's
+// weights fit in shared memory, organised around input planes instead of
+// tap-shifted tiles, with no TMA and no waits between MMAs.
+//
+// A CTA owns a 16 (y) x 8 (z) voxel tile at xr consecutive x planes x0 ..
+// x0 + xr - 1; GEMM row m is voxel (y0 + m / 8, z0 + m % 8).  First all 128
+// threads stage, with coalesced 16-byte loads:
+//   - input plane p (x = x0 - 1 + p, p = 0 .. xr + 1) of each source as the
+//     haloed 18 x 10 voxel region, zero outside the volume (the padding), in
+//     the no-swizzle K-major layout
+//         [chunk of 8 channels][y 0..17][z 0..9][8 channels]   (16-byte rows);
+//   - every tap's weights, [tap][chunk][Cout][8 channels], the same layout
+//     for the B operand (core matrix = 8 output channels x 16 bytes).
+// A proxy fence publishes them to the tensor core.  The A operand of tap
+// (dx, dy, dz) for output plane xi is plane xi + dx + 1 read from start
+// offset ((dy + 1) * 10 + dz + 1) * 16 bytes: a core matrix is the 8 z-voxels
+// of one y-row (128 contiguous bytes), core matrices adjacent in M are one
+// padded row apart (SBO = 160 bytes) and adjacent chunks one chunk region apart
+// (LBO = kHaloChunk).  So all 27 taps read one copy of the data, and one
+// thread then issues every MMA of the CTA back to back into xr FP32
+// accumulators side by side in TMEM (columns xi * Cout ...).
+//
+// Staging the weights with plain loads matters: per-tap TMA boxes of a few
+// hundred bytes, requested by many CTAs per SM, arrived about 0.4 us apart
+// and left the MMA thread waiting on every tap.
+constexpr int kHaloZ = 10, kHaloY = 18;
+constexpr int kHaloRows = kHaloZ * kHaloY;                      // 16-byte rows per chunk (180)
+constexpr int kHaloChunk = (kHaloRows * 16 + 127) / 128 * 128;  // chunk region, 128-byte aligned (2944)
+
+struct HaloGeom {
+    int B, NX, NY, NZ;
+    int xr;                 // output planes per CTA
+    int cin0, cin1, relu;   // cin1 = 0: one source
+    int plane0, plane1;     // bytes of one input plane per source (chunks x kHaloChunk)
+    int planes1_off;        // offset of source 1's planes
+    int w0_off, w1_off;     // weights of source 0 and 1 (27 taps each)
+    int bar_off;            // completion mbarrier and TMEM slot
+    uint32_t tmem_cols;
+};
+
+// tcgen05 shared-memory matrix descriptor, K-major without swizzle: core
+// matrices of 8 rows x 16 bytes; lbo = bytes between core matrices adjacent
+// in K, sbo = bytes between core matrices adjacent in M (or N).
+__device__ __forceinline__ uint64_t ns_desc(uint32_t saddr, uint32_t lbo, uint32_t sbo) {
+    uint64_t d = 0;
+    d |= (uint64_t)((saddr & 0x3FFFFu) >> 4);
+    d |= (uint64_t)((lbo >> 4) & 0x3FFFu) << 16;
+    d |= (uint64_t)((sbo >> 4) & 0x3FFFu) << 32;
+    d |= (uint64_t)1 << 46;  // descriptor version; layout type 0 (no swizzle) in bits 61-63
+    return d;
+}
+
+// Stages the np haloed input planes of one source into dst (layout above).
+// Item q = ((p * 18 + yh) * 10 + zh) * C8 + c, chunks fastest, so that a
+// warp's loads cover whole voxel rows of the channels-last input.  Eight
+// loads are in flight per thread before their stores.
+__device__ __forceinline__ void halo_stage(const uint4 *__restrict__ x, unsigned char *dst, int c8_log2, int np,
+                                           int plane_bytes, int b, int x0, int y0, int z0, const HaloGeom &g) {
+    const int C8 = 1 << c8_log2;
+    const int total = np * kHaloRows * C8;
+    for (int base = 0; base < total; base += 8 * kConvThreads) {
+        uint4 v[8];
+        int off[8];
+#pragma unroll
+        for (int u = 0; u < 8; u++) {
+            const int q = base + u * kConvThreads + threadIdx.x;
+            off[u] = -1;
+            v[u] = make_uint4(0u, 0u, 0u, 0u);
+            if (q < total) {
+                const int c = q & (C8 - 1);
+                int r = q >> c8_log2;
+                const int zh = r % kHaloZ;
+                r /= kHaloZ;
+                const int yh = r % kHaloY, p = r / kHaloY;
+                const int xx = x0 - 1 + p, yy = y0 - 1 + yh, zz = z0 - 1 + zh;
+                off[u] = p * plane_bytes + c * kHaloChunk + (yh * kHaloZ + zh) * 16;
+                if ((unsigned)xx < (unsigned)g.NX && (unsigned)yy < (unsigned)g.NY && (unsigned)zz < (unsigned)g.NZ)
+                    v[u] = __ldg(x + ((((int64_t)b * g.NX + xx) * g.NY + yy) * g.NZ + zz) * C8 + c);
+            }
+        }
+#pragma unroll
+        for (int u = 0; u < 8; u++)
+            if (off[u] >= 0) *reinterpret_cast<uint4 *>(dst + off[u]) = v[u];
+    }
+}
+
+// Stages weights [27][COUT][Cin] (Cin = 8 << c8_log2) as [tap][chunk][COUT][8].
+template <int COUT>
+__device__ __forceinline__ void halo_stage_weights(const uint4 *__restrict__ w, unsigned char *dst, int c8_log2) {
+    const int C8 = 1 << c8_log2;
+    const int total = 27 * COUT * C8;
+    for (int q = threadIdx.x; q < total; q += kConvThreads) {
+        const int c = q & (C8 - 1);
+        const int r = q >> c8_log2;  // tap * COUT + co
+        const int tap = r / COUT, co = r - tap * COUT;
+        *reinterpret_cast<uint4 *>(dst + (((tap << c8_log2) + c) * COUT + co) * 16) = __ldg(w + q);
+    }
+}
+
+template <int COUT>
+__global__ void __launch_bounds__(kConvThreads, 1)
+    k_conv3d_halo(const __nv_bfloat16 *__restrict__ x0p, const __nv_bfloat16 *__restrict__ w0p,
+                  const __nv_bfloat16 *__restrict__ x1p, const __nv_bfloat16 *__restrict__ w1p, const HaloGeom g,
+                  const float *__restrict__ bias, __nv_bfloat16 *__restrict__ y) {
+    extern __shared__ unsigned char conv_smem_raw[];
+    unsigned char *smem = reinterpret_cast<unsigned char *>(
+        (reinterpret_cast<uintptr_t>(conv_smem_raw) + 1023) & ~static_cast<uintptr_t>(1023));
+    unsigned char *planes1 = smem + g.planes1_off;
+    uint64_t *done = reinterpret_cast<uint64_t *>(smem + g.bar_off);
+    uint32_t *tmem_slot = reinterpret_cast<uint32_t *>(done + 1);
+    __shared__ int fail;
+
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    int t = blockIdx.x;
+    const int tz = g.NZ >> 3, ty = g.NY >> 4, tx = g.NX / g.xr;
+    const int z0 = (t % tz) * 8;
+    t /= tz;
+    const int y0 = (t % ty) * 16;
+    t /= ty;
+    const int x0 = (t % tx) * g.xr, b = t / tx;
+    const int nsrc = g.cin1 > 0 ? 2 : 1;
+    const int lg0 = g.cin0 == 16 ? 1 : (g.cin0 == 32 ? 2 : 3), lg1 = g.cin1 == 16 ? 1 : (g.cin1 == 32 ? 2 : 3);
+
+    if (threadIdx.x == 0) {
+        fail = 0;
+        asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_u32(done)));
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    }
+    if (warp == 0) {
+        asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(tmem_slot)),
+                     "r"(g.tmem_cols));
+        asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;");
+    }
+
+    // every input plane and every weight once, by all threads; then visible
+    // to the tensor core
+    halo_stage(reinterpret_cast<const uint4 *>(x0p), smem, lg0, g.xr + 2, g.plane0, b, x0, y0, z0, g);
+    halo_stage_weights<COUT>(reinterpret_cast<const uint4 *>(w0p), smem + g.w0_off, lg0);
+    if (nsrc > 1) {
+        halo_stage(reinterpret_cast<const uint4 *>(x1p), planes1, lg1, g.xr + 2, g.plane1, b, x0, y0, z0, g);
+        halo_stage_weights<COUT>(reinterpret_cast<const uint4 *>(w1p), smem + g.w1_off, lg1);
+    }
+    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+    asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+    __syncthreads();
+    asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+    const uint32_t tmem = *tmem_slot;
+
+    if (threadIdx.x == 32) {
+        // MMA issuer: 27 taps x sources x planes x (Cin / 16), then one commit
+        const uint32_t idesc = mma_idesc(COUT);
+        for (int src = 0; src < nsrc; src++) {
+            const int lg = src ? lg1 : lg0, ksteps = 1 << (lg - 1);
+            const int pl = src ? g.plane1 : g.plane0;
+            const uint32_t pbase = smem_u32(src ? planes1 : smem);
+            const uint32_t wbase = smem_u32(smem + (src ? g.w1_off : g.w0_off));
+            const uint64_t pstep = (uint64_t)(pl >> 4);
+            for (int tap = 0; tap < 27; tap++) {
+                const int dx = tap / 9 - 1, dy = (tap / 3) % 3 - 1, dz = tap % 3 - 1;
+                const uint32_t off = (uint32_t)(((dy + 1) * kHaloZ + dz + 1) * 16);
+                // descriptors of (xi = 0, kk = 0); the start address field
+                // (16-byte units) advances by one plane per xi and by two
+                // chunks per kk
+                const uint64_t a0 = ns_desc(pbase + (uint32_t)((dx + 1) * pl) + off, kHaloChunk, kHaloZ * 16);
+                const uint64_t b0 = ns_desc(wbase + (uint32_t)(tap << lg) * (COUT * 16), COUT * 16, 128);
+                const uint32_t acc = (tap > 0 || src > 0) ? 1u : 0u;
+                uint64_t ax = a0;
+                uint32_t d = tmem;
+                for (int xi = 0; xi < g.xr; xi++, ax += pstep, d += COUT) {
+#pragma unroll 1
+                    for (int kk = 0; kk < ksteps; kk++) {
+                        const uint64_t ad = ax + (uint64_t)(kk * (2 * kHaloChunk >> 4));
+                        const uint64_t bd = b0 + (uint64_t)(kk * (2 * COUT * 16 >> 4));
+                        asm volatile(
+                            "{\n\t.reg .pred p;\n\tsetp.ne.b32 p, %4, 0;\n\t"
+                            "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n\t}" ::"r"(d),
+                            "l"(ad), "l"(bd), "r"(idesc), "r"(acc | (uint32_t)kk));
+                    }
+                }
+            }
+        }
+        asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(
+            smem_u32(done))
+                     : "memory");
+    }
+    __syncwarp();
+    // epilogue: row m of each accumulator is TMEM lane m, owned by warp m / 32
+    const bool got = __all_sync(0xffffffffu, mbar_wait(smem_u32(done), 0) ? 1 : 0) != 0;
+    if (!got) fail = 1;
+    asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+    const int m = warp * 32 + lane;
+    const int yy = y0 + (m >> 3), zz = z0 + (m & 7);
+    if (got) {
+        for (int xi = 0; xi < g.xr; xi++) {
+            float acc[COUT];
+#pragma unroll
+            for (int c = 0; c < COUT; c += 16)
+                tmem_ld16(tmem + ((uint32_t)(warp * 32) << 16) + (uint32_t)(xi * COUT + c), acc + c);
+            __align__(16) __nv_bfloat16 out[COUT];
+#pragma unroll
+            for (int c = 0; c < COUT; c++) {
+                float v = acc[c] + (bias ? __ldg(bias + c) : 0.0f);
+                if (g.relu) v = fmaxf(v, 0.0f);
+                out[c] = __float2bfloat16_rn(v);
+            }
+            const int64_t vox = (((int64_t)b * g.NX + x0 + xi) * g.NY + yy) * g.NZ + zz;
+            uint4 *dst = reinterpret_cast<uint4 *>(y + vox * COUT);
+#pragma unroll
+            for (int q = 0; q < COUT / 8; q++) dst[q] = reinterpret_cast<const uint4 *>(out)[q];
+        }
+    }
+    asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+    __syncthreads();
+    if (fail && threadIdx.x == 0) atomicExch(&g_conv_error, 1);
+    if (warp == 0) asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(g.tmem_cols));
+}
+
 // ---------------------------------------------------------------- weight gradient
 //
 //   dW[tap][co][ci] = sum over voxels v of X[v + off(tap)][ci] * dY[v][co]
@@ -498,6 +717,86 @@ static int launch_conv(const CUtensorMap &mx0, const CUtensorMap &mw0, const CUt
 
 static bool aligned16(const void *p) { return (reinterpret_cast<uintptr_t>(p) & 15) == 0; }
 
+// opt-in shared memory per block less an allowance for the kernel's static shared variables
+constexpr int kHaloSmemMax = 227 * 1024 - 128;
+
+static inline int align_up(int v, int a) { return (v + a - 1) / a * a; }
+
+// Shared-memory layout of k_conv3d_halo for xr planes; returns the dynamic
+// shared memory size (including the 1 KB alignment slack).
+static size_t halo_layout(HaloGeom &h, int cout) {
+    h.plane0 = (h.cin0 >> 3) * kHaloChunk;
+    h.plane1 = (h.cin1 >> 3) * kHaloChunk;
+    const int np = h.xr + 2;
+    h.planes1_off = np * h.plane0;
+    h.w0_off = h.planes1_off + np * h.plane1;
+    h.w1_off = h.w0_off + 27 * cout * h.cin0 * 2;
+    h.bar_off = align_up(h.w1_off + 27 * cout * h.cin1 * 2, 16);
+    uint32_t cols = 32;
+    while (cols < (uint32_t)(h.xr * cout)) cols <<= 1;
+    h.tmem_cols = cols;
+    return (size_t)h.bar_off + 16 /* mbarrier, TMEM slot */ + 1024;
+}
+
+static bool halo_enabled() {
+    const char *e = getenv("FLUB_CONV_HALO");
+    return !(e && e[0] == '0');
+}
+
+// FLUB_CONV_XR=n forces n planes per CTA (1, 2, 4 or 8) where it fits.
+static int forced_xr() {
+    const char *e = getenv("FLUB_CONV_XR");
+    return e ? atoi(e) : 0;
+}
+
+// Chooses the planes per CTA for k_conv3d_halo: the largest xr in {8, 4, 2, 1}
+// that divides NX, keeps the accumulators within 256 TMEM columns and the
+// planes and weights within shared memory, and still gives at least three
+// CTAs per SM (xr = 1 when none does).  Returns 0 when the layer goes to
+// k_conv3d_tc instead: its weights do not fit beside three planes, or it has
+// two sources and a shape k_conv3d_tc takes.  Both kernels run the same count of M = 128, N = Cout, K = 16
+// MMAs, which at N = 16 to 64 are bound by the SM reading their A operand
+// (about 44 cycles for one 128 x 16 BF16 tile); the halo kernel saves the
+// tap-shifted tile loads, and wins where its planes and weights leave room
+// for several CTAs per SM.  For the two-source decoder layers they do not,
+// and the tap-tile kernel measured faster.  FLUB_CONV_XR forces the halo
+// kernel wherever it fits.
+static size_t halo_plan(HaloGeom &h, int cout) {
+    if (h.NZ % 8 || h.NY % 16 || !halo_enabled()) return 0;
+    const int64_t tiles = (int64_t)h.B * (h.NY / 16) * (h.NZ / 8);
+    const int fx = forced_xr();
+    const int nzb = h.NZ < 128 ? h.NZ : 128;
+    const bool tap_ok = 128 % nzb == 0 && h.NZ % nzb == 0 && h.NY % (128 / nzb) == 0;
+    if (!fx && h.cin1 > 0 && tap_ok) return 0;
+    for (int xr = 8; xr >= 1; xr >>= 1) {
+        if (fx && xr != fx) continue;
+        if (h.NX % xr || xr * cout > 256) continue;
+        if (!fx && xr > 1 && tiles * (h.NX / xr) < 3 * kNumSMs) continue;
+        h.xr = xr;
+        const size_t smem = halo_layout(h, cout);
+        if (smem <= (size_t)kHaloSmemMax) return smem;
+    }
+    return 0;
+}
+
+template <int COUT>
+static int launch_halo(const void *x0, const void *w0, const void *x1, const void *w1, const HaloGeom &h, size_t smem,
+                       const float *bias, __nv_bfloat16 *y, cudaStream_t s) {
+    static size_t attr_smem = 0;  // largest dynamic shared memory enabled so far
+    if (smem > attr_smem) {
+        FLUB_CHECK_CUDA(
+            cudaFuncSetAttribute(k_conv3d_halo<COUT>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+        attr_smem = smem;
+    }
+    const unsigned ctas = (unsigned)((int64_t)h.B * (h.NX / h.xr) * (h.NY / 16) * (h.NZ / 8));
+    k_conv3d_halo<COUT><<<ctas, kConvThreads, smem, s>>>(
+        static_cast<const __nv_bfloat16 *>(x0), static_cast<const __nv_bfloat16 *>(w0),
+        static_cast<const __nv_bfloat16 *>(x1 ? x1 : x0), static_cast<const __nv_bfloat16 *>(w1 ? w1 : w0), h, bias,
+        y);
+    FLUB_CHECK_LAUNCH();
+    return FLUB_OK;
+}
+
 }  // namespace flub
 
 using namespace flub;
@@ -512,6 +811,26 @@ extern "C" int flub_conv3d_bf16(const void *x0, int cin0, const void *w0, const 
     FLUB_REQUIRE(B > 0 && NX > 0 && NY > 0 && NZ > 0, "flub_conv3d_bf16: bad shape");
     FLUB_REQUIRE(aligned16(x0) && aligned16(w0) && aligned16(y) && (!x1 || (aligned16(x1) && aligned16(w1))),
                  "flub_conv3d_bf16: pointers must be 16-byte aligned");
+    int st = get_encode();
+    if (st) return st;
+    {
+        HaloGeom h;
+        memset(&h, 0, sizeof(h));
+        h.B = B; h.NX = NX; h.NY = NY; h.NZ = NZ;
+        h.cin0 = cin0;
+        h.cin1 = x1 ? cin1 : 0;
+        h.relu = relu ? 1 : 0;
+        const size_t smem = halo_plan(h, cout);
+        if (smem) {
+            cudaStream_t s = as_stream(stream);
+            __nv_bfloat16 *yo = static_cast<__nv_bfloat16 *>(y);
+            switch (cout) {
+            case 16: return launch_halo<16>(x0, w0, x1, w1, h, smem, bias, yo, s);
+            case 32: return launch_halo<32>(x0, w0, x1, w1, h, smem, bias, yo, s);
+            default: return launch_halo<64>(x0, w0, x1, w1, h, smem, bias, yo, s);
+            }
+        }
+    }
     ConvGeom g;
     g.B = B; g.NX = NX; g.NY = NY; g.NZ = NZ;
     g.nzb = NZ < 128 ? NZ : 128;
@@ -528,8 +847,6 @@ extern "C" int flub_conv3d_bf16(const void *x0, int cin0, const void *w0, const 
         g.a_bytes = 128 * cmax * 2;
         g.stage_bytes = (g.a_bytes + cout * cmax * 2 + 1023) & ~1023;
     }
-    int st = get_encode();
-    if (st) return st;
     CUtensorMap mx0, mw0, mx1, mw1;
     if ((st = make_act_map(&mx0, x0, cin0, g)) || (st = make_w_map(&mw0, w0, cin0, cout))) return st;
     if (x1) {

@@ -41,6 +41,12 @@ CONV_CASES = [
     (1, 2, 8, 16, 64, 0, 16),
     (1, 4, 4, 32, 64, 32, 32),
     (2, 2, 8, 16, 32, 16, 16),
+    # NY % 16 == 0 and NZ % 8 == 0: the halo-plane kernel (NZ = 24 only there)
+    (1, 5, 16, 8, 16, 0, 16),
+    (2, 4, 32, 16, 16, 0, 32),
+    (1, 3, 16, 24, 32, 16, 16),
+    (1, 6, 16, 16, 64, 32, 32),
+    (1, 2, 16, 8, 64, 0, 64),
 ]
 
 
@@ -67,6 +73,39 @@ def test_conv3d_matches_float64(case):
         # FP32 accumulation, BF16 output: a few BF16 ulps of the output scale
         assert float(err.max()) <= 1e-2 * float(ref.abs().max()) + 1e-6, (case, relu, float(err.max()))
         assert _rel(y, ref) <= 4e-3, (case, relu)
+
+
+@pytest.mark.parametrize("case", [(1, 64, 64, 64, 16, 0, 16), (1, 64, 64, 64, 32, 16, 16), (1, 32, 32, 32, 64, 32, 32),
+                                  (2, 32, 32, 32, 16, 0, 32)])
+def test_conv3d_halo_planes_at_network_sizes(case, monkeypatch):
+    """The U-Net's own layer shapes, where the halo-plane kernel marches up
+    to 8 x planes per CTA: against float64 and against the tap-tile kernel
+    (FLUB_CONV_HALO=0), which accumulates the same products in another order."""
+    from flub_gb300 import unet as U
+    from oracle import unet_ref as R
+    B, X, Y, Z, c0, c1, co = case
+    g = torch.Generator().manual_seed(11)
+    x0 = _bf(_rand((B, X, Y, Z, c0), g))
+    w0 = _bf(_rand((27, co, c0), g, 1.0 / math.sqrt(27 * c0)))
+    x1 = _bf(_rand((B, X, Y, Z, c1), g)) if c1 else None
+    w1 = _bf(_rand((27, co, c1), g, 1.0 / math.sqrt(27 * c1))) if c1 else None
+    bias = _rand((co,), g, 0.1).float()
+    args = (x0.to(_dev()), w0.to(_dev()), x1.to(_dev()) if c1 else None, w1.to(_dev()) if c1 else None,
+            bias.to(_dev()))
+    U.conv_error(reset=True)
+    y = U.conv3d(*args, relu=True)
+    monkeypatch.setenv("FLUB_CONV_HALO", "0")
+    y_tap = U.conv3d(*args, relu=True)
+    monkeypatch.delenv("FLUB_CONV_HALO")
+    torch.cuda.synchronize()
+    assert U.conv_error() == 0
+    ref = R.conv3d(x0.double(), w0.double(), x1.double() if c1 else None, w1.double() if c1 else None,
+                   bias.double(), relu=True)
+    assert _rel(y, ref) <= 4e-3
+    assert float((y.double().cpu() - ref).abs().max()) <= 1e-2 * float(ref.abs().max())
+    # the two kernels round the same FP32 sums differently: at most a BF16 ulp or two apart
+    d = (y.double() - y_tap.double()).abs()
+    assert float(d.max()) <= 2.0 ** -6 * float(y_tap.double().abs().max())
 
 
 @pytest.mark.parametrize("case", [(1, 4, 8, 16, 16, 16), (2, 2, 4, 32, 32, 64), (1, 2, 2, 64, 64, 32),
