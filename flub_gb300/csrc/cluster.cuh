@@ -75,28 +75,61 @@ __device__ __forceinline__ float *cl_r(const ClusterCtx &x, const ClusterLevel &
     return reinterpret_cast<float *>(x.smem + L.off_r);
 }
 
-// Update of one cell from shared memory.  zs/cs use the ghost-padded layout
-// (plane 0 and P+1 are ghosts); c is the index of the cell in that layout.
+// The codes and z of a cell's six neighbours from shared memory (zs/cs in
+// the ghost-padded layout: plane 0 and P+1 are ghosts; c is the cell's index
+// there).  Everything is loaded before anything is tested (a neighbour past
+// the j or k edge reads the cell itself and counts as solid), so the loads
+// issue together instead of one after another behind each test.
+struct ClNb {
+    uint8_t cc, cip, cim, cjp, cjm, ckp, ckm;
+    float xc, zip, zim, zjp, zjm, zkp, zkm;
+};
+
+__device__ __forceinline__ ClNb cl_nb(const float *zs, const uint8_t *cs, int c, int j, int k, const Dims D) {
+    const int sj = D.nz, si = D.ny * D.nz;
+    const bool jp = j + 1 < D.ny, jm = j > 0, kp = k + 1 < D.nz, km = k > 0;
+    const int ijp = jp ? c + sj : c, ijm = jm ? c - sj : c, ikp = kp ? c + 1 : c, ikm = km ? c - 1 : c;
+    ClNb n;
+    n.cc = cs[c];
+    n.cip = cs[c + si];
+    n.cim = cs[c - si];
+    const uint8_t cjp = cs[ijp], cjm = cs[ijm], ckp = cs[ikp], ckm = cs[ikm];
+    n.xc = zs[c];
+    n.zip = zs[c + si];
+    n.zim = zs[c - si];
+    n.zjp = zs[ijp];
+    n.zjm = zs[ijm];
+    n.zkp = zs[ikp];
+    n.zkm = zs[ikm];
+    n.cjp = jp ? cjp : kCodeSolid;
+    n.cjm = jm ? cjm : kCodeSolid;
+    n.ckp = kp ? ckp : kCodeSolid;
+    n.ckm = km ? ckm : kCodeSolid;
+    return n;
+}
+
+// Neighbour sum of L z at a fluid cell (lap_at's operation order).
+__device__ __forceinline__ float cl_nb_sum(const ClNb &n) {
+    float ret = 0.0f;
+    ret = __fadd_rn(ret, __fadd_rn(nb_term(n.cip, n.cip == kCodeFluid ? n.zip : 0.0f, n.xc),
+                                   nb_term(n.cim, n.cim == kCodeFluid ? n.zim : 0.0f, n.xc)));
+    ret = __fadd_rn(ret, __fadd_rn(nb_term(n.cjp, n.cjp == kCodeFluid ? n.zjp : 0.0f, n.xc),
+                                   nb_term(n.cjm, n.cjm == kCodeFluid ? n.zjm : 0.0f, n.xc)));
+    ret = __fadd_rn(ret, __fadd_rn(nb_term(n.ckp, n.ckp == kCodeFluid ? n.zkp : 0.0f, n.xc),
+                                   nb_term(n.ckm, n.ckm == kCodeFluid ? n.zkm : 0.0f, n.xc)));
+    return ret;
+}
+
+// Update of one cell from shared memory.
 __device__ __forceinline__ float cl_update(const float *zs, const uint8_t *cs, int c, int j, int k, const Dims D,
                                            float rc, bool from_zero) {
-    if (cs[c] != kCodeFluid) return 0.0f;
-    const int sj = D.nz, si = D.ny * D.nz;
-    const uint8_t cip = cs[c + si], cim = cs[c - si];
-    const uint8_t cjp = j + 1 < D.ny ? cs[c + sj] : kCodeSolid, cjm = j > 0 ? cs[c - sj] : kCodeSolid;
-    const uint8_t ckp = k + 1 < D.nz ? cs[c + 1] : kCodeSolid, ckm = k > 0 ? cs[c - 1] : kCodeSolid;
-    const int d = (cip != kCodeSolid) + (cim != kCodeSolid) + (cjp != kCodeSolid) + (cjm != kCodeSolid) +
-                  (ckp != kCodeSolid) + (ckm != kCodeSolid);
+    const ClNb n = cl_nb(zs, cs, c, j, k, D);
+    if (n.cc != kCodeFluid) return 0.0f;
+    const int d = (n.cip != kCodeSolid) + (n.cim != kCodeSolid) + (n.cjp != kCodeSolid) + (n.cjm != kCodeSolid) +
+                  (n.ckp != kCodeSolid) + (n.ckm != kCodeSolid);
     if (d == 0) return 0.0f;
     if (from_zero) return __fdiv_rn(rc, (float)d);
-    const float xc = zs[c];
-    float ret = 0.0f;
-    ret = __fadd_rn(ret, __fadd_rn(nb_term(cip, cip == kCodeFluid ? zs[c + si] : 0.0f, xc),
-                                   nb_term(cim, cim == kCodeFluid ? zs[c - si] : 0.0f, xc)));
-    ret = __fadd_rn(ret, __fadd_rn(nb_term(cjp, cjp == kCodeFluid ? zs[c + sj] : 0.0f, xc),
-                                   nb_term(cjm, cjm == kCodeFluid ? zs[c - sj] : 0.0f, xc)));
-    ret = __fadd_rn(ret, __fadd_rn(nb_term(ckp, ckp == kCodeFluid ? zs[c + 1] : 0.0f, xc),
-                                   nb_term(ckm, ckm == kCodeFluid ? zs[c - 1] : 0.0f, xc)));
-    return __fadd_rn(xc, __fdiv_rn(__fadd_rn(rc, ret), (float)d));
+    return __fadd_rn(n.xc, __fdiv_rn(__fadd_rn(rc, cl_nb_sum(n)), (float)d));
 }
 
 // r of an owned cell (the first level's r is copied from global memory at start).
@@ -124,20 +157,8 @@ __device__ __forceinline__ void cl_store(const ClusterCtx &x, const ClusterLevel
 
 // L z at an owned cell (0 off the fluid), for the restriction.
 __device__ __forceinline__ float cl_lap(const float *zs, const uint8_t *cs, int c, int j, int k, const Dims D) {
-    if (cs[c] != kCodeFluid) return 0.0f;
-    const int sj = D.nz, si = D.ny * D.nz;
-    const uint8_t cip = cs[c + si], cim = cs[c - si];
-    const uint8_t cjp = j + 1 < D.ny ? cs[c + sj] : kCodeSolid, cjm = j > 0 ? cs[c - sj] : kCodeSolid;
-    const uint8_t ckp = k + 1 < D.nz ? cs[c + 1] : kCodeSolid, ckm = k > 0 ? cs[c - 1] : kCodeSolid;
-    const float xc = zs[c];
-    float ret = 0.0f;
-    ret = __fadd_rn(ret, __fadd_rn(nb_term(cip, cip == kCodeFluid ? zs[c + si] : 0.0f, xc),
-                                   nb_term(cim, cim == kCodeFluid ? zs[c - si] : 0.0f, xc)));
-    ret = __fadd_rn(ret, __fadd_rn(nb_term(cjp, cjp == kCodeFluid ? zs[c + sj] : 0.0f, xc),
-                                   nb_term(cjm, cjm == kCodeFluid ? zs[c - sj] : 0.0f, xc)));
-    ret = __fadd_rn(ret, __fadd_rn(nb_term(ckp, ckp == kCodeFluid ? zs[c + 1] : 0.0f, xc),
-                                   nb_term(ckm, ckm == kCodeFluid ? zs[c - 1] : 0.0f, xc)));
-    return ret;
+    const ClNb n = cl_nb(zs, cs, c, j, k, D);
+    return n.cc != kCodeFluid ? 0.0f : cl_nb_sum(n);
 }
 
 // One red-black half-sweep of level t (mgpcg.py:72-86), then a cluster barrier.

@@ -200,6 +200,7 @@ static size_t tail_layout(const flub_mg *mg, int lt, TailParams *P) {
         T.off_z = take(sizeof(float) * n);
         T.off_r = take(sizeof(float) * n);
         T.off_c = take(n);
+        T.off_v = l + 1 < mg->levels ? take(sizeof(float) * n) : -1;
     }
     P->nt = mg->levels - lt;
     P->nu = mg->sched_nu;

@@ -24,6 +24,7 @@ struct TailLevel {
     const uint8_t *code;  // global cell codes of this level
     int abs_level;        // level index in the full hierarchy (sets 6 << l)
     int off_z, off_r, off_c;  // byte offsets in shared memory
+    int off_v;                // fine residual scratch for the restriction (-1 at the bottom level)
 };
 
 struct TailParams {
@@ -58,10 +59,9 @@ __device__ __forceinline__ uint32_t cell_mask(const uint8_t *code, const Dims D,
     const int si = D.ny * D.nz, sj = D.nz;
     uint32_t m = 0;
     auto nb = [&](bool inside, int off, int bit) {
-        if (!inside) return;
-        const uint8_t cn = code[c + off];
-        if (cn != kCodeSolid) m |= 1u << bit;
-        if (cn == kCodeAir) m |= 1u << (bit + 6);
+        const uint8_t cn = code[inside ? c + off : c];  // loaded either way: the loads issue together
+        if (inside && cn != kCodeSolid) m |= 1u << bit;
+        if (inside && cn == kCodeAir) m |= 1u << (bit + 6);
     };
     nb(i + 1 < D.nx, si, 0);
     nb(i > 0, -si, 1);
@@ -96,6 +96,28 @@ __device__ __forceinline__ void tail_cache(TailCache &tc, const uint8_t *code, c
     }
 }
 
+// Neighbour sum of L z at a fluid cell from its mask, in the operation order
+// of lap_at.  All six neighbours are loaded whether they count or not (an
+// excluded one reads the cell itself), so the loads issue together instead of
+// one after another behind each mask test: a dependent chain of shared loads
+// was most of a half-sweep's time.
+__device__ __forceinline__ float tail_lap(const float *z, int c, uint32_t m, int si, int sj) {
+    const float xc = z[c];
+    const float zip = z[(m & 1u) ? c + si : c], zim = z[(m & 2u) ? c - si : c];
+    const float zjp = z[(m & 4u) ? c + sj : c], zjm = z[(m & 8u) ? c - sj : c];
+    const float zkp = z[(m & 16u) ? c + 1 : c], zkm = z[(m & 32u) ? c - 1 : c];
+    float tp, tm, ret = 0.0f;
+    tp = (m & 1u) ? __fsub_rn((m & 64u) ? 0.0f : zip, xc) : 0.0f;
+    tm = (m & 2u) ? __fsub_rn((m & 128u) ? 0.0f : zim, xc) : 0.0f;
+    ret = __fadd_rn(ret, __fadd_rn(tp, tm));
+    tp = (m & 4u) ? __fsub_rn((m & 256u) ? 0.0f : zjp, xc) : 0.0f;
+    tm = (m & 8u) ? __fsub_rn((m & 512u) ? 0.0f : zjm, xc) : 0.0f;
+    ret = __fadd_rn(ret, __fadd_rn(tp, tm));
+    tp = (m & 16u) ? __fsub_rn((m & 1024u) ? 0.0f : zkp, xc) : 0.0f;
+    tm = (m & 32u) ? __fsub_rn((m & 2048u) ? 0.0f : zkm, xc) : 0.0f;
+    return __fadd_rn(ret, __fadd_rn(tp, tm));
+}
+
 // z update of one cell with the mask m (same operation order as lap_at).
 __device__ __forceinline__ float tail_update(const float *z, int c, uint32_t m, float rc, int si, int sj,
                                              bool from_zero) {
@@ -103,22 +125,29 @@ __device__ __forceinline__ float tail_update(const float *z, int c, uint32_t m, 
     const int d = __popc(m & 63u);
     if (d == 0) return 0.0f;
     if (from_zero) return __fdiv_rn(rc, (float)d);
-    const float xc = z[c];
-    float tp, tm, ret = 0.0f;
-    tp = (m & 1u) ? __fsub_rn((m & 64u) ? 0.0f : z[c + si], xc) : 0.0f;
-    tm = (m & 2u) ? __fsub_rn((m & 128u) ? 0.0f : z[c - si], xc) : 0.0f;
-    ret = __fadd_rn(ret, __fadd_rn(tp, tm));
-    tp = (m & 4u) ? __fsub_rn((m & 256u) ? 0.0f : z[c + sj], xc) : 0.0f;
-    tm = (m & 8u) ? __fsub_rn((m & 512u) ? 0.0f : z[c - sj], xc) : 0.0f;
-    ret = __fadd_rn(ret, __fadd_rn(tp, tm));
-    tp = (m & 16u) ? __fsub_rn((m & 1024u) ? 0.0f : z[c + 1], xc) : 0.0f;
-    tm = (m & 32u) ? __fsub_rn((m & 2048u) ? 0.0f : z[c - 1], xc) : 0.0f;
-    ret = __fadd_rn(ret, __fadd_rn(tp, tm));
-    return __fadd_rn(xc, __fdiv_rn(__fadd_rn(rc, ret), (float)d));
+    return __fadd_rn(z[c], __fdiv_rn(__fadd_rn(rc, tail_lap(z, c, m, si, sj)), (float)d));
+}
+
+// Threads that own a pair of the level: whole warps, all of them from 16^3
+// up (2048 pairs), the first 8 warps at 8^3.
+__device__ __forceinline__ int tail_threads(const Dims D) {
+    const int npairs = D.nx * D.ny * (D.nz >> 1);
+    const int w = (npairs + 31) & ~31;
+    return w < kTailThreads ? w : kTailThreads;
+}
+
+// Barrier among the first nthr threads: the block barrier when all take part,
+// else named barrier 1 (the threads above nthr own no cells of the level and
+// wait at the next block barrier instead).
+__device__ __forceinline__ void tail_sync(int nthr) {
+    if (nthr >= kTailThreads)
+        __syncthreads();
+    else
+        asm volatile("bar.sync 1, %0;" ::"r"(nthr) : "memory");
 }
 
 __device__ __forceinline__ void tail_half_lean(float *z, const TailCache &tc, const Dims D, int phase,
-                                               bool from_zero) {
+                                               bool from_zero, int nthr) {
     const int si = D.ny * D.nz, sj = D.nz;
 #pragma unroll
     for (int q = 0; q < kTailPairs; q++) {
@@ -131,12 +160,27 @@ __device__ __forceinline__ void tail_half_lean(float *z, const TailCache &tc, co
         z[cu] = zn;
         if (from_zero) z[odd ? c : c + 1] = 0.0f;
     }
-    __syncthreads();
+    tail_sync(nthr);
 }
 
-__device__ __forceinline__ void tail_restrict(const float *rf, const float *zf, const uint8_t *cf, float *rc,
-                                              const uint8_t *cc, const Dims C, float rscale) {
-    const Dims F{2 * C.nx, 2 * C.ny, 2 * C.nz};
+
+// Restriction of the residual r + L z (multigrid/mgpcg.py:306-318): first
+// every fine cell's r + L z (r alone off the fluid) into the scratch v, each
+// thread for the pairs it caches, then each coarse fluid cell sums its 8
+// children in (i, j, k) order and scales; coarse cells that are not fluid get
+// 0.  Same values, bit for bit, as summing r + lap_at per child.
+__device__ __forceinline__ void tail_restrict_cached(float *v, const float *zf, const TailCache &tc, const Dims F,
+                                                     float *rc, const uint8_t *cc, const Dims C, float rscale) {
+    const int si = F.ny * F.nz, sj = F.nz;
+#pragma unroll
+    for (int q = 0; q < kTailPairs; q++) {
+        const int c = tc.idx[q];
+        if (c < 0) continue;
+        const uint32_t m0 = tc.msk[q] & 0xffffu, m1 = tc.msk[q] >> 16;
+        v[c] = __fadd_rn(tc.r0[q], (m0 & (1u << 12)) ? tail_lap(zf, c, m0, si, sj) : 0.0f);
+        v[c + 1] = __fadd_rn(tc.r1[q], (m1 & (1u << 12)) ? tail_lap(zf, c + 1, m1, si, sj) : 0.0f);
+    }
+    __syncthreads();
     const int n = C.nx * C.ny * C.nz;
     for (int q = threadIdx.x; q < n; q += blockDim.x) {
         if (cc[q] != kCodeFluid) {
@@ -144,25 +188,15 @@ __device__ __forceinline__ void tail_restrict(const float *rf, const float *zf, 
             continue;
         }
         const int K = q % C.nz, J = (q / C.nz) % C.ny, I = q / (C.nz * C.ny);
-        float s = 0.0f;
-        bool first = true;
-#pragma unroll
-        for (int ii = 0; ii < 2; ii++)
-#pragma unroll
-            for (int jj = 0; jj < 2; jj++)
-#pragma unroll
-                for (int kk = 0; kk < 2; kk++) {
-                    const int i = 2 * I + ii, j = 2 * J + jj, k = 2 * K + kk;
-                    const int64_t c = ((int64_t)i * F.ny + j) * F.nz + k;
-                    float lz = 0.0f;
-                    if (cf[c] == kCodeFluid) {
-                        int d;
-                        lz = lap_at(zf, cf, i, j, k, F, c, zf[c], d);
-                    }
-                    const float v = __fadd_rn(rf[c], lz);
-                    s = first ? v : __fadd_rn(s, v);
-                    first = false;
-                }
+        const int c0 = ((2 * I) * F.ny + 2 * J) * F.nz + 2 * K;
+        float s = v[c0];
+        s = __fadd_rn(s, v[c0 + 1]);
+        s = __fadd_rn(s, v[c0 + sj]);
+        s = __fadd_rn(s, v[c0 + sj + 1]);
+        s = __fadd_rn(s, v[c0 + si]);
+        s = __fadd_rn(s, v[c0 + si + 1]);
+        s = __fadd_rn(s, v[c0 + si + sj]);
+        s = __fadd_rn(s, v[c0 + si + sj + 1]);
         rc[q] = __fmul_rn(s, rscale);
     }
     __syncthreads();
@@ -187,6 +221,19 @@ __device__ __forceinline__ void tail_run(const TailParams &P, unsigned char *sme
     auto Z = [&](int t) { return reinterpret_cast<float *>(smem + P.lv[t].off_z); };
     auto R = [&](int t) { return reinterpret_cast<float *>(smem + P.lv[t].off_r); };
     auto C = [&](int t) { return reinterpret_cast<uint8_t *>(smem + P.lv[t].off_c); };
+    auto V = [&](int t) { return reinterpret_cast<float *>(smem + P.lv[t].off_v); };
+    // the sweeps of a level on the threads that own its pairs; the others
+    // meet them at the block barrier after the loop
+    auto sweeps = [&](int t, const TailCache &tc, int iters, bool down) {
+        const Dims D = P.lv[t].D;
+        const int nthr = tail_threads(D);
+        if ((int)threadIdx.x < nthr)
+            for (int it = 0; it < iters; it++) {
+                tail_half_lean(Z(t), tc, D, down ? 0 : 1, down && it == 0, nthr);
+                tail_half_lean(Z(t), tc, D, down ? 1 : 0, false, nthr);
+            }
+        if (nthr < kTailThreads) __syncthreads();
+    };
     for (int t = 0; t < P.nt; t++) {
         const int n = P.lv[t].D.nx * P.lv[t].D.ny * P.lv[t].D.nz;
         uint8_t *c = C(t);
@@ -207,34 +254,17 @@ __device__ __forceinline__ void tail_run(const TailParams &P, unsigned char *sme
     for (int t = 0; t < nb; t++) {
         const Dims D = P.lv[t].D;
         tail_cache(tc, C(t), R(t), D);
-        const int iters = P.nu < 0 ? (6 << P.lv[t].abs_level) : P.nu;
-        for (int it = 0; it < iters; it++) {
-            tail_half_lean(Z(t), tc, D, 0, it == 0);
-            tail_half_lean(Z(t), tc, D, 1, false);
-        }
-        tail_restrict(R(t), Z(t), C(t), R(t + 1), C(t + 1), P.lv[t + 1].D, P.rscale);
+        sweeps(t, tc, P.nu < 0 ? (6 << P.lv[t].abs_level) : P.nu, true);
+        tail_restrict_cached(V(t), Z(t), tc, D, R(t + 1), C(t + 1), P.lv[t + 1].D, P.rscale);
     }
-    {
-        const Dims D = P.lv[nb].D;
-        tail_cache(tc, C(nb), R(nb), D);
-        for (int it = 0; it < P.nbottom; it++) {
-            tail_half_lean(Z(nb), tc, D, 0, it == 0);
-            tail_half_lean(Z(nb), tc, D, 1, false);
-        }
-        for (int it = 0; it < P.nbottom; it++) {
-            tail_half_lean(Z(nb), tc, D, 1, false);
-            tail_half_lean(Z(nb), tc, D, 0, false);
-        }
-    }
+    tail_cache(tc, C(nb), R(nb), P.lv[nb].D);
+    sweeps(nb, tc, P.nbottom, true);
+    sweeps(nb, tc, P.nbottom, false);
     for (int t = nb - 1; t >= 0; t--) {
         const Dims D = P.lv[t].D;
         tail_prolong(Z(t), Z(t + 1), D);
         tail_cache(tc, C(t), R(t), D);
-        const int iters = P.nu < 0 ? (6 << P.lv[t].abs_level) : P.nu;
-        for (int it = 0; it < iters; it++) {
-            tail_half_lean(Z(t), tc, D, 1, false);
-            tail_half_lean(Z(t), tc, D, 0, false);
-        }
+        sweeps(t, tc, P.nu < 0 ? (6 << P.lv[t].abs_level) : P.nu, false);
     }
     if (io) {
         const Dims D = P.lv[0].D;

@@ -17,6 +17,10 @@
 // issues the MMAs (one per 16 input channels), all four warps run the
 // epilogue (TMEM -> registers, bias, ReLU, BF16 store).  Every mbarrier wait
 // is bounded; a timeout sets the error word and the CTA still frees its TMEM.
+//
+// k_conv3d_halo (below) computes the same convolution from input planes
+// staged once per CTA; halo_plan chooses between the two kernels per layer.
+// The weight gradient (k_conv3d_wgrad_tc) is a third tcgen05 kernel.
 #include <cuda.h>
 #include <cuda_bf16.h>
 #include <cudaTypedefs.h>
@@ -753,21 +757,23 @@ static int forced_xr() {
 // that divides NX, keeps the accumulators within 256 TMEM columns and the
 // planes and weights within shared memory, and still gives at least three
 // CTAs per SM (xr = 1 when none does).  Returns 0 when the layer goes to
-// k_conv3d_tc instead: its weights do not fit beside three planes, or it has
-// two sources and a shape k_conv3d_tc takes.  Both kernels run the same count of M = 128, N = Cout, K = 16
-// MMAs, which at N = 16 to 64 are bound by the SM reading their A operand
-// (about 44 cycles for one 128 x 16 BF16 tile); the halo kernel saves the
-// tap-shifted tile loads, and wins where its planes and weights leave room
-// for several CTAs per SM.  For the two-source decoder layers they do not,
-// and the tap-tile kernel measured faster.  FLUB_CONV_XR forces the halo
-// kernel wherever it fits.
+// k_conv3d_tc instead: its weights do not fit beside three planes, or
+// k_conv3d_tc takes its shape and it has two sources or fewer tiles than SMs.
+// Both kernels run the same count of M = 128, N = Cout, K = 16 MMAs, which at
+// N = 16 to 64 are bound by the SM reading their A operand (about 44 cycles
+// for one 128 x 16 BF16 tile); the halo kernel saves the tap-shifted tile
+// loads, and wins where its planes and weights leave room for several CTAs
+// per SM.  For the two-source decoder layers they do not, and on grids of
+// fewer tiles than SMs (16^3) its staging is not hidden: the tap-tile kernel
+// measured faster in both cases.  FLUB_CONV_XR forces the halo kernel
+// wherever it fits.
 static size_t halo_plan(HaloGeom &h, int cout) {
     if (h.NZ % 8 || h.NY % 16 || !halo_enabled()) return 0;
     const int64_t tiles = (int64_t)h.B * (h.NY / 16) * (h.NZ / 8);
     const int fx = forced_xr();
     const int nzb = h.NZ < 128 ? h.NZ : 128;
     const bool tap_ok = 128 % nzb == 0 && h.NZ % nzb == 0 && h.NY % (128 / nzb) == 0;
-    if (!fx && h.cin1 > 0 && tap_ok) return 0;
+    if (!fx && tap_ok && (h.cin1 > 0 || tiles * h.NX < kNumSMs)) return 0;
     for (int xr = 8; xr >= 1; xr >>= 1) {
         if (fx && xr != fx) continue;
         if (h.NX % xr || xr * cout > 256) continue;
