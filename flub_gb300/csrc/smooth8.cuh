@@ -115,22 +115,20 @@ template <bool kFromZero>
 __device__ __forceinline__ float smooth_cell(uint32_t w, float xc, float xip, float xim, float xjp, float xjm,
                                              float xkp, float xkm, float r) {
     if (sw_code(w, 0) != kCodeFluid) return 0.0f;
-    int d = 0;
-    float tp, tm, ret = 0.0f;
-    uint32_t cn;
-    tp = 0.0f; tm = 0.0f;
-    cn = sw_code(w, 1); if (cn != kCodeSolid) { tp = __fsub_rn(cn == kCodeAir ? 0.0f : xip, xc); d++; }
-    cn = sw_code(w, 2); if (cn != kCodeSolid) { tm = __fsub_rn(cn == kCodeAir ? 0.0f : xim, xc); d++; }
-    ret = __fadd_rn(ret, __fadd_rn(tp, tm));
-    tp = 0.0f; tm = 0.0f;
-    cn = sw_code(w, 3); if (cn != kCodeSolid) { tp = __fsub_rn(cn == kCodeAir ? 0.0f : xjp, xc); d++; }
-    cn = sw_code(w, 4); if (cn != kCodeSolid) { tm = __fsub_rn(cn == kCodeAir ? 0.0f : xjm, xc); d++; }
-    ret = __fadd_rn(ret, __fadd_rn(tp, tm));
-    tp = 0.0f; tm = 0.0f;
-    cn = sw_code(w, 5); if (cn != kCodeSolid) { tp = __fsub_rn(cn == kCodeAir ? 0.0f : xkp, xc); d++; }
-    cn = sw_code(w, 6); if (cn != kCodeSolid) { tm = __fsub_rn(cn == kCodeAir ? 0.0f : xkm, xc); d++; }
-    ret = __fadd_rn(ret, __fadd_rn(tp, tm));
+    // neighbour q (1..6) sits at bits 2q, 2q + 1 with solid 0, air 1, fluid 2:
+    // bit 2q | bit 2q + 1 = "not solid" (it counts in d), bit 2q + 1 = "fluid"
+    // (its z enters; an air neighbour enters as 0)
+    const uint32_t ns = (w | (w >> 1)) & 0x1554u;
+    const int d = __popc(ns);
     if (d == 0) return 0.0f;
+    auto term = [&](int q, float xn) {
+        const float v = (w & (2u << (2 * q))) ? xn : 0.0f;
+        return (ns & (1u << (2 * q))) ? __fsub_rn(v, xc) : 0.0f;
+    };
+    float ret = 0.0f;
+    ret = __fadd_rn(ret, __fadd_rn(term(1, xip), term(2, xim)));
+    ret = __fadd_rn(ret, __fadd_rn(term(3, xjp), term(4, xjm)));
+    ret = __fadd_rn(ret, __fadd_rn(term(5, xkp), term(6, xkm)));
     return kFromZero ? __fdiv_rn(r, (float)d) : __fadd_rn(xc, __fdiv_rn(__fadd_rn(r, ret), (float)d));
 }
 
@@ -155,9 +153,11 @@ __device__ __forceinline__ float smooth_cell(uint32_t w, float xc, float xip, fl
 // without one every group is.
 // Grid: one-dimensional; each warp walks 16 groups (32 halves) per step,
 // grid-stride, so both lanes of a pair always run the same iterations.
-// Requires nz % 8 == 0.
+// Requires nz % 8 == 0.  The prolongation variant holds the coarse values as
+// well: 5 blocks per SM (51 registers) instead of 6 (40) keep it free of
+// spills.
 template <bool kFromZero, bool kProlong, typename TO, typename TI, typename TR, typename TC>
-__global__ void __launch_bounds__(256, 6) k_smooth8(TO *zout, const TI *zin, const TC *__restrict__ zc,
+__global__ void __launch_bounds__(256, kProlong ? 5 : 6) k_smooth8(TO *zout, const TI *zin, const TC *__restrict__ zc,
                                                     float zc_scale, const TR *__restrict__ r,
                                                     const uint8_t *__restrict__ code,
                                                     const uint16_t *__restrict__ sw, Dims D, int phase,
