@@ -49,24 +49,8 @@ __device__ __forceinline__ void lap_row8(const float *__restrict__ x, const uint
         out[m] = 0.0f;
         const uint32_t w = word_at(wd, m);
         if (sw_code(w, 0) != kCodeFluid) continue;
-        const float c = xc.v[m];
-        float tp, tm, ret = 0.0f;
-        uint32_t cn;
-        tp = 0.0f; tm = 0.0f;
-        cn = sw_code(w, 1); if (cn != kCodeSolid) tp = __fsub_rn(cn == kCodeAir ? 0.0f : xip.v[m], c);
-        cn = sw_code(w, 2); if (cn != kCodeSolid) tm = __fsub_rn(cn == kCodeAir ? 0.0f : xim.v[m], c);
-        ret = __fadd_rn(ret, __fadd_rn(tp, tm));
-        tp = 0.0f; tm = 0.0f;
-        cn = sw_code(w, 3); if (cn != kCodeSolid) tp = __fsub_rn(cn == kCodeAir ? 0.0f : xjp.v[m], c);
-        cn = sw_code(w, 4); if (cn != kCodeSolid) tm = __fsub_rn(cn == kCodeAir ? 0.0f : xjm.v[m], c);
-        ret = __fadd_rn(ret, __fadd_rn(tp, tm));
-        tp = 0.0f; tm = 0.0f;
-        cn = sw_code(w, 5);
-        if (cn != kCodeSolid) tp = __fsub_rn(cn == kCodeAir ? 0.0f : (m < 7 ? xc.v[m + 1] : xkp), c);
-        cn = sw_code(w, 6);
-        if (cn != kCodeSolid) tm = __fsub_rn(cn == kCodeAir ? 0.0f : (m > 0 ? xc.v[m - 1] : xkm), c);
-        ret = __fadd_rn(ret, __fadd_rn(tp, tm));
-        out[m] = ret;
+        out[m] = sw_nbsum(w, xc.v[m], xip.v[m], xim.v[m], xjp.v[m], xjm.v[m], m < 7 ? xc.v[m + 1] : xkp,
+                          m > 0 ? xc.v[m - 1] : xkm);
     }
 }
 

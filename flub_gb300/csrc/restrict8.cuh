@@ -47,23 +47,8 @@ __device__ __forceinline__ void residual_row8(const TR *__restrict__ r, const TZ
     for (int m = 0; m < 8; m++) {
         float lz = 0.0f;
         const uint32_t w = word_at(wd, m);
-        if (sw_code(w, 0) == kCodeFluid) {
-            const float c = xc[m];
-            float tp, tm;
-            uint32_t cn;
-            tp = 0.0f; tm = 0.0f;
-            cn = sw_code(w, 1); if (cn != kCodeSolid) tp = __fsub_rn(cn == kCodeAir ? 0.0f : xip[m], c);
-            cn = sw_code(w, 2); if (cn != kCodeSolid) tm = __fsub_rn(cn == kCodeAir ? 0.0f : xim[m], c);
-            lz = __fadd_rn(lz, __fadd_rn(tp, tm));
-            tp = 0.0f; tm = 0.0f;
-            cn = sw_code(w, 3); if (cn != kCodeSolid) tp = __fsub_rn(cn == kCodeAir ? 0.0f : xjp[m], c);
-            cn = sw_code(w, 4); if (cn != kCodeSolid) tm = __fsub_rn(cn == kCodeAir ? 0.0f : xjm[m], c);
-            lz = __fadd_rn(lz, __fadd_rn(tp, tm));
-            tp = 0.0f; tm = 0.0f;
-            cn = sw_code(w, 5); if (cn != kCodeSolid) tp = __fsub_rn(cn == kCodeAir ? 0.0f : (m < 7 ? xc[m + 1] : xkp), c);
-            cn = sw_code(w, 6); if (cn != kCodeSolid) tm = __fsub_rn(cn == kCodeAir ? 0.0f : (m > 0 ? xc[m - 1] : xkm), c);
-            lz = __fadd_rn(lz, __fadd_rn(tp, tm));
-        }
+        if (sw_code(w, 0) == kCodeFluid)
+            lz = sw_nbsum(w, xc[m], xip[m], xim[m], xjp[m], xjm[m], m < 7 ? xc[m + 1] : xkp, m > 0 ? xc[m - 1] : xkm);
         out[m] = __fadd_rn(rv[m], lz);
     }
 }

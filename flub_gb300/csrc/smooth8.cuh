@@ -53,6 +53,27 @@ __device__ __forceinline__ uint8_t code_at(uint2 c, int m) {
 // codes by the same function set_tags uses.
 __device__ __forceinline__ uint32_t sw_code(uint32_t w, int q) { return (w >> (2 * q)) & 3u; }
 
+// Bit q of sw_ns(w) (q = 2, 4, .., 12) is set when neighbour q / 2 is not
+// solid: with solid 0, air 1, fluid 2 that is bit q | bit q + 1 of the word.
+__device__ __forceinline__ uint32_t sw_ns(uint32_t w) { return (w | (w >> 1)) & 0x1554u; }
+
+// Neighbour sum of L x at a fluid cell from its stencil word w, in lap_at's
+// operation order: per neighbour (i+, i-, j+, j-, k+, k-) 0 when solid, else
+// (x_n - x_c) with x_n = 0 for air, summed in pairs per axis.  Bit tests on
+// the word replace the per-neighbour code compares.
+__device__ __forceinline__ float sw_nbsum(uint32_t w, float xc, float xip, float xim, float xjp, float xjm,
+                                          float xkp, float xkm) {
+    const uint32_t ns = sw_ns(w);
+    auto term = [&](int q, float xn) {
+        const float v = (w & (2u << (2 * q))) ? xn : 0.0f;
+        return (ns & (1u << (2 * q))) ? __fsub_rn(v, xc) : 0.0f;
+    };
+    float ret = 0.0f;
+    ret = __fadd_rn(ret, __fadd_rn(term(1, xip), term(2, xim)));
+    ret = __fadd_rn(ret, __fadd_rn(term(3, xjp), term(4, xjm)));
+    return __fadd_rn(ret, __fadd_rn(term(5, xkp), term(6, xkm)));
+}
+
 __device__ __forceinline__ uint32_t word_at(const uint4 &u, int m) {
     const uint32_t v = m < 2 ? u.x : (m < 4 ? u.y : (m < 6 ? u.z : u.w));
     return (m & 1) ? (v >> 16) : (v & 0xffffu);
@@ -115,20 +136,9 @@ template <bool kFromZero>
 __device__ __forceinline__ float smooth_cell(uint32_t w, float xc, float xip, float xim, float xjp, float xjm,
                                              float xkp, float xkm, float r) {
     if (sw_code(w, 0) != kCodeFluid) return 0.0f;
-    // neighbour q (1..6) sits at bits 2q, 2q + 1 with solid 0, air 1, fluid 2:
-    // bit 2q | bit 2q + 1 = "not solid" (it counts in d), bit 2q + 1 = "fluid"
-    // (its z enters; an air neighbour enters as 0)
-    const uint32_t ns = (w | (w >> 1)) & 0x1554u;
-    const int d = __popc(ns);
+    const int d = __popc(sw_ns(w));
     if (d == 0) return 0.0f;
-    auto term = [&](int q, float xn) {
-        const float v = (w & (2u << (2 * q))) ? xn : 0.0f;
-        return (ns & (1u << (2 * q))) ? __fsub_rn(v, xc) : 0.0f;
-    };
-    float ret = 0.0f;
-    ret = __fadd_rn(ret, __fadd_rn(term(1, xip), term(2, xim)));
-    ret = __fadd_rn(ret, __fadd_rn(term(3, xjp), term(4, xjm)));
-    ret = __fadd_rn(ret, __fadd_rn(term(5, xkp), term(6, xkm)));
+    const float ret = kFromZero ? 0.0f : sw_nbsum(w, xc, xip, xim, xjp, xjm, xkp, xkm);
     return kFromZero ? __fdiv_rn(r, (float)d) : __fadd_rn(xc, __fdiv_rn(__fadd_rn(r, ret), (float)d));
 }
 
