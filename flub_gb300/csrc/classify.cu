@@ -130,6 +130,113 @@ __global__ void __launch_bounds__(kRowThreads) k_classify(const float *__restric
     tag[c] = t;
 }
 
+// ---------------------------------------------------------------- four cells per thread
+//
+// k_classify for nz % 4 == 0: a thread classifies cells k = 4t .. 4t + 3 of
+// row (i, j).  Within a row only w = (k + 1/2) h changes, so the SDF terms
+// that involve only u, v and the primitive are computed once per row and
+// primitive: the same operations on the same operands as phi_prims_at,
+// sdf_atom, sdf_cube and quat_rotate_inv perform per cell, hence the same
+// bits.
+
+// Row-invariant part of sdf_cube's quat_rotate_inv(q, (p0, p1, p2)) for fixed p0, p1.
+struct CubeRow {
+    float c, w2, a01, q2p1, q2p0, cz, p0c, p1c, czw2;
+    float q[4], r[3];
+};
+
+__device__ __forceinline__ void cube_row(CubeRow &cr, float p0, float p1, const float q[4], const float r[3]) {
+    cr.c = __fsub_rn(__fmul_rn(__fmul_rn(2.0f, q[3]), q[3]), 1.0f);
+    cr.a01 = __fadd_rn(__fmul_rn(q[0], p0), __fmul_rn(q[1], p1));
+    cr.q2p1 = __fmul_rn(q[2], p1);
+    cr.q2p0 = __fmul_rn(q[2], p0);
+    cr.cz = __fsub_rn(__fmul_rn(q[0], p1), __fmul_rn(q[1], p0));
+    cr.w2 = __fmul_rn(q[3], 2.0f);
+    cr.p0c = __fmul_rn(p0, cr.c);
+    cr.p1c = __fmul_rn(p1, cr.c);
+    cr.czw2 = __fmul_rn(cr.cz, cr.w2);
+#pragma unroll
+    for (int a = 0; a < 4; a++) cr.q[a] = q[a];
+#pragma unroll
+    for (int a = 0; a < 3; a++) cr.r[a] = r[a];
+}
+
+// sdf_cube at (p0, p1, p2) from the row part.
+__device__ __forceinline__ float cube_at(const CubeRow &cr, float p2) {
+    const float d = __fmul_rn(2.0f, __fadd_rn(cr.a01, __fmul_rn(cr.q[2], p2)));
+    const float cx = __fsub_rn(__fmul_rn(cr.q[1], p2), cr.q2p1);
+    const float cy = __fsub_rn(cr.q2p0, __fmul_rn(cr.q[0], p2));
+    float p[3], m[3];
+    p[0] = __fadd_rn(__fsub_rn(cr.p0c, __fmul_rn(cx, cr.w2)), __fmul_rn(cr.q[0], d));
+    p[1] = __fadd_rn(__fsub_rn(cr.p1c, __fmul_rn(cy, cr.w2)), __fmul_rn(cr.q[1], d));
+    p[2] = __fadd_rn(__fsub_rn(__fmul_rn(p2, cr.c), cr.czw2), __fmul_rn(cr.q[2], d));
+#pragma unroll
+    for (int a = 0; a < 3; a++) m[a] = __fsub_rn(fmaxf(p[a], -p[a]), cr.r[a]);
+    const float mx = fmaxf(fmaxf(m[0], m[1]), m[2]);
+    if (mx < 0.0f) return mx;
+    return len3(fmaxf(m[0], 0.0f), fmaxf(m[1], 0.0f), fmaxf(m[2], 0.0f));
+}
+
+__global__ void __launch_bounds__(kRowThreads) k_classify4(const float4 *__restrict__ phi, int4 *__restrict__ tag,
+                                                          float4 *__restrict__ phr, int ny, int nz, float h,
+                                                          float h0, const PrimSet ps) {
+    const int t = blockIdx.x * blockDim.x + threadIdx.x, j = blockIdx.y, i = blockIdx.z;
+    const int nz4 = nz >> 2;
+    if (t >= nz4) return;
+    const int64_t c4 = ((int64_t)i * ny + j) * nz4 + t;
+    const float4 pv = __ldg(phi + c4);
+    int tt[4] = {pv.x > 0.0f ? 0 : 1, pv.y > 0.0f ? 0 : 1, pv.z > 0.0f ? 0 : 1, pv.w > 0.0f ? 0 : 1};
+    if (ps.n > 0 || phr) {
+        const float hs = __fmul_rn(0.5f, h);
+        const float u = __fadd_rn(__fmul_rn((float)i, h), hs), v = __fadd_rn(__fmul_rn((float)j, h), hs);
+        float wv[4], in[4];
+#pragma unroll
+        for (int e = 0; e < 4; e++) {
+            wv[e] = __fadd_rn(__fmul_rn((float)(4 * t + e), h), hs);
+            in[e] = 2.0f;
+        }
+        for (int o = 0; o < ps.n; o++) {
+            const flub_prim &g = ps.p[o];
+            const float p0 = __fsub_rn(u, g.x[0]), p1 = __fsub_rn(v, g.x[1]);
+            float s[4];
+            if (g.geometry == 1 || g.geometry == 3 || g.geometry == 4) {
+                CubeRow cr;
+                cube_row(cr, p0, p1, g.q, g.radius);
+#pragma unroll
+                for (int e = 0; e < 4; e++) s[e] = cube_at(cr, __fsub_rn(wv[e], g.x[2]));
+                if (g.geometry == 4) {
+                    const float sq = 0.70710678118654752f;
+                    const float zq[4] = {0.0f, 0.0f, sq, sq}, zi[4] = {0.0f, 0.0f, -sq, sq};
+                    float tq[4], q2[4];
+                    quat_mul(zq, g.q, tq);
+                    quat_mul(tq, zi, q2);
+                    cube_row(cr, p0, p1, q2, g.radius);
+#pragma unroll
+                    for (int e = 0; e < 4; e++) s[e] = fminf(s[e], cube_at(cr, __fsub_rn(wv[e], g.x[2])));
+                }
+            } else if (g.geometry == 2) {
+                const float s01 = __fadd_rn(__fmul_rn(p0, p0), __fmul_rn(p1, p1));
+#pragma unroll
+                for (int e = 0; e < 4; e++) {
+                    const float p2 = __fsub_rn(wv[e], g.x[2]);
+                    s[e] = __fsub_rn(__fsqrt_rn(__fadd_rn(s01, __fmul_rn(p2, p2))), g.radius[0]);
+                }
+            } else {
+#pragma unroll
+                for (int e = 0; e < 4; e++) s[e] = g.geometry == 5 ? 2.0f : 1.0f;
+            }
+#pragma unroll
+            for (int e = 0; e < 4; e++)
+                if (s[e] < fminf(h0, in[e])) in[e] = s[e];
+        }
+        if (phr) phr[c4] = make_float4(in[0], in[1], in[2], in[3]);
+#pragma unroll
+        for (int e = 0; e < 4; e++)
+            if (in[e] < 0.0f) tt[e] = 2;
+    }
+    tag[c4] = make_int4(tt[0], tt[1], tt[2], tt[3]);
+}
+
 static int make_primset(const flub_prim *prims, int nprims, PrimSet *ps) {
     FLUB_REQUIRE(nprims >= 0 && nprims <= FLUB_MAX_PRIMS, "nprims=%d outside [0, %d]", nprims, FLUB_MAX_PRIMS);
     FLUB_REQUIRE(nprims == 0 || prims != nullptr, "prims is NULL with nprims=%d", nprims);
@@ -185,8 +292,14 @@ int flub_classify(const float *phi, const flub_prim *prims, int nprims, int nx, 
     int st = make_primset(prims, nprims, &ps);
     if (st) return st;
     FLUB_REQUIRE(nx < 65536 && ny < 65536, "flub_classify: nx, ny must be below 65536");
-    k_classify<<<row_grid(nx, ny, nz), kRowThreads, 0, as_stream(stream)>>>(phi, tag, phi_rigid, nx, ny, nz, h, h0,
-                                                                          ps);
+    const bool v4 = nz % 4 == 0 && ((uintptr_t)phi | (uintptr_t)tag | (uintptr_t)phi_rigid) % 16 == 0;
+    if (v4)
+        k_classify4<<<row_grid(nx, ny, nz / 4), kRowThreads, 0, as_stream(stream)>>>(
+            reinterpret_cast<const float4 *>(phi), reinterpret_cast<int4 *>(tag), reinterpret_cast<float4 *>(phi_rigid),
+            ny, nz, h, h0, ps);
+    else
+        k_classify<<<row_grid(nx, ny, nz), kRowThreads, 0, as_stream(stream)>>>(phi, tag, phi_rigid, nx, ny, nz, h,
+                                                                              h0, ps);
     FLUB_CHECK_LAUNCH();
     return FLUB_OK;
 }

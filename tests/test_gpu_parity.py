@@ -64,6 +64,33 @@ def test_classify_bit_exact(scene):
     assert np.array_equal(host(phr), phr_o)
 
 
+@pytest.mark.parametrize("shape", [(20, 24, 32), (20, 24, 30)])
+def test_classify_every_primitive_kind_bit_exact(shape):
+    """Rotated boxes (geometry 1 and 3), a sphere (2), the two-box primitive
+    (4), the constant ones (5 and an unknown kind) and overlaps between them,
+    on a grid with nz % 4 == 0 (four cells per thread) and one without."""
+    def unit(q):
+        q = np.asarray(q, np.float64)
+        return tuple((q / np.linalg.norm(q)).astype(np.float32))
+    prims = scenes.make_prims([
+        dict(geometry=1, x=(0.3, 0.4, 0.5), radius=(0.12, 0.2, 0.08), q=unit((0.1, 0.3, -0.2, 0.9))),
+        dict(geometry=3, x=(0.6, 0.5, 0.4), radius=0.1, q=unit((-0.4, 0.1, 0.2, 0.8))),
+        dict(geometry=2, x=(0.45, 0.6, 0.55), radius=0.17),
+        dict(geometry=4, x=(0.7, 0.3, 0.6), radius=(0.15, 0.04, 0.06), q=unit((0.2, -0.1, 0.5, 0.7))),
+        dict(geometry=5, x=(0.1, 0.1, 0.1), radius=0.1),
+        dict(geometry=7, x=(0.9, 0.9, 0.9), radius=0.1),
+    ])
+    rng = np.random.default_rng(17)
+    phi = rng.standard_normal(shape).astype(np.float32) * 0.1
+    h, h0 = 1.0 / shape[0], 0.05
+    tag_o, phr_o = O.classify(phi, prims, h, h0)
+    assert (tag_o == 2).any() and (tag_o == 0).any() and (tag_o == 1).any()
+    phr = torch.empty(shape, dtype=torch.float32, device="cuda")
+    tag = K.classify(dev(phi), prims, h, h0, phi_rigid=phr)
+    assert np.array_equal(host(tag), tag_o)
+    assert np.array_equal(host(phr), phr_o)
+
+
 def test_classify_unfused_kernels_bit_exact(scene):
     tag_o, phr_o = O.classify(scene.phi, scene.prims, scene.h, scene.h0)
     tag = IntField(torch.empty(scene.shape, dtype=torch.int32, device="cuda"))
