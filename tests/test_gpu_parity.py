@@ -152,6 +152,27 @@ def test_subtract_gradient_bit_exact(scene):
         assert np.array_equal(host(a), o)
 
 
+@pytest.mark.parametrize("shape", [(12, 20, 28), (12, 20, 30), (9, 7, 4)])
+def test_fused_subtract_gradient_ragged_shapes_bit_exact(shape):
+    """The fused three-axis update on random tags (air, fluid and solid mixed
+    everywhere) at nz % 4 == 0 (four faces per thread) and not."""
+    rng = np.random.default_rng(31)
+    nx, ny, nz = shape
+    tag = rng.integers(0, 3, shape).astype(np.int32)
+    p = rng.standard_normal(shape).astype(np.float32)
+    vel = [rng.standard_normal(s).astype(np.float32) for s in ((nx + 1, ny, nz), (nx, ny + 1, nz), (nx, ny, nz + 1))]
+    velr = [rng.standard_normal(a.shape).astype(np.float32) for a in vel]
+    outs = [a.copy() for a in vel]
+    pg = p.copy()
+    O.scale(pg, np.float32(2.0))
+    for d, (a, ar) in enumerate(zip(outs, velr)):
+        O.subtract_gradient(a, ar, pg, tag, d + 1)
+    vd = mac(*vel)
+    K.subtract_gradient(vd, mac(*velr), dev(p), dev(tag), p_scale=2.0)
+    for a, o in zip((vd.u.f, vd.v.f, vd.w.f), outs):
+        assert np.array_equal(host(a), o)
+
+
 # ---------------------------------------------------------------- multigrid
 
 def _setup(scene):
