@@ -125,6 +125,25 @@ def test_divergence_bit_exact(scene):
     assert np.array_equal(host(fused), div_o)
 
 
+@pytest.mark.parametrize("shape", [(12, 20, 28), (12, 20, 30), (9, 7, 4)])
+def test_divergence_ragged_shapes_bit_exact(shape):
+    """Plain and fused (masked, scaled) divergence on random tags (air, fluid
+    and solid mixed everywhere) at nz % 4 == 0 (four cells per thread) and not."""
+    rng = np.random.default_rng(37)
+    nx, ny, nz = shape
+    tag = rng.integers(0, 3, shape).astype(np.int32)
+    vel = [rng.standard_normal(s).astype(np.float32) for s in ((nx + 1, ny, nz), (nx, ny + 1, nz), (nx, ny, nz + 1))]
+    velr = [rng.standard_normal(a.shape).astype(np.float32) for a in vel]
+    div_o = O.divergence(*vel, *velr, tag)
+    vd, vrd = mac(*vel), mac(*velr)
+    div = Field(torch.empty(shape, device="cuda"))
+    launch(K.divergence_tag, shape, [vd, div, vrd, IntField(dev(tag))])
+    assert np.array_equal(host(div.f), div_o)
+    O.mask_with_tag(div_o, tag)
+    O.scale(div_o, np.float32(-3.0))
+    assert np.array_equal(host(K.divergence(vd, vrd, dev(tag), scale=-3.0)), div_o)
+
+
 def test_subtract_gradient_bit_exact(scene):
     tag_o, _ = O.classify(scene.phi, scene.prims, scene.h, scene.h0)
     rng = np.random.default_rng(5)
