@@ -166,6 +166,15 @@ __global__ void k_encode_tags(const int32_t *__restrict__ tag, uint8_t *__restri
         code[c] = encode_tag(tag[c]);
 }
 
+// The same for n % 4 == 0 (aligned arrays): four tags in, four packed codes out.
+__global__ void k_encode_tags4(const int4 *__restrict__ tag, uint32_t *__restrict__ code, int64_t n4) {
+    for (int64_t q = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; q < n4; q += (int64_t)gridDim.x * blockDim.x) {
+        const int4 t = __ldg(tag + q);
+        code[q] = (uint32_t)encode_tag(t.x) | ((uint32_t)encode_tag(t.y) << 8) | ((uint32_t)encode_tag(t.z) << 16) |
+                  ((uint32_t)encode_tag(t.w) << 24);
+    }
+}
+
 // multigrid/mgpcg.py:162-174 restrict_tag on cell codes.
 __global__ void k_restrict_codes(const uint8_t *__restrict__ cf, uint8_t *__restrict__ cc, Dims C) {
     const int64_t n = C.n();
@@ -298,6 +307,27 @@ __global__ void k_init(float *__restrict__ r, const float *__restrict__ rhs, flo
 __global__ void k_mask_interior(float *__restrict__ r, const uint8_t *__restrict__ code, int64_t n) {
     for (int64_t c = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; c < n; c += (int64_t)gridDim.x * blockDim.x)
         if (code[c] != kCodeFluid) r[c] = 0.0f;
+}
+
+// The same for n % 4 == 0 (aligned arrays), four cells per step; like the
+// scalar kernel it only writes: one 16-byte zero store for four cells without
+// fluid, single zero stores in a mixed quad.
+__global__ void k_mask_interior4(float4 *__restrict__ r, const uint32_t *__restrict__ code, int64_t n4) {
+    for (int64_t q = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; q < n4; q += (int64_t)gridDim.x * blockDim.x) {
+        const uint32_t c4 = __ldg(code + q);
+        bool fl[4];
+#pragma unroll
+        for (int e = 0; e < 4; e++) fl[e] = ((c4 >> (8 * e)) & 0xffu) == kCodeFluid;
+        if (fl[0] && fl[1] && fl[2] && fl[3]) continue;  // r unchanged
+        if (!fl[0] && !fl[1] && !fl[2] && !fl[3]) {
+            r[q] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+            continue;
+        }
+        float *rr = reinterpret_cast<float *>(r + q);
+#pragma unroll
+        for (int e = 0; e < 4; e++)
+            if (!fl[e]) rr[e] = 0.0f;
+    }
 }
 
 // Plain L p (flub_mg_matvec).

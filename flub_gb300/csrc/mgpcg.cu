@@ -1238,7 +1238,12 @@ int flub_mg_destroy(flub_mg *mg) {
 int flub_mg_set_tags(flub_mg *mg, const int32_t *tag, void *stream) {
     FLUB_REQUIRE(mg && tag, "flub_mg_set_tags: NULL argument");
     cudaStream_t s = as_stream(stream);
-    k_encode_tags<<<blocks_for(mg->n, 256), 256, 0, s>>>(tag, mg->lv[0].code, mg->n);
+    if (mg->n % 4 == 0 && (uintptr_t)tag % 16 == 0)
+        k_encode_tags4<<<blocks_for(mg->n / 4, 256), 256, 0, s>>>(reinterpret_cast<const int4 *>(tag),
+                                                                  reinterpret_cast<uint32_t *>(mg->lv[0].code),
+                                                                  mg->n / 4);
+    else
+        k_encode_tags<<<blocks_for(mg->n, 256), 256, 0, s>>>(tag, mg->lv[0].code, mg->n);
     FLUB_CHECK_LAUNCH();
     for (int l = 0; l + 1 < mg->levels; l++) {
         const Level &C = mg->lv[l + 1];
@@ -1301,7 +1306,11 @@ int flub_mg_init(flub_mg *mg, const float *rhs, float k, void *stream) {
 
 int flub_mg_mask_interior(flub_mg *mg, void *stream) {
     FLUB_REQUIRE(mg, "flub_mg_mask_interior: NULL handle");
-    k_mask_interior<<<blocks_for(mg->n, 256), 256, 0, as_stream(stream)>>>(mg->lv[0].r, mg->lv[0].code, mg->n);
+    if (mg->n % 4 == 0)
+        k_mask_interior4<<<blocks_for(mg->n / 4, 256), 256, 0, as_stream(stream)>>>(
+            reinterpret_cast<float4 *>(mg->lv[0].r), reinterpret_cast<const uint32_t *>(mg->lv[0].code), mg->n / 4);
+    else
+        k_mask_interior<<<blocks_for(mg->n, 256), 256, 0, as_stream(stream)>>>(mg->lv[0].r, mg->lv[0].code, mg->n);
     FLUB_CHECK_LAUNCH();
     mg->r_masked = true;
     return FLUB_OK;
