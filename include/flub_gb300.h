@@ -331,14 +331,18 @@ int flub_mg_smooth_iteration(flub_mg *mg, int level, int phase, int *tiled, void
  * callers that cannot allocate device memory themselves -- a plugin whose host
  * application owns every device allocation and forbids cudaMalloc in its frame
  * loop, or a real-time caller that cannot pay for cudaMalloc's implicit
- * synchronisation.  Computes z = M r exactly as flub_mg_set_tags(tag) followed
- * by flub_mg_apply_preconditioner(r, z) would (same kernels, same results),
- * but keeps the level hierarchy in a 2 MiB array compiled into the library
- * (resident on every device that loads it, until the process exits) and
- * allocates nothing.  Limits: nx * ny * nz <= FLUB_NOALLOC_MAX_CELLS, plus
- * the shape rules of flub_mg_create; larger grids are rejected with
- * FLUB_ERR_INVALID_ARGUMENT.  The first call on each device looks up the
- * array's device address; make that first call before any stream capture.
+ * synchronisation.  Always runs the reference's V-cycle schedule with FP32
+ * level storage: it computes z = M r exactly as flub_mg_set_tags(tag) followed
+ * by flub_mg_apply_preconditioner(r, z) would on an FP32 handle left at the
+ * default schedule (same kernels, same results), but keeps the level
+ * hierarchy in a 2 MiB array compiled into the library (resident on every
+ * device that loads it, until the process exits) and allocates nothing.
+ * Limits: nx * ny * nz <= FLUB_NOALLOC_MAX_CELLS, plus the shape rules of
+ * flub_mg_create; larger grids are rejected with FLUB_ERR_INVALID_ARGUMENT.
+ * The first call on each device looks up the array's device address and
+ * keeps it for the life of the process; make that first call before any
+ * stream capture, and do not call this entry point again on a device after
+ * cudaDeviceReset (the kept address belongs to the context that was reset).
  * Every call shares the one array: calls that can overlap on the GPU (other
  * streams, other host threads) race and must be serialised by the caller. */
 #define FLUB_NOALLOC_MAX_CELLS 262144 /* 64^3 */

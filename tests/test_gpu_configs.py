@@ -1,0 +1,80 @@
+"""The benchmark configurations themselves, projected on the GPU with the
+reference's V-cycle schedule, against the FP64 oracle run on the same scene:
+
+* ``box64``     64^3, 4 levels (fluid box, walls Neumann);
+* ``sphere128`` 128^3, 5 levels (flow past a solid sphere; solid inflow layer
+  with u = 1 on its face, air outflow layer);
+* ``dam256``    256^3, 6 levels (dam break with a water sphere and a solid box).
+
+Plain FP32 and the mixed-precision solver (FP16 V-cycle storage, flexible
+CG), each to relative residual 1e-6 (squared-norm tolerance 1e-12):
+
+* tags bit for bit;
+* CG iterations within 1 of the oracle's (FP32), within 2 above it (mixed);
+* pressure within relative L2 1e-5 of the FP64 oracle's;
+* the post-projection max |div u| over fluid cells (example_fluid.py:146-147)
+  printed and at least 1e3 below the right-hand side's.
+"""
+import numpy as np
+import pytest
+import torch
+
+import oracle as O
+from flub_gb300 import Projection, scenes
+from flub_gb300.fields import Field, MACGrid
+
+pytestmark = pytest.mark.gpu
+
+PRESSURE_RTOL = 1e-5
+
+CONFIGS = {
+    "box64": lambda: scenes.box(64, 0),
+    "sphere128": lambda: scenes.sphere(128, 1),
+    "dam256": lambda: scenes.dam(256, 2),
+}
+
+_cache = {}
+
+
+def _reference(name):
+    """The scene and the FP64 oracle's projection of it, computed once."""
+    if name not in _cache:
+        s = CONFIGS[name]()
+        _cache[name] = (s, O.project(s, dtype=np.float64))
+    return _cache[name]
+
+
+def dev(a):
+    return torch.from_numpy(np.ascontiguousarray(a)).cuda()
+
+
+def mac(u, v, w):
+    return MACGrid(Field(dev(u), d=1), Field(dev(v), d=2), Field(dev(w), d=3))
+
+
+@pytest.mark.parametrize("precision", ["fp32", "mixed"])
+@pytest.mark.parametrize("name", sorted(CONFIGS))
+def test_config_projection_against_fp64_oracle(name, precision):
+    s, ref = _reference(name)
+    assert ref["converged"]
+    proj = Projection(s.shape, s.levels, precision=precision)
+    vel, velr = mac(s.u, s.v, s.w), mac(s.ur, s.vr, s.wr)
+    info = proj.project(vel, velr, dev(s.phi), s.prims, max_iters=200, abs_tol=0.0, rel_tol=1e-12)
+    torch.cuda.synchronize()
+    assert np.array_equal(proj.tag.f.cpu().numpy(), ref["tag"])
+    assert info["converged"] and info["status"] == 0
+    if precision == "fp32":
+        assert abs(info["iterations"] - ref["iters"]) <= 1, (info["iterations"], ref["iters"])
+    else:
+        assert ref["iters"] - 1 <= info["iterations"] <= ref["iters"] + 2, (info["iterations"], ref["iters"])
+    p = proj.p.f.cpu().numpy().astype(np.float64)
+    err = np.linalg.norm(p - ref["p"]) / np.linalg.norm(ref["p"])
+    assert err <= PRESSURE_RTOL, err
+    before = float(np.abs(ref["div"][ref["tag"] == 1]).max()) * s.h
+    after = proj.max_abs_div(vel, velr)
+    print(f"\n{name} {precision}: {info['iterations']} iterations (FP64 oracle {ref['iters']}), pressure rel. L2 "
+          f"vs FP64 {err:.2e}, max|div u| {before:.3e} -> {after:.3e}")
+    assert after <= 1e-3 * before
+    for k, a in zip("uvw", (vel.u.f, vel.v.f, vel.w.f)):
+        o = ref[k]
+        assert np.linalg.norm(a.cpu().numpy() - o) <= PRESSURE_RTOL * np.linalg.norm(o), k

@@ -496,7 +496,7 @@ def test_mixed_precision_solve(name):
     ref64 = O.pcg(r0, O.tag_levels(tag_o, scene.levels), max_iters=200, abs_tol=0.0, rel_tol=1e-12,
                   dtype=np.float64)
     err = np.linalg.norm(x - ref64["x"]) / np.linalg.norm(ref64["x"])
-    assert err <= 1e-4, err
+    assert err <= PRESSURE_RTOL, err
 
 
 def test_mixed_precision_vcycle_close_to_fp32():

@@ -36,7 +36,7 @@ def _rank_main(rank, world, port, out):
 def test_two_replicas_time_and_seeds():
     world = 2
     port = _free_port()
-    with mp.Manager() as m:
+    with mp.get_context("spawn").Manager() as m:
         out = m.dict()
         mp.start_processes(_rank_main, args=(world, port, out), nprocs=world, start_method="spawn", join=True)
         res = dict(out)

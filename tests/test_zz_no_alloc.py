@@ -58,6 +58,25 @@ def test_noalloc_vcycle_matches_regular_path_twice():
         assert torch.isfinite(z_free).all()
 
 
+@pytest.mark.parametrize("no_cluster", ["0", "1"])
+def test_noalloc_vcycle_non_cubic_ragged_grid(no_cluster, monkeypatch):
+    """A non-cubic grid whose coarse level has nz % 8 != 0 (the scalar sweep and
+    restriction kernels), with the thread-block-cluster coarse levels and
+    without them (FLUB_NO_CLUSTER=1: global sweeps and the one-block tail)."""
+    monkeypatch.setenv("FLUB_NO_CLUSTER", no_cluster)
+    shape = (16, 32, 24)
+    rng = np.random.default_rng(43)
+    phi = (rng.uniform(-1, 1, shape) + 0.4).astype(np.float32)
+    tag = O.tag_dirichlet(phi)
+    tag[rng.random(shape) < 0.05] = 2
+    r = np.where(tag == 1, rng.standard_normal(shape), 0).astype(np.float32)
+    tag_d, r_d = torch.from_numpy(tag).cuda(), torch.from_numpy(r).cuda()
+    for _ in range(2):
+        z_free = _noalloc(tag_d, r_d, 2)
+        assert torch.equal(z_free, _regular(tag_d, r_d, 2))
+        assert np.array_equal(z_free.cpu().numpy(), O.vcycle(r, O.tag_levels(tag, 2), np.float32))
+
+
 def test_noalloc_vcycle_rejects_grids_over_the_limit():
     lib = _lib.load()
     shape = (128, 64, 64)  # 524288 cells > 64^3
