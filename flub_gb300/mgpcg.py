@@ -248,12 +248,13 @@ class MGPCG:
         _lib.check(self._lib.flub_mg_smooth(self._h, int(level), int(phase), _stream()), "flub_mg_smooth")
 
     def smooth_iteration(self, level=0, phase=0):
-        """One red-black iteration on a level (the TMA-tiled kernel where the
-        level has tiles); returns True when the tiled kernel ran."""
+        """One red-black iteration on a level; returns which kernel ran: 0 the
+        natural-order row kernel (two half-sweeps), 1 the TMA-tiled kernel (one
+        launch), 2 the colour-split row kernel of level 0 (two half-sweeps)."""
         t = ctypes.c_int(0)
         _lib.check(self._lib.flub_mg_smooth_iteration(self._h, int(level), int(phase), ctypes.byref(t), _stream()),
                    "flub_mg_smooth_iteration")
-        return bool(t.value)
+        return int(t.value)
 
     def get_x(self, out, scale=1.0):
         """x * scale into out (water_3d.py:67-68)."""

@@ -11,7 +11,8 @@ CG), each to relative residual 1e-6 (squared-norm tolerance 1e-12):
 
 * tags bit for bit;
 * CG iterations within 1 of the oracle's (FP32), within 2 above it (mixed);
-* pressure within relative L2 1e-5 of the FP64 oracle's;
+* pressure within relative L2 1e-5 of the FP64 oracle's, velocities within
+  5e-5 (the FP32 floor of a differenced pressure, see VELOCITY_RTOL);
 * the post-projection max |div u| over fluid cells (example_fluid.py:146-147)
   printed and at least 1e3 below the right-hand side's.
 """
@@ -26,6 +27,11 @@ from flub_gb300.fields import Field, MACGrid
 pytestmark = pytest.mark.gpu
 
 PRESSURE_RTOL = 1e-5
+# The velocity update differences neighbouring pressures (p_hi - p_lo) of
+# values far larger than their difference, so an FP32 pressure carries more
+# relative error into the velocities than it has itself: the oracle's own
+# FP32 projection of dam256 is 1.1e-5 from its FP64 one in w.
+VELOCITY_RTOL = 5e-5
 
 CONFIGS = {
     "box64": lambda: scenes.box(64, 0),
@@ -77,4 +83,4 @@ def test_config_projection_against_fp64_oracle(name, precision):
     assert after <= 1e-3 * before
     for k, a in zip("uvw", (vel.u.f, vel.v.f, vel.w.f)):
         o = ref[k]
-        assert np.linalg.norm(a.cpu().numpy() - o) <= PRESSURE_RTOL * np.linalg.norm(o), k
+        assert np.linalg.norm(a.cpu().numpy() - o) <= VELOCITY_RTOL * np.linalg.norm(o), k
