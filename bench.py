@@ -479,7 +479,8 @@ def run_ours(args):
     peak, peak_kind = load_peaks()
     reps = 24
     plain_mg = variants["plain"].mg
-    tiled = plain_mg.smooth_iteration(0, 0)
+    smoother = plain_mg.smooth_iteration(0, 0)  # 0 natural-order rows, 1 TMA tiles, 2 colour-split rows
+    tiled = smoother == 1
     plain_mg.smooth_iteration(0, 0)
     torch.cuda.synchronize()
     k0, k1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
@@ -506,9 +507,14 @@ def run_ours(args):
         groups = fluid.view(nx_, ny_, nz_ // 8, 8).any(dim=-1)
         n_units = int(groups.sum().item())
         alg_bytes = SMOOTH_HALF_SWEEP_BYTES_PER_CELL * 8 * n_units + 4.0 * n_units
-        kname = "k_smooth8<false,false> (level-0 red-black half-sweep over the active list)"
+        if smoother == 2:
+            kname = ("k_smooth_split<kInPlace> (level-0 red-black half-sweep on colour-split storage, "
+                     "over the active list)")
+            traffic = load_traffic("k_smooth_split")
+        else:
+            kname = "k_smooth8<false,false> (level-0 red-black half-sweep over the active list)"
+            traffic = load_traffic("k_smooth8")
         unit_frac = n_units / groups.numel()
-        traffic = load_traffic("k_smooth8")
     achieved = alg_bytes / (launch_ms * 1e-3) / 1e9
     roofline = {"bound": "hbm", "kernel": kname,
                 "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,

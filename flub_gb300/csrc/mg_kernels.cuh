@@ -28,6 +28,7 @@ struct MgState {
     int skip_r;    // r is 0 off the fluid (masked), so r.r may skip groups without fluid
     float zscale;  // mixed precision: z = zscale * (V-cycle output); the FP16 residual copy is r / zscale
     float pad_;
+    unsigned int bar_count, bar_gen;  // grid barrier of the persistent V-cycle kernels (persist.cuh)
 };
 
 // Power of two near 1 / RMS of a vector with squared norm rtr over n entries:

@@ -16,14 +16,17 @@
 #include <cstdlib>
 #include <cstring>
 #include <mutex>
+#include <type_traits>
 #include <vector>
 
 #include "mg_kernels.cuh"
 #include "cg8.cuh"
 #include "cluster.cuh"
 #include "mixed.cuh"
+#include "persist.cuh"
 #include "restrict8.cuh"
 #include "smooth8.cuh"
+#include "smooth_split.cuh"
 #include "smooth_tile.cuh"
 #include "tail.cuh"
 
@@ -51,6 +54,13 @@ struct Level {
     int *act, *act_n;
     // stencil words (smooth8.cuh), same condition
     uint16_t *sw;
+    // level 0 with nz % 8 == 0: the colour-split buffers of smooth_split.cuh --
+    // stencil words, the residual (FP32 rs, or FP16 rsh in mixed precision) and
+    // the post-smoothing correction zs; z2 / z2h hold the pre-smoothing
+    // correction split the same way
+    uint16_t *sws;
+    float *rs, *zs;
+    __half *rsh;
     // TMA-tiled smoothing (smooth_tile.cuh) on FP32 levels whose extents are
     // multiples of the tile: a third correction buffer for the ping-pong of
     // the out-of-place iterations, the tile flags, and the list of tiles that
@@ -91,10 +101,12 @@ struct flub_mg {
     bool host_loop;
     bool skip_ok;   // internal z buffers keep z = 0 off the fluid (see k_smooth8)
     bool tile_ok;   // the TMA-tiled smoother runs where a level has tiles (FLUB_TILE=1)
+    bool split_ok;  // level 0 smooths on colour-split storage (smooth_split.cuh); FLUB_NO_SPLIT=1 turns it off
     bool iter_toggle[flub::kMaxLevels];  // flub_mg_smooth_iteration: direction of the next tiled call
     bool r_masked;  // r is 0 off the fluid (mask_interior since the last init)
     int tail_start;  // first level run by the one-block tail kernel (== levels: none)
     size_t tail_smem;
+    int persist_blocks;  // blocks of the persistent V-cycle legs (persist.cuh); 0: launch per pass
     int cl_start;    // first level run by the cluster kernel (== levels: none)
     int cl_size;     // blocks per cluster
     size_t cl_smem;
@@ -153,10 +165,21 @@ static size_t carve(flub_mg *mg, char *base) {
         }
         L.act = L.act_n = nullptr;
         L.sw = nullptr;
+        L.sws = nullptr;
+        L.rs = L.zs = nullptr;
+        L.rsh = nullptr;
         if (L.D.nz % 8 == 0) {
             L.act = (int *)take(sizeof(int) * (size_t)(nl >> 3));
             L.act_n = (int *)take(sizeof(int));
             L.sw = (uint16_t *)take(sizeof(uint16_t) * (size_t)nl);
+            if (l == 0 && mg->split_ok) {
+                L.sws = (uint16_t *)take(sizeof(uint16_t) * (size_t)nl);
+                L.zs = (float *)take(sizeof(float) * nl);
+                if (mg->precision == FLUB_PRECISION_MIXED)
+                    L.rsh = (__half *)take(sizeof(__half) * nl);
+                else
+                    L.rs = (float *)take(sizeof(float) * nl);
+            }
         }
         L.z3 = nullptr;
         L.tflags = nullptr;
@@ -361,6 +384,93 @@ static int choose_cluster(flub_mg *mg) {
     return FLUB_OK;
 }
 
+// The persistent cooperative V-cycle legs (persist.cuh), opt-in with
+// FLUB_PERSIST=1 when the device can run them: one block count for all four
+// kernels (the smallest co-resident count times the SMs).  Measured on the
+// 256^3 dam break they are slower than one launch per pass (V(2,2) solve 2.93
+// against 2.77 ms, the reference schedule 28.9 against 25.4 ms): a grid-wide
+// barrier across both dies costs more than the kernel boundary it replaces.
+static int choose_persist(flub_mg *mg) {
+    mg->persist_blocks = 0;
+    const char *on = getenv("FLUB_PERSIST");
+    if (!(on && on[0] == '1')) return FLUB_OK;
+    int dev = 0, coop = 0, nsm = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess || cudaDeviceGetAttribute(&coop, cudaDevAttrCooperativeLaunch, dev) != cudaSuccess ||
+        cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess || !coop) {
+        cudaGetLastError();
+        return FLUB_OK;
+    }
+    int occ = 1 << 30;
+    const void *kerns[4] = {(const void *)k_vcycle_down<float>, (const void *)k_vcycle_up<float>,
+                            (const void *)k_vcycle_down<__half>, (const void *)k_vcycle_up<__half>};
+    for (const void *k : kerns) {
+        int b = 0;
+        if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, k, kPersistThreads, 0) != cudaSuccess) {
+            cudaGetLastError();
+            return FLUB_OK;
+        }
+        occ = b < occ ? b : occ;
+    }
+    if (occ < 1) return FLUB_OK;
+    mg->persist_blocks = occ * nsm;
+    return FLUB_OK;
+}
+
+// Levels 1 .. lg-1 go to the persistent legs when every one of them walks an
+// active list with stencil words (nz % 8 == 0), the internal z buffers keep
+// z = 0 off the fluid, and no tiled smoothing is asked for there.
+static bool use_persist(const flub_mg *mg, int lg) {
+    if (mg->persist_blocks <= 0 || !mg->skip_ok || lg < 2) return false;
+    for (int l = 1; l < lg; l++) {
+        const Level &L = mg->lv[l];
+        if (L.D.nz % 8 != 0 || !L.act || !L.sw) return false;
+        if (mg->tile_ok && L.n_tiles > 0) return false;
+    }
+    return true;
+}
+
+template <typename T>
+static int launch_leg(flub_mg *mg, const LaunchCtx &c, bool down, int l0, int l1) {
+    constexpr bool half = std::is_same<T, __half>::value;
+    LegParams P = {};
+    P.l0 = l0;
+    P.l1 = l1;
+    P.st = mg->st;
+    P.rscale = (half ? 0.125f : 1.0f) * mg->sched_rscale;
+    P.zc_scale = half ? 8.0f : 1.0f;
+    for (int l = l0; l <= l1; l++) {
+        const Level &L = mg->lv[l];
+        LegLevel &Q = P.lv[l];
+        Q.D = L.D;
+        Q.code = L.code;
+        Q.sw = L.sw;
+        Q.act = L.act;
+        Q.act_n = L.act_n;
+        Q.iters = level_iters(mg, l);
+        Q.r = half ? (void *)L.rh : (void *)L.r;
+        Q.z = half ? (void *)L.zh : (void *)L.z;
+        Q.z2 = half ? (void *)L.z2h : (void *)L.z2;
+    }
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = dim3((unsigned)mg->persist_blocks);
+    cfg.blockDim = dim3(kPersistThreads);
+    cfg.stream = c.s;
+    cudaLaunchAttribute attr[1];
+    attr[0].id = cudaLaunchAttributeCooperative;
+    attr[0].val.cooperative = 1;
+    cfg.attrs = attr;
+    cfg.numAttrs = 1;
+    const cudaError_t e = down ? cudaLaunchKernelEx(&cfg, k_vcycle_down<T>, (const LegParams)P, c.kc)
+                               : cudaLaunchKernelEx(&cfg, k_vcycle_up<T>, (const LegParams)P, c.kc);
+    if (e != cudaSuccess) {
+        set_last_error("persistent V-cycle launch: %s", cudaGetErrorString(e));
+        cudaGetLastError();
+        return FLUB_ERR_CUDA;
+    }
+    count_launches(1);
+    return FLUB_OK;
+}
+
 static int validate_shape(int nx, int ny, int nz, int levels, int precision) {
     FLUB_REQUIRE(nx > 0 && ny > 0 && nz > 0, "MGPCG shape (%d, %d, %d) must be positive", nx, ny, nz);
     FLUB_REQUIRE(levels >= 1 && levels <= kMaxLevels, "n_mg_levels=%d outside [1, %d]", levels, kMaxLevels);
@@ -454,6 +564,54 @@ static int sweep(const LaunchCtx &c, const Level &L, int phase, int mode, int sk
                       c.kc);
 }
 
+
+// One level-0 half-sweep on colour-split storage (smooth_split.cuh).
+template <int kMode, typename TRN, typename TR, typename TZI, typename TZ, typename TC>
+static int split_sweep(const LaunchCtx &c, const Level &L, int phase, const TRN *rn, TR *rs, const TZI *zin, TZ *z,
+                       const TC *zc, float zc_scale, float *zn) {
+    SplitArgs A = {};
+    A.D = L.D;
+    A.act = L.act;
+    A.act_n = L.act_n;
+    A.sws = L.sws;
+    A.rn = rn;
+    A.rs = rs;
+    A.zin = zin;
+    A.z = z;
+    A.zc = zc;
+    A.zc_scale = zc_scale;
+    A.zn = zn;
+    // one lane per active group, grid-stride with one resident wave of blocks
+    static int resident = 0;
+    if (resident <= 0) {
+        int b = 0;
+        if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, k_smooth_split<kMode, TRN, TR, TZI, TZ, TC>, 256, 0) !=
+                cudaSuccess || b < 1) {
+            cudaGetLastError();
+            b = 4;
+        }
+        resident = b;
+    }
+    const dim3 grd(blocks_for(L.D.n() >> 3, 256, (int64_t)kNumSMs * resident));
+    return launch_pdl(k_smooth_split<kMode, TRN, TR, TZI, TZ, TC>, grd, dim3(256), 0, c.s, (const SplitArgs)A, phase,
+                      c.kc);
+}
+
+// Colour-split level-0 smoothing unless FLUB_NO_SPLIT=1 (read when a handle is
+// created or sized).
+static bool split_requested() {
+    const char *e = getenv("FLUB_NO_SPLIT");
+    return !(e && e[0] == '1');
+}
+
+// Level 0 of the V-cycle on colour-split storage: the handle has the split
+// buffers, level 0 hands on to a coarser level (lg >= 1), the sweeps may skip
+// fluid-free groups, no tiled smoothing is asked for there, and the output z
+// is not the input r.
+static bool use_split(const flub_mg *mg, int lg, int sk, const void *r0, const void *z0) {
+    const Level &L = mg->lv[0];
+    return mg->split_ok && L.sws && lg >= 1 && sk == 1 && !(mg->tile_ok && L.n_tiles > 0) && r0 != z0;
+}
 
 // ---------------------------------------------------------------- tiled smoothing (smooth_tile.cuh)
 
@@ -572,9 +730,35 @@ static int enqueue_vcycle(flub_mg *mg, const LaunchCtx &c, const float *r0, floa
     // smoothing ends in ZF(l), the caller's z0 at level 0
     auto TILED_PRE = [&](int l) { return mg->tile_ok && mg->lv[l].n_tiles > 0 && sk == 1; };
     auto TILED_POST = [&](int l) { return mg->tile_ok && mg->lv[l].n_tiles > 0 && SK(l) == 1; };
-    for (int l = 0; l < lg; l++) {
+    // levels 1 .. lg-1 in the persistent cooperative kernels, or one launch per pass
+    const bool pers = use_persist(mg, lg);
+    // level 0 on colour-split storage (smooth_split.cuh)
+    const bool split0 = use_split(mg, lg, sk, r0, z0);
+    for (int l = 0; l < (pers ? 1 : lg); l++) {
         const Level &L = mg->lv[l];
         const int iters = level_iters(mg, l);
+        if (l == 0 && split0) {
+            float *z2 = ZP(0);
+            for (int it = 0; it < iters; it++) {
+                if (it == 0) {
+                    FLUB_TRY((split_sweep<kFirst, float, float, float, float, float>(c, L, 0, r0, L.rs, nullptr, z2,
+                                                                                   nullptr, 1.0f, nullptr)));
+                    FLUB_TRY((split_sweep<kOwnZero, float, float, float, float, float>(
+                        c, L, 1, nullptr, L.rs, nullptr, z2, nullptr, 1.0f, nullptr)));
+                } else {
+                    FLUB_TRY((split_sweep<kInPlace, float, float, float, float, float>(
+                        c, L, 0, nullptr, L.rs, nullptr, z2, nullptr, 1.0f, nullptr)));
+                    FLUB_TRY((split_sweep<kInPlace, float, float, float, float, float>(
+                        c, L, 1, nullptr, L.rs, nullptr, z2, nullptr, 1.0f, nullptr)));
+                }
+            }
+            const Level &C = mg->lv[1];
+            FLUB_TRY(launch_pdl(k_restrict8_split<float, float, float>, dim3(blocks_for(C.D.n(), 256, kNumSMs * 4)),
+                                dim3(256), 0, c.s, r0, (const float *)z2, (const uint8_t *)L.code,
+                                (const uint16_t *)L.sw, C.r, (const uint8_t *)C.code, C.D, mg->sched_rscale,
+                                (const int *)C.act, (const int *)C.act_n, c.kc));
+            continue;
+        }
         if (TILED_PRE(l)) {
             FLUB_TRY(tile_side(mg, c, l, false, iters, R(l), nullptr, ZP(l), nullptr));
         } else {
@@ -594,6 +778,7 @@ static int enqueue_vcycle(flub_mg *mg, const LaunchCtx &c, const float *r0, floa
             FLUB_TRY(launch_pdl(k_restrict, dim3(blocks_for(C.D.n(), 256, 1 << 20)), dim3(256), 0, c.s, R(l), ZP(l),
                                 L.code, C.r, C.code, C.D, mg->sched_rscale, c.kc));
     }
+    if (pers) FLUB_TRY(launch_leg<float>(mg, c, true, 1, lg));
     if (use_cl) {
         ClusterParams P = {};
         cluster_layout(mg, lt, mg->cl_size, &P);
@@ -627,9 +812,30 @@ static int enqueue_vcycle(flub_mg *mg, const LaunchCtx &c, const float *r0, floa
             FLUB_TRY(sweep(c, L, 0, kSweepInPlace, SK(b), R(b), ZF(b), ZF(b), nullptr));
         }
     }
-    for (int l = lg - 1; l >= 0; l--) {
+    if (pers) FLUB_TRY(launch_leg<float>(mg, c, false, 1, lg));
+    for (int l = pers ? 0 : lg - 1; l >= 0; l--) {
         const Level &L = mg->lv[l];
         const int iters = level_iters(mg, l);
+        if (l == 0 && split0) {
+            // the last half-sweep writes the groups with fluid of the natural z0;
+            // a caller's z0 gets 0 everywhere else first
+            if (!z0_clean) FLUB_CHECK_CUDA(cudaMemsetAsync(z0, 0, sizeof(float) * (size_t)mg->n, c.s));
+            for (int it = 0; it < iters; it++) {
+                if (it == 0)
+                    FLUB_TRY((split_sweep<kProlong, float, float, float, float, float>(
+                        c, L, 1, nullptr, L.rs, ZP(0), L.zs, mg->lv[1].z, 1.0f, nullptr)));
+                else
+                    FLUB_TRY((split_sweep<kInPlace, float, float, float, float, float>(
+                        c, L, 1, nullptr, L.rs, nullptr, L.zs, nullptr, 1.0f, nullptr)));
+                if (it + 1 == iters)
+                    FLUB_TRY((split_sweep<kLast, float, float, float, float, float>(c, L, 0, nullptr, L.rs, nullptr,
+                                                                                  L.zs, nullptr, 1.0f, z0)));
+                else
+                    FLUB_TRY((split_sweep<kInPlace, float, float, float, float, float>(
+                        c, L, 0, nullptr, L.rs, nullptr, L.zs, nullptr, 1.0f, nullptr)));
+            }
+            continue;
+        }
         if (TILED_POST(l)) {
             FLUB_TRY(tile_side(mg, c, l, true, iters, R(l), ZP(l), ZF(l), mg->lv[l + 1].z));
             continue;
@@ -684,9 +890,33 @@ static int enqueue_vcycle_mixed(flub_mg *mg, const LaunchCtx &c, float *z0, bool
     const int sk = mg->skip_ok ? 1 : 0;
     const int sk0 = z0_clean ? sk : 0;
     const int lg = lt < Lm - 1 ? lt : Lm - 1;
-    for (int l = 0; l < lg; l++) {
+    const bool pers = use_persist(mg, lg);
+    const bool split0 = use_split(mg, lg, sk0, mg->lv[0].rh, z0);
+    for (int l = 0; l < (pers ? 1 : lg); l++) {
         const Level &L = mg->lv[l];
         const int iters = level_iters(mg, l);
+        if (l == 0 && split0) {
+            using H = __half;
+            for (int it = 0; it < iters; it++) {
+                if (it == 0) {
+                    FLUB_TRY((split_sweep<kFirst, H, H, H, H, H>(c, L, 0, (const H *)L.rh, L.rsh, nullptr, L.z2h,
+                                                                 nullptr, 1.0f, nullptr)));
+                    FLUB_TRY((split_sweep<kOwnZero, H, H, H, H, H>(c, L, 1, nullptr, L.rsh, nullptr, L.z2h, nullptr,
+                                                                   1.0f, nullptr)));
+                } else {
+                    FLUB_TRY((split_sweep<kInPlace, H, H, H, H, H>(c, L, 0, nullptr, L.rsh, nullptr, L.z2h, nullptr,
+                                                                   1.0f, nullptr)));
+                    FLUB_TRY((split_sweep<kInPlace, H, H, H, H, H>(c, L, 1, nullptr, L.rsh, nullptr, L.z2h, nullptr,
+                                                                   1.0f, nullptr)));
+                }
+            }
+            const Level &C = mg->lv[1];
+            FLUB_TRY(launch_pdl(k_restrict8_split<H, H, H>, dim3(blocks_for(C.D.n(), 256, kNumSMs * 4)), dim3(256),
+                                0, c.s, (const H *)L.rh, (const H *)L.z2h, (const uint8_t *)L.code,
+                                (const uint16_t *)L.sw, C.rh, (const uint8_t *)C.code, C.D,
+                                0.125f * mg->sched_rscale, (const int *)C.act, (const int *)C.act_n, c.kc));
+            continue;
+        }
         for (int it = 0; it < iters; it++) {
             FLUB_TRY(sweep8<__half, __half, __half, __half>(c, L, 0, it == 0 ? kSweepFromZero : kSweepInPlace, sk,
                                                             L.rh, L.z2h, L.z2h, nullptr, 1.0f));
@@ -699,6 +929,7 @@ static int enqueue_vcycle_mixed(flub_mg *mg, const LaunchCtx &c, float *z0, bool
                             (const uint16_t *)L.sw, C.rh, (const uint8_t *)C.code, C.D, 0.125f * mg->sched_rscale, (const int *)C.act,
                             (const int *)C.act_n, c.kc));
     }
+    if (pers) FLUB_TRY(launch_leg<__half>(mg, c, true, 1, lg));
     if (lt < Lm) {
         if (lt == 0)
             FLUB_TRY(launch_coarse(mg, c, 0, nullptr, z0, mg->lv[0].rh, nullptr));
@@ -722,10 +953,30 @@ static int enqueue_vcycle_mixed(flub_mg *mg, const LaunchCtx &c, float *z0, bool
             }
         }
     }
-    for (int l = lg - 1; l >= 0; l--) {
+    if (pers) FLUB_TRY(launch_leg<__half>(mg, c, false, 1, lg));
+    for (int l = pers ? 0 : lg - 1; l >= 0; l--) {
         const Level &L = mg->lv[l];
         const __half *zc = mg->lv[l + 1].zh;
         const int iters = level_iters(mg, l);
+        if (l == 0 && split0) {
+            using H = __half;
+            if (!z0_clean) FLUB_CHECK_CUDA(cudaMemsetAsync(z0, 0, sizeof(float) * (size_t)mg->n, c.s));
+            for (int it = 0; it < iters; it++) {
+                if (it == 0)
+                    FLUB_TRY((split_sweep<kProlong, H, H, H, float, H>(c, L, 1, nullptr, L.rsh, L.z2h, L.zs, zc, 8.0f,
+                                                                       nullptr)));
+                else
+                    FLUB_TRY((split_sweep<kInPlace, H, H, float, float, float>(c, L, 1, nullptr, L.rsh, nullptr,
+                                                                               L.zs, nullptr, 1.0f, nullptr)));
+                if (it + 1 == iters)
+                    FLUB_TRY((split_sweep<kLast, H, H, float, float, float>(c, L, 0, nullptr, L.rsh, nullptr, L.zs,
+                                                                            nullptr, 1.0f, z0)));
+                else
+                    FLUB_TRY((split_sweep<kInPlace, H, H, float, float, float>(c, L, 0, nullptr, L.rsh, nullptr,
+                                                                               L.zs, nullptr, 1.0f, nullptr)));
+            }
+            continue;
+        }
         for (int it = 0; it < iters; it++) {
             if (l == 0) {
                 if (it == 0)
@@ -993,6 +1244,29 @@ __global__ void __launch_bounds__(256) k_stencil_words(const uint8_t *__restrict
 
 // ---------------------------------------------------------------- warm-start support (no reference counterpart)
 
+// Stencil words in the colour-split order of smooth_split.cuh: natural cell
+// (i, j, k) -> element k >> 1 of row (i, j) in half (i + j + k) & 1.  One
+// thread per natural 8-cell group.
+__global__ void __launch_bounds__(256) k_split_words(const uint16_t *__restrict__ sw, uint16_t *__restrict__ sws,
+                                                     Dims D) {
+    const int ng = (int)(D.n() >> 3), hz = D.nz >> 1, hn = (int)(D.n() >> 1);
+    for (int g = blockIdx.x * blockDim.x + threadIdx.x; g < ng; g += gridDim.x * blockDim.x) {
+        int i, j, kg;
+        group_ijk(g, D, i, j, kg);
+        const uint4 u = __ldg(reinterpret_cast<const uint4 *>(sw + ((size_t)g << 3)));
+        const int h = (i * D.ny + j) * hz + 4 * kg, p = (i + j) & 1;
+        uint32_t e[4], o[4];
+#pragma unroll
+        for (int m = 0; m < 8; m++) {
+            const uint32_t w = word_at(u, m);
+            if (((p + m) & 1) == 0) e[m >> 1] = w;
+            else o[m >> 1] = w;
+        }
+        *reinterpret_cast<uint2 *>(sws + h) = make_uint2(e[0] | (e[1] << 16), e[2] | (e[3] << 16));
+        *reinterpret_cast<uint2 *>(sws + hn + h) = make_uint2(o[0] | (o[1] << 16), o[2] | (o[3] << 16));
+    }
+}
+
 __global__ void k_set_x0_scale(MgState *st, double v) { st->x0_scale = v; }
 
 // gamma = (d . b) / (d . L d) over fluid cells: the multiple of d closest to
@@ -1150,6 +1424,7 @@ size_t flub_mg_workspace_bytes(int nx, int ny, int nz, int levels, int precision
     tmp.nx = nx; tmp.ny = ny; tmp.nz = nz; tmp.levels = levels; tmp.precision = precision;
     tmp.n = (int64_t)nx * ny * nz;
     tmp.tile_ok = tile_requested();
+    tmp.split_ok = split_requested();
     return carve(&tmp, nullptr);
 }
 
@@ -1163,7 +1438,8 @@ int flub_mg_create(int nx, int ny, int nz, int levels, int precision, void *work
     reference_schedule(mg);
     mg->nx = nx; mg->ny = ny; mg->nz = nz; mg->levels = levels; mg->precision = precision;
     mg->n = (int64_t)nx * ny * nz;
-    mg->tile_ok = tile_requested();  // decides the tile buffers carved below
+    mg->tile_ok = tile_requested();    // decides the tile buffers carved below
+    mg->split_ok = split_requested();  // and the colour-split ones
     const size_t need = carve(mg, nullptr);
     if (workspace) {
         if (workspace_bytes < need || ((uintptr_t)workspace & 255)) {
@@ -1198,6 +1474,7 @@ int flub_mg_create(int nx, int ny, int nz, int levels, int precision, void *work
     mg->skip_ok = true;  // the workspace is zeroed below and set_tags re-zeroes the z buffers
     choose_tail(mg);
     choose_cluster(mg);
+    choose_persist(mg);
     if (precision == FLUB_PRECISION_MIXED) {
         // the FP16 sweeps work on rows of 8 cells: every level left to the global
         // kernels needs nz % 8 == 0
@@ -1256,6 +1533,11 @@ int flub_mg_set_tags(flub_mg *mg, const int32_t *tag, void *stream) {
         if (L.sw) {
             k_stencil_words<<<blocks_for(L.D.n() >> 3, 256), 256, 0, s>>>(L.code, L.sw, L.D);
             FLUB_CHECK_LAUNCH();
+        }
+        if (L.sws) {
+            k_split_words<<<blocks_for(L.D.n() >> 3, 256), 256, 0, s>>>(L.sw, L.sws, L.D);
+            FLUB_CHECK_LAUNCH();
+            FLUB_CHECK_CUDA(cudaMemsetAsync(L.zs, 0, sizeof(float) * (size_t)L.D.n(), s));
         }
         if (!L.act) continue;
         const int ng = (int)(L.D.n() >> 3);
@@ -1512,6 +1794,20 @@ int flub_mg_smooth_iteration(flub_mg *mg, int level, int phase, int *tiled, void
     const Level &L = mg->lv[level];
     const bool t = mg->tile_ok && L.n_tiles > 0 && mg->skip_ok;
     if (tiled) *tiled = t ? 1 : 0;
+    if (!t && level == 0 && L.sws && mg->skip_ok) {
+        // the colour-split kernels the V-cycle runs at level 0, in place on the
+        // post-smoothing buffer with the split residual of the last V-cycle
+        if (tiled) *tiled = 2;
+        for (int ph : {phase, 1 - phase}) {
+            if (mg->precision == FLUB_PRECISION_MIXED)
+                FLUB_TRY((split_sweep<kInPlace, __half, __half, float, float, float>(
+                    c, L, ph, nullptr, L.rsh, nullptr, L.zs, nullptr, 1.0f, nullptr)));
+            else
+                FLUB_TRY((split_sweep<kInPlace, float, float, float, float, float>(c, L, ph, nullptr, L.rs, nullptr,
+                                                                                  L.zs, nullptr, 1.0f, nullptr)));
+        }
+        return FLUB_OK;
+    }
     if (t) {
         // z -> z3 and z3 -> z on alternate calls (both keep 0 off the fluid);
         // the handle's pointers stay as the captured solve graphs know them

@@ -12,9 +12,34 @@
 
 namespace flub {
 
+// Natural-order row (ii, jj), cells 8 kg .. 8 kg + 7, of a colour-split
+// level-0 vector (smooth_split.cuh): element m >> 1 of the half of parity
+// (ii + jj + m) & 1.
+template <typename TZ>
+__device__ __forceinline__ void ld_row8_split(const TZ *__restrict__ z, const Dims D, int ii, int jj, int kg,
+                                              float o[8]) {
+    const int hz = D.nz >> 1, hn = (int)(D.n() >> 1);
+    const int h = (ii * D.ny + jj) * hz + 4 * kg;
+    const int p = (ii + jj) & 1;
+    float e[4], od[4];
+    St<TZ>::ld4_ro(z + h, e);
+    St<TZ>::ld4_ro(z + hn + h, od);
+#pragma unroll
+    for (int m = 0; m < 8; m++) o[m] = ((p + m) & 1) ? od[m >> 1] : e[m >> 1];
+}
+
+// Natural cell (ii, jj, k) of a colour-split level-0 vector.
+template <typename TZ>
+__device__ __forceinline__ float ld_cell_split(const TZ *__restrict__ z, const Dims D, int ii, int jj, int k) {
+    const int hz = D.nz >> 1, hn = (int)(D.n() >> 1);
+    return St<TZ>::ld_ro(z + (((ii + jj + k) & 1) ? hn : 0) + (ii * D.ny + jj) * hz + (k >> 1));
+}
+
 // (r + L z) on the 8 cells of fine group g (L z is 0 at non-fluid cells),
 // neighbour codes from the stencil words (sw, or the codes when sw is NULL).
-template <typename TR, typename TZ>
+// kNC: r and z may be read through the read-only path (see smooth8_pass).
+// kSplitZ: z is a colour-split level-0 vector (r stays in natural order).
+template <bool kNC, bool kSplitZ, typename TR, typename TZ>
 __device__ __forceinline__ void residual_row8(const TR *__restrict__ r, const TZ *__restrict__ z,
                                               const uint8_t *__restrict__ code, const uint16_t *__restrict__ sw,
                                               const Dims D, int g, float out[8]) {
@@ -24,7 +49,7 @@ __device__ __forceinline__ void residual_row8(const TR *__restrict__ r, const TZ
     const int sj = D.nz, si = D.ny * D.nz;
     const int c0 = g << 3;
     float rv[8];
-    St<TR>::ld8_ro(r + c0, rv);
+    if (kNC) St<TR>::ld8_ro(r + c0, rv); else St<TR>::ld8(r + c0, rv);
     const uint4 wd = load_words8(sw, code, D, i, j, k0, c0);
     if (!words_have_fluid(wd)) {
 #pragma unroll
@@ -34,15 +59,30 @@ __device__ __forceinline__ void residual_row8(const TR *__restrict__ r, const TZ
     const bool hip = i + 1 < D.nx, him = i > 0, hjp = j + 1 < D.ny, hjm = j > 0;
     const bool hkp = k0 + 8 < D.nz, hkm = k0 > 0;
     float xc[8], xip[8], xim[8], xjp[8], xjm[8];
-    St<TZ>::ld8_ro(z + c0, xc);
+    auto ld8 = [&](const TZ *p, float o[8]) {
+        if (kNC) St<TZ>::ld8_ro(p, o); else St<TZ>::ld8(p, o);
+    };
+    auto ld1 = [&](const TZ *p) { return kNC ? St<TZ>::ld_ro(p) : St<TZ>::ld(p); };
 #pragma unroll
     for (int m = 0; m < 8; m++) xip[m] = xim[m] = xjp[m] = xjm[m] = 0.0f;
-    if (hip) St<TZ>::ld8_ro(z + c0 + si, xip);
-    if (him) St<TZ>::ld8_ro(z + c0 - si, xim);
-    if (hjp) St<TZ>::ld8_ro(z + c0 + sj, xjp);
-    if (hjm) St<TZ>::ld8_ro(z + c0 - sj, xjm);
-    const float xkm = hkm ? St<TZ>::ld_ro(z + c0 - 1) : 0.0f;
-    const float xkp = hkp ? St<TZ>::ld_ro(z + c0 + 8) : 0.0f;
+    float xkm = 0.0f, xkp = 0.0f;
+    if (kSplitZ) {
+        ld_row8_split(z, D, i, j, kg, xc);
+        if (hip) ld_row8_split(z, D, i + 1, j, kg, xip);
+        if (him) ld_row8_split(z, D, i - 1, j, kg, xim);
+        if (hjp) ld_row8_split(z, D, i, j + 1, kg, xjp);
+        if (hjm) ld_row8_split(z, D, i, j - 1, kg, xjm);
+        if (hkm) xkm = ld_cell_split(z, D, i, j, k0 - 1);
+        if (hkp) xkp = ld_cell_split(z, D, i, j, k0 + 8);
+    } else {
+        ld8(z + c0, xc);
+        if (hip) ld8(z + c0 + si, xip);
+        if (him) ld8(z + c0 - si, xim);
+        if (hjp) ld8(z + c0 + sj, xjp);
+        if (hjm) ld8(z + c0 - sj, xjm);
+        if (hkm) xkm = ld1(z + c0 - 1);
+        if (hkp) xkp = ld1(z + c0 + 8);
+    }
 #pragma unroll
     for (int m = 0; m < 8; m++) {
         float lz = 0.0f;
@@ -66,22 +106,21 @@ __device__ __forceinline__ void residual_row8(const TR *__restrict__ r, const TZ
 // out_scale: restriction scale (times 1/8 between FP16 levels at 8^-l).
 // Grid: one-dimensional, grid-stride by warps (all lanes of a warp run the same
 // iterations, so the shuffles see every lane).
-template <typename TRI, typename TZI, typename TRO>
-__global__ void __launch_bounds__(256, 4) k_restrict8(const TRI *__restrict__ rf, const TZI *__restrict__ zf,
-                                                      const uint8_t *__restrict__ cf, const uint16_t *__restrict__ swf,
-                                                      TRO *__restrict__ rc,
-                                                      const uint8_t *__restrict__ cc, Dims C, float out_scale,
-                                                      const int *__restrict__ act, const int *__restrict__ act_n,
-                                                      unsigned long long *kc) {
-    count_kernel(kc);
+// bid / nblk: this block's index and the number of blocks sharing the loop.
+template <bool kNC, bool kSplitZ, typename TRI, typename TZI, typename TRO>
+__device__ __forceinline__ void restrict8_pass(const TRI *__restrict__ rf, const TZI *__restrict__ zf,
+                                               const uint8_t *__restrict__ cf, const uint16_t *__restrict__ swf,
+                                               TRO *__restrict__ rc, const uint8_t *__restrict__ cc, const Dims C,
+                                               float out_scale, const int *__restrict__ act,
+                                               const int *__restrict__ act_n, int bid, int nblk) {
     const Dims F{2 * C.nx, 2 * C.ny, 2 * C.nz};
     const int nh = (int)(C.n() >> 2);  // coarse half-groups of 4 cells
     const int items = act ? 2 * *act_n : nh;
     const int total = 4 * items;
     const int fz8 = F.nz >> 3;
     const int lane = threadIdx.x & 31, q = lane & 3;
-    const int stride = gridDim.x * blockDim.x;
-    for (int base = blockIdx.x * blockDim.x + (threadIdx.x & ~31); base < total; base += stride) {
+    const int stride = nblk * blockDim.x;
+    for (int base = bid * blockDim.x + (threadIdx.x & ~31); base < total; base += stride) {
         const int t = base + lane;
         const bool valid = t < total;  // the 4 lanes of an item agree (total is a multiple of 4)
         const int it = t >> 2;
@@ -97,7 +136,7 @@ __global__ void __launch_bounds__(256, 4) k_restrict8(const TRI *__restrict__ rf
             int I, J, K4;
             group_ijk(h, Dims{C.nx, C.ny, C.nz << 1}, I, J, K4);  // C.nz / 4 half-groups per row
             const int g = ((2 * I + (q >> 1)) * F.ny + 2 * J + (q & 1)) * fz8 + K4;  // fine group at k = 8 K4
-            residual_row8(rf, zf, cf, swf, F, g, v);
+            residual_row8<kNC, kSplitZ>(rf, zf, cf, swf, F, g, v);
         }
         // coarse cell m gets (v[2m], v[2m + 1]) of lanes q = 0..3 in turn
         float s[4];
@@ -124,6 +163,30 @@ __global__ void __launch_bounds__(256, 4) k_restrict8(const TRI *__restrict__ rf
         }
         St<TRO>::st4(rc + q0, s);
     }
+}
+
+template <typename TRI, typename TZI, typename TRO>
+__global__ void __launch_bounds__(256, 4) k_restrict8(const TRI *__restrict__ rf, const TZI *__restrict__ zf,
+                                                      const uint8_t *__restrict__ cf, const uint16_t *__restrict__ swf,
+                                                      TRO *__restrict__ rc,
+                                                      const uint8_t *__restrict__ cc, Dims C, float out_scale,
+                                                      const int *__restrict__ act, const int *__restrict__ act_n,
+                                                      unsigned long long *kc) {
+    count_kernel(kc);
+    restrict8_pass<true, false>(rf, zf, cf, swf, rc, cc, C, out_scale, act, act_n, blockIdx.x, gridDim.x);
+}
+
+// Restriction out of level 0 whose pre-smoothed z is colour-split
+// (smooth_split.cuh); r is the natural-order residual.
+template <typename TRI, typename TZI, typename TRO>
+__global__ void __launch_bounds__(256, 4) k_restrict8_split(const TRI *__restrict__ rf, const TZI *__restrict__ zf,
+                                                            const uint8_t *__restrict__ cf,
+                                                            const uint16_t *__restrict__ swf, TRO *__restrict__ rc,
+                                                            const uint8_t *__restrict__ cc, Dims C, float out_scale,
+                                                            const int *__restrict__ act,
+                                                            const int *__restrict__ act_n, unsigned long long *kc) {
+    count_kernel(kc);
+    restrict8_pass<true, true>(rf, zf, cf, swf, rc, cc, C, out_scale, act, act_n, blockIdx.x, gridDim.x);
 }
 
 }  // namespace flub

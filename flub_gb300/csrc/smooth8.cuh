@@ -122,9 +122,9 @@ __device__ __forceinline__ void add_coarse_row8(Row8 &o, const TC *__restrict__ 
     for (int m = 0; m < 8; m++) o.v[m] = __fadd_rn(o.v[m], __fmul_rn(cv[m >> 1], scale));
 }
 
-template <typename TC>
+template <bool kNC, typename TC>
 __device__ __forceinline__ float coarse_at(const TC *__restrict__ p, float scale) {
-    return __fmul_rn(St<TC>::ld_ro(p), scale);
+    return __fmul_rn(kNC ? St<TC>::ld_ro(p) : St<TC>::ld(p), scale);
 }
 
 // One cell's red-black update (multigrid/mgpcg.py:72-86 in the reference's
@@ -166,20 +166,23 @@ __device__ __forceinline__ float smooth_cell(uint32_t w, float xc, float xip, fl
 // Requires nz % 8 == 0.  The prolongation variant holds the coarse values as
 // well: 5 blocks per SM (51 registers) instead of 6 (40) keep it free of
 // spills.
-template <bool kFromZero, bool kProlong, typename TO, typename TI, typename TR, typename TC>
-__global__ void __launch_bounds__(256, kProlong ? 5 : 6) k_smooth8(TO *zout, const TI *zin, const TC *__restrict__ zc,
-                                                    float zc_scale, const TR *__restrict__ r,
-                                                    const uint8_t *__restrict__ code,
-                                                    const uint16_t *__restrict__ sw, Dims D, int phase,
-                                                    const int *__restrict__ act, const int *__restrict__ act_n,
-                                                    unsigned long long *kc) {
-    count_kernel(kc);
+// kNC: r and zc may be read through the read-only (non-coherent) path, i.e.
+// nothing writes them while the kernel runs; false inside the persistent
+// V-cycle kernels (persist.cuh), where other blocks wrote them earlier in the
+// same launch.  bid / nblk: this block's index and the number of blocks that
+// share the grid-stride loop.
+template <bool kFromZero, bool kProlong, bool kNC, typename TO, typename TI, typename TR, typename TC>
+__device__ __forceinline__ void smooth8_pass(TO *zout, const TI *zin, const TC *__restrict__ zc, float zc_scale,
+                                             const TR *__restrict__ r, const uint8_t *__restrict__ code,
+                                             const uint16_t *__restrict__ sw, const Dims D, int phase,
+                                             const int *__restrict__ act, const int *__restrict__ act_n, int bid,
+                                             int nblk) {
     const int lane = threadIdx.x & 31;
     const int total = 2 * (act ? *act_n : (int)(D.n() >> 3));
-    const int stride = gridDim.x * blockDim.x;
+    const int stride = nblk * blockDim.x;
     // list entry of this lane's next group, fetched one grid-stride step ahead
     // so that the list read is off the critical path of the loads it feeds
-    const int base0 = blockIdx.x * blockDim.x + (threadIdx.x & ~31);
+    const int base0 = bid * blockDim.x + (threadIdx.x & ~31);
     int g_next = (base0 + lane < total) ? (act ? __ldg(act + ((base0 + lane) >> 1)) : ((base0 + lane) >> 1)) : 0;
     for (int base = base0; base < total; base += stride) {
         const int t = base + lane;
@@ -211,7 +214,7 @@ __global__ void __launch_bounds__(256, kProlong ? 5 : 6) k_smooth8(TO *zout, con
                 const uint4 w8 = words8_from_codes(code, D, i, j, k0, c0);
                 wd = h ? make_uint2(w8.z, w8.w) : make_uint2(w8.x, w8.y);
             }
-            St<TR>::ld4_ro(r + ch, rr);
+            if (kNC) St<TR>::ld4_ro(r + ch, rr); else St<TR>::ld4(r + ch, rr);
             if (!kFromZero) {
                 St<TI>::ld4(zin + ch, zc0);
                 if (hip) St<TI>::ld4(zin + ch + si, zip);
@@ -227,7 +230,7 @@ __global__ void __launch_bounds__(256, kProlong ? 5 : 6) k_smooth8(TO *zout, con
                     float cv[2];
 #define FLUB_ADD_COARSE(row, p)                                                         \
     {                                                                                   \
-        St<TC>::ld2_ro((p), cv);                                                        \
+        if (kNC) St<TC>::ld2_ro((p), cv); else St<TC>::ld2((p), cv);                    \
         _Pragma("unroll") for (int mm = 0; mm < 4; mm++)                                \
             row[mm] = __fadd_rn(row[mm], __fmul_rn(cv[mm >> 1], zc_scale));             \
     }
@@ -237,8 +240,8 @@ __global__ void __launch_bounds__(256, kProlong ? 5 : 6) k_smooth8(TO *zout, con
                     if (hjp) FLUB_ADD_COARSE(zjp, zc + (ci * cy + ((j + 1) >> 1)) * cz + ck)
                     if (hjm) FLUB_ADD_COARSE(zjm, zc + (ci * cy + ((j - 1) >> 1)) * cz + ck)
 #undef FLUB_ADD_COARSE
-                    if (h == 0 && hkm) zout_k = __fadd_rn(zout_k, coarse_at(zc + cb - 1, zc_scale));
-                    if (h == 1 && hkp) zout_k = __fadd_rn(zout_k, coarse_at(zc + cb + 2, zc_scale));
+                    if (h == 0 && hkm) zout_k = __fadd_rn(zout_k, coarse_at<kNC>(zc + cb - 1, zc_scale));
+                    if (h == 1 && hkp) zout_k = __fadd_rn(zout_k, coarse_at<kNC>(zc + cb + 2, zc_scale));
                 }
             }
         }
@@ -286,6 +289,18 @@ __global__ void __launch_bounds__(256, kProlong ? 5 : 6) k_smooth8(TO *zout, con
         }
         St<TO>::st4(zout + ch, out);
     }
+}
+
+template <bool kFromZero, bool kProlong, typename TO, typename TI, typename TR, typename TC>
+__global__ void __launch_bounds__(256, kProlong ? 5 : 6) k_smooth8(TO *zout, const TI *zin, const TC *__restrict__ zc,
+                                                    float zc_scale, const TR *__restrict__ r,
+                                                    const uint8_t *__restrict__ code,
+                                                    const uint16_t *__restrict__ sw, Dims D, int phase,
+                                                    const int *__restrict__ act, const int *__restrict__ act_n,
+                                                    unsigned long long *kc) {
+    count_kernel(kc);
+    smooth8_pass<kFromZero, kProlong, true>(zout, zin, zc, zc_scale, r, code, sw, D, phase, act, act_n, blockIdx.x,
+                                            gridDim.x);
 }
 
 }  // namespace flub

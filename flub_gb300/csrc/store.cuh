@@ -35,6 +35,10 @@ struct St<float> {
         const float2 a = __ldg(reinterpret_cast<const float2 *>(p));
         o[0] = a.x; o[1] = a.y;
     }
+    static __device__ __forceinline__ void ld2(const float *p, float o[2]) {
+        const float2 a = *reinterpret_cast<const float2 *>(p);
+        o[0] = a.x; o[1] = a.y;
+    }
     static __device__ __forceinline__ void st8(float *p, const float v[8]) {
         reinterpret_cast<float4 *>(p)[0] = make_float4(v[0], v[1], v[2], v[3]);
         reinterpret_cast<float4 *>(p)[1] = make_float4(v[4], v[5], v[6], v[7]);
@@ -78,6 +82,10 @@ struct St<__half> {
     }
     static __device__ __forceinline__ void ld2_ro(const __half *p, float o[2]) {
         const float2 a = __half22float2(__ldg(reinterpret_cast<const __half2 *>(p)));
+        o[0] = a.x; o[1] = a.y;
+    }
+    static __device__ __forceinline__ void ld2(const __half *p, float o[2]) {
+        const float2 a = __half22float2(*reinterpret_cast<const __half2 *>(p));
         o[0] = a.x; o[1] = a.y;
     }
     static __device__ __forceinline__ void st8(__half *p, const float v[8]) {

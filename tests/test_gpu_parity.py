@@ -233,6 +233,36 @@ def test_vcycle_fallback_paths_bit_exact(name, monkeypatch):
     assert np.array_equal(z_plain, z_o)
 
 
+@pytest.mark.parametrize("case", [("dam128", "0"), ("dam64", "1")])
+@pytest.mark.parametrize("precision", ["fp32", "mixed"])
+def test_persistent_legs_bit_exact(case, precision, monkeypatch):
+    """The persistent cooperative kernels for the middle levels (FLUB_PERSIST=1)
+    give the same V-cycle and the same solve as one launch per pass, with the
+    reference schedule and the light one: dam128 runs its 64^3 level there
+    (the 32^3 level and below in the cluster), dam64 without the cluster its
+    32^3 level (16^3 and below in the one-block tail)."""
+    name, no_cluster = case
+    scene = TILE_SCENES[name]() if name in TILE_SCENES else SCENES[name]()
+    monkeypatch.setenv("FLUB_NO_CLUSTER", no_cluster)
+    out = []
+    for on in ("1", "0"):
+        monkeypatch.setenv("FLUB_PERSIST", on)
+        tag_o, r0, _ = _setup(scene)
+        mg = MGPCG(3, scene.shape, scene.levels, float, precision=precision)
+        mg.set_tags(dev(tag_o))
+        z = host(mg.apply_preconditioner(dev(r0)))
+        mg.set_schedule("v22")
+        z22 = host(mg.apply_preconditioner(dev(r0)))
+        mg.init(dev(r0), 1.0)
+        mg.mask_interior()
+        info = mg.solve(200, 1e-12, 0.0, 1e-12, smoother="phases")
+        out.append((z, z22, info["iterations"], host(mg.x).copy()))
+    assert np.array_equal(out[0][0], out[1][0]) and np.array_equal(out[0][1], out[1][1])
+    assert out[0][2] == out[1][2] and np.array_equal(out[0][3], out[1][3])
+    if precision == "fp32":
+        assert np.array_equal(out[0][0], O.vcycle(r0, O.tag_levels(tag_o, scene.levels), np.float32))
+
+
 def test_solve_matches_oracle(scene):
     tag_o, r0, mg = _setup(scene)
     info = mg.solve(200, 1e-12, 0.0, 1e-12, smoother="phases")
