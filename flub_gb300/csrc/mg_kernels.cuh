@@ -85,6 +85,18 @@ __device__ __forceinline__ double dot8_ff(const float *x, const float *y) {
 // has completed and its writes are visible (both are no-ops for a launch
 // without the programmatic-serialisation attribute).  Then one increment of the
 // kernel counter per launch (first thread of the first block).
+// Programmatic dependent launch in two steps, for kernels that first read
+// data no earlier kernel of the solve writes (active lists, stencil words):
+// pdl_open lets the next kernel launch, the reads of that constant data follow,
+// and pdl_wait then waits for the previous kernel's results.
+__device__ __forceinline__ void pdl_open() { asm volatile("griddepcontrol.launch_dependents;" ::: "memory"); }
+
+__device__ __forceinline__ void pdl_wait(unsigned long long *kc) {
+    asm volatile("griddepcontrol.wait;" ::: "memory");
+    if (kc && (blockIdx.x | blockIdx.y | blockIdx.z | threadIdx.x | threadIdx.y | threadIdx.z) == 0)
+        atomicAdd(kc, 1ull);
+}
+
 __device__ __forceinline__ void count_kernel(unsigned long long *kc) {
     asm volatile("griddepcontrol.launch_dependents;" ::: "memory");
     asm volatile("griddepcontrol.wait;" ::: "memory");

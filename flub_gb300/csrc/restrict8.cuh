@@ -107,16 +107,20 @@ __device__ __forceinline__ void residual_row8(const TR *__restrict__ r, const TZ
 // Grid: one-dimensional, grid-stride by warps (all lanes of a warp run the same
 // iterations, so the shuffles see every lane).
 // bid / nblk: this block's index and the number of blocks sharing the loop.
+// pdl: called at the start of a kernel launched with programmatic dependent
+// launch; the item count is read first, then pdl_wait(kc).
 template <bool kNC, bool kSplitZ, typename TRI, typename TZI, typename TRO>
 __device__ __forceinline__ void restrict8_pass(const TRI *__restrict__ rf, const TZI *__restrict__ zf,
                                                const uint8_t *__restrict__ cf, const uint16_t *__restrict__ swf,
                                                TRO *__restrict__ rc, const uint8_t *__restrict__ cc, const Dims C,
                                                float out_scale, const int *__restrict__ act,
-                                               const int *__restrict__ act_n, int bid, int nblk) {
+                                               const int *__restrict__ act_n, int bid, int nblk, bool pdl = false,
+                                               unsigned long long *kc = nullptr) {
     const Dims F{2 * C.nx, 2 * C.ny, 2 * C.nz};
     const int nh = (int)(C.n() >> 2);  // coarse half-groups of 4 cells
     const int items = act ? 2 * *act_n : nh;
     const int total = 4 * items;
+    if (pdl) pdl_wait(kc);
     const int fz8 = F.nz >> 3;
     const int lane = threadIdx.x & 31, q = lane & 3;
     const int stride = nblk * blockDim.x;
@@ -172,8 +176,8 @@ __global__ void __launch_bounds__(256, 4) k_restrict8(const TRI *__restrict__ rf
                                                       const uint8_t *__restrict__ cc, Dims C, float out_scale,
                                                       const int *__restrict__ act, const int *__restrict__ act_n,
                                                       unsigned long long *kc) {
-    count_kernel(kc);
-    restrict8_pass<true, false>(rf, zf, cf, swf, rc, cc, C, out_scale, act, act_n, blockIdx.x, gridDim.x);
+    pdl_open();
+    restrict8_pass<true, false>(rf, zf, cf, swf, rc, cc, C, out_scale, act, act_n, blockIdx.x, gridDim.x, true, kc);
 }
 
 // Restriction out of level 0 whose pre-smoothed z is colour-split
@@ -185,8 +189,8 @@ __global__ void __launch_bounds__(256, 4) k_restrict8_split(const TRI *__restric
                                                             const uint8_t *__restrict__ cc, Dims C, float out_scale,
                                                             const int *__restrict__ act,
                                                             const int *__restrict__ act_n, unsigned long long *kc) {
-    count_kernel(kc);
-    restrict8_pass<true, true>(rf, zf, cf, swf, rc, cc, C, out_scale, act, act_n, blockIdx.x, gridDim.x);
+    pdl_open();
+    restrict8_pass<true, true>(rf, zf, cf, swf, rc, cc, C, out_scale, act, act_n, blockIdx.x, gridDim.x, true, kc);
 }
 
 }  // namespace flub

@@ -171,12 +171,14 @@ __device__ __forceinline__ float smooth_cell(uint32_t w, float xc, float xip, fl
 // V-cycle kernels (persist.cuh), where other blocks wrote them earlier in the
 // same launch.  bid / nblk: this block's index and the number of blocks that
 // share the grid-stride loop.
+// kc != NULL: called at the start of a kernel launched with programmatic
+// dependent launch: the list reads come first, then pdl_wait(kc).
 template <bool kFromZero, bool kProlong, bool kNC, typename TO, typename TI, typename TR, typename TC>
 __device__ __forceinline__ void smooth8_pass(TO *zout, const TI *zin, const TC *__restrict__ zc, float zc_scale,
                                              const TR *__restrict__ r, const uint8_t *__restrict__ code,
                                              const uint16_t *__restrict__ sw, const Dims D, int phase,
                                              const int *__restrict__ act, const int *__restrict__ act_n, int bid,
-                                             int nblk) {
+                                             int nblk, bool pdl = false, unsigned long long *kc = nullptr) {
     const int lane = threadIdx.x & 31;
     const int total = 2 * (act ? *act_n : (int)(D.n() >> 3));
     const int stride = nblk * blockDim.x;
@@ -184,6 +186,7 @@ __device__ __forceinline__ void smooth8_pass(TO *zout, const TI *zin, const TC *
     // so that the list read is off the critical path of the loads it feeds
     const int base0 = bid * blockDim.x + (threadIdx.x & ~31);
     int g_next = (base0 + lane < total) ? (act ? __ldg(act + ((base0 + lane) >> 1)) : ((base0 + lane) >> 1)) : 0;
+    if (pdl) pdl_wait(kc);
     for (int base = base0; base < total; base += stride) {
         const int t = base + lane;
         const bool valid = t < total;  // both lanes of a pair agree (total is even)
@@ -298,9 +301,9 @@ __global__ void __launch_bounds__(256, kProlong ? 5 : 6) k_smooth8(TO *zout, con
                                                     const uint16_t *__restrict__ sw, Dims D, int phase,
                                                     const int *__restrict__ act, const int *__restrict__ act_n,
                                                     unsigned long long *kc) {
-    count_kernel(kc);
+    pdl_open();
     smooth8_pass<kFromZero, kProlong, true>(zout, zin, zc, zc_scale, r, code, sw, D, phase, act, act_n, blockIdx.x,
-                                            gridDim.x);
+                                            gridDim.x, true, kc);
 }
 
 }  // namespace flub

@@ -88,7 +88,7 @@ __device__ __forceinline__ uint32_t word_kcode(uint32_t w, bool kp) { return sw_
 
 template <int kMode, typename TRN, typename TR, typename TZI, typename TZ, typename TC>
 __global__ void __launch_bounds__(256, 4) k_smooth_split(const SplitArgs A, int phase, unsigned long long *kc) {
-    count_kernel(kc);
+    pdl_open();
     const Dims D = A.D;
     const int hz = D.nz >> 1;             // split row length
     const int hn = (int)(D.n() >> 1);     // elements per half
@@ -101,6 +101,15 @@ __global__ void __launch_bounds__(256, 4) k_smooth_split(const SplitArgs A, int 
     const int stride = gridDim.x * blockDim.x;
     int t = blockIdx.x * blockDim.x + threadIdx.x;
     int g_next = t < total ? __ldg(A.act + t) : 0;
+    // the list and the first stencil words do not depend on the previous kernel
+    uint2 wd_next = make_uint2(0u, 0u);
+    if (t < total) {
+        int i0, j0, kg0;
+        group_ijk(g_next, D, i0, j0, kg0);
+        wd_next = __ldg(reinterpret_cast<const uint2 *>(A.sws + uoff + (i0 * D.ny + j0) * hz + 4 * kg0));
+    }
+    pdl_wait(kc);
+    bool first = true;
     for (; t < total; t += stride) {
         const int g = g_next;
         const int tn = t + stride;
@@ -109,7 +118,8 @@ __global__ void __launch_bounds__(256, 4) k_smooth_split(const SplitArgs A, int 
         group_ijk(g, D, i, j, kg);
         const int h = (i * D.ny + j) * hz + 4 * kg;  // split index of the group's first element
         const int q = (col + i + j) & 1;             // updated cell m sits at natural k = 8 kg + 2 m + q
-        const uint2 wd = __ldg(reinterpret_cast<const uint2 *>(A.sws + uoff + h));
+        const uint2 wd = first ? wd_next : __ldg(reinterpret_cast<const uint2 *>(A.sws + uoff + h));
+        first = false;
         float rr[4];
         if (kMode == kFirst) {
             // natural residual row -> both halves of the split residual
