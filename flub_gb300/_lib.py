@@ -89,6 +89,8 @@ SIGNATURES = {
     "flub_mg_smooth": (_i32, [_vp, _i32, _i32, _vp]),
     "flub_mg_smooth_iteration": (_i32, [_vp, _i32, _i32, ctypes.POINTER(_i32), _vp]),
     "flub_mg_set_schedule": (_i32, [_vp, _i32, _i32, _f32]),
+    "flub_mg_set_bottom_precision": (_i32, [_vp, _i32]),
+    "flub_mg_get_bottom_precision": (_i32, [_vp, ctypes.POINTER(_i32)]),
     "flub_mg_set_x0_scaled": (_i32, [_vp, _vp, _vp]),
     "flub_mg_level_shape": (_i32, [_vp, _i32, ctypes.POINTER(_i32), ctypes.POINTER(_i32), ctypes.POINTER(_i32)]),
     "flub_mg_level_tags": (_i32, [_vp, _i32, _vp, _vp]),

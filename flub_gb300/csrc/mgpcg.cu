@@ -114,6 +114,7 @@ struct flub_mg {
     int sched_nu;        // red-black iterations per side at every level (< 0: 6 << level)
     int sched_bottom;    // bottom: this many (0, 1) iterations, then as many (1, 0)
     float sched_rscale;  // restriction scale
+    bool bottom64;       // bottom level smoothed in FP64 (flub_mg_set_bottom_precision; mixed precision's default)
 };
 
 namespace flub {
@@ -229,6 +230,9 @@ static size_t tail_layout(const flub_mg *mg, int lt, TailParams *P) {
     P->nu = mg->sched_nu;
     P->nbottom = mg->sched_bottom;
     P->rscale = mg->sched_rscale;
+    P->bottom64 = mg->bottom64 ? 1 : 0;
+    P->off_zd = 0;
+    if (mg->bottom64) P->off_zd = take(sizeof(double) * (size_t)P->lv[P->nt - 1].D.n());
     return off;
 }
 
@@ -469,6 +473,16 @@ static int launch_leg(flub_mg *mg, const LaunchCtx &c, bool down, int l0, int l1
     }
     count_launches(1);
     return FLUB_OK;
+}
+
+// Whether the bottom level runs inside the one-block tail (tail.cuh), alone or
+// inside the cluster kernel: the only place with an FP64 bottom.
+static bool bottom_in_tail(flub_mg *mg) {
+    if (mg->cl_start < mg->levels) {
+        ClusterParams P;
+        return cluster_layout(mg, mg->cl_start, mg->cl_size, &P) > 0 && P.tail;
+    }
+    return mg->tail_start < mg->levels;
 }
 
 static int validate_shape(int nx, int ny, int nz, int levels, int precision) {
@@ -1475,6 +1489,18 @@ int flub_mg_create(int nx, int ny, int nz, int levels, int precision, void *work
     choose_tail(mg);
     choose_cluster(mg);
     choose_persist(mg);
+    if (precision == FLUB_PRECISION_MIXED && bottom_in_tail(mg)) {
+        // mixed precision: FP64 at the coarsest level (the tail layouts grow by
+        // the bottom's doubles, so they are chosen again)
+        mg->bottom64 = true;
+        choose_tail(mg);
+        choose_cluster(mg);
+        if (!bottom_in_tail(mg)) {
+            mg->bottom64 = false;
+            choose_tail(mg);
+            choose_cluster(mg);
+        }
+    }
     if (precision == FLUB_PRECISION_MIXED) {
         // the FP16 sweeps work on rows of 8 cells: every level left to the global
         // kernels needs nz % 8 == 0
@@ -1687,6 +1713,41 @@ int flub_mg_set_schedule(flub_mg *mg, int smooth_iters, int bottom_iters, float 
     mg->sched_rscale = restrict_scale;
     // the cluster kernel's layout depends on the schedule
     FLUB_TRY(choose_cluster(mg));
+    return FLUB_OK;
+}
+
+int flub_mg_set_bottom_precision(flub_mg *mg, int bits) {
+    FLUB_REQUIRE(mg, "flub_mg_set_bottom_precision: NULL handle");
+    FLUB_REQUIRE(bits == 32 || bits == 64, "flub_mg_set_bottom_precision: bits must be 32 or 64, got %d", bits);
+    const bool want = bits == 64;
+    if (mg->bottom64 == want) return FLUB_OK;
+    if (want && !bottom_in_tail(mg)) {
+        set_last_error("flub_mg_set_bottom_precision: the bottom level does not run in the one-block tail here "
+                       "(FP64 bottom needs it)");
+        return FLUB_ERR_UNSUPPORTED;
+    }
+    FLUB_CHECK_CUDA(cudaDeviceSynchronize());
+    for (int g = 0; g < 3; g++)
+        if (mg->graph[g]) {
+            cudaGraphExecDestroy(mg->graph[g]);
+            mg->graph[g] = nullptr;
+        }
+    mg->bottom64 = want;
+    choose_tail(mg);
+    FLUB_TRY(choose_cluster(mg));
+    if (want && !bottom_in_tail(mg)) {
+        mg->bottom64 = false;
+        choose_tail(mg);
+        choose_cluster(mg);
+        set_last_error("flub_mg_set_bottom_precision: the FP64 bottom does not fit the coarse-level kernels");
+        return FLUB_ERR_UNSUPPORTED;
+    }
+    return FLUB_OK;
+}
+
+int flub_mg_get_bottom_precision(flub_mg *mg, int *bits) {
+    FLUB_REQUIRE(mg && bits, "flub_mg_get_bottom_precision: NULL argument");
+    *bits = mg->bottom64 ? 64 : 32;
     return FLUB_OK;
 }
 

@@ -37,6 +37,11 @@ struct TailParams {
     int nu;        // red-black iterations per side at every level (< 0: 6 << level, the reference's)
     int nbottom;   // iterations of each of the two bottom orders (3 in the reference)
     float rscale;  // restriction scale (1 in the reference)
+    // bottom64: the bottom level is smoothed in FP64 (z as doubles at byte
+    // offset off_zd; r converted exactly from FP32), the result rounded to FP32
+    // once for the prolongation.  No reference counterpart: the reference
+    // smooths the bottom in FP32 (multigrid/mgpcg.py:319-336).
+    int bottom64, off_zd;
 };
 
 // ---------------------------------------------------------------- lean smoothing
@@ -212,6 +217,67 @@ __device__ __forceinline__ void tail_prolong(float *zf, const float *zc, const D
     __syncthreads();
 }
 
+// ---------------------------------------------------------------- FP64 bottom
+// tail_lap / tail_update / tail_half_lean in FP64, the same operations in the
+// same order with IEEE double rounding at each (no contraction).
+__device__ __forceinline__ double tail_lap64(const double *z, int c, uint32_t m, int si, int sj) {
+    const double xc = z[c];
+    const double zip = z[(m & 1u) ? c + si : c], zim = z[(m & 2u) ? c - si : c];
+    const double zjp = z[(m & 4u) ? c + sj : c], zjm = z[(m & 8u) ? c - sj : c];
+    const double zkp = z[(m & 16u) ? c + 1 : c], zkm = z[(m & 32u) ? c - 1 : c];
+    double tp, tm, ret = 0.0;
+    tp = (m & 1u) ? __dsub_rn((m & 64u) ? 0.0 : zip, xc) : 0.0;
+    tm = (m & 2u) ? __dsub_rn((m & 128u) ? 0.0 : zim, xc) : 0.0;
+    ret = __dadd_rn(ret, __dadd_rn(tp, tm));
+    tp = (m & 4u) ? __dsub_rn((m & 256u) ? 0.0 : zjp, xc) : 0.0;
+    tm = (m & 8u) ? __dsub_rn((m & 512u) ? 0.0 : zjm, xc) : 0.0;
+    ret = __dadd_rn(ret, __dadd_rn(tp, tm));
+    tp = (m & 16u) ? __dsub_rn((m & 1024u) ? 0.0 : zkp, xc) : 0.0;
+    tm = (m & 32u) ? __dsub_rn((m & 2048u) ? 0.0 : zkm, xc) : 0.0;
+    return __dadd_rn(ret, __dadd_rn(tp, tm));
+}
+
+__device__ __forceinline__ void tail_half64(double *z, const TailCache &tc, const Dims D, int phase, int nthr) {
+    const int si = D.ny * D.nz, sj = D.nz;
+#pragma unroll
+    for (int q = 0; q < kTailPairs; q++) {
+        const int c = tc.idx[q];
+        if (c < 0) continue;
+        const bool odd = (((tc.upd0 >> q) & 1) != 0) == (phase == 0);
+        const uint32_t m = odd ? (tc.msk[q] >> 16) : (tc.msk[q] & 0xffffu);
+        const int cu = c + (odd ? 1 : 0);
+        const double rc = (double)(odd ? tc.r1[q] : tc.r0[q]);
+        double zn = 0.0;
+        const int d = __popc(m & 63u);
+        if ((m & (1u << 12)) && d != 0)
+            zn = __dadd_rn(z[cu], __ddiv_rn(__dadd_rn(rc, tail_lap64(z, cu, m, si, sj)), (double)d));
+        z[cu] = zn;
+    }
+    tail_sync(nthr);
+}
+
+// The bottom's 2 x nbottom red-black iterations in FP64, starting from z = 0,
+// then z rounded to FP32 into zf.
+__device__ __forceinline__ void tail_bottom64(double *zd, float *zf, const TailCache &tc, const Dims D, int nbottom) {
+    const int n = D.nx * D.ny * D.nz;
+    for (int q = threadIdx.x; q < n; q += blockDim.x) zd[q] = 0.0;
+    __syncthreads();
+    const int nthr = tail_threads(D);
+    if ((int)threadIdx.x < nthr) {
+        for (int it = 0; it < nbottom; it++) {
+            tail_half64(zd, tc, D, 0, nthr);
+            tail_half64(zd, tc, D, 1, nthr);
+        }
+        for (int it = 0; it < nbottom; it++) {
+            tail_half64(zd, tc, D, 1, nthr);
+            tail_half64(zd, tc, D, 0, nthr);
+        }
+    }
+    __syncthreads();
+    for (int q = threadIdx.x; q < n; q += blockDim.x) zf[q] = __double2float_rn(zd[q]);
+    __syncthreads();
+}
+
 // The tail sub-V-cycle on one block with the layout P in the shared memory at
 // smem.  io: the first level's r comes from P.r_top / P.r_top_h and its z goes
 // back to P.z_top / P.z_top_h; otherwise both stay in shared memory (the
@@ -258,8 +324,12 @@ __device__ __forceinline__ void tail_run(const TailParams &P, unsigned char *sme
         tail_restrict_cached(V(t), Z(t), tc, D, R(t + 1), C(t + 1), P.lv[t + 1].D, P.rscale);
     }
     tail_cache(tc, C(nb), R(nb), P.lv[nb].D);
-    sweeps(nb, tc, P.nbottom, true);
-    sweeps(nb, tc, P.nbottom, false);
+    if (P.bottom64) {
+        tail_bottom64(reinterpret_cast<double *>(smem + P.off_zd), Z(nb), tc, P.lv[nb].D, P.nbottom);
+    } else {
+        sweeps(nb, tc, P.nbottom, true);
+        sweeps(nb, tc, P.nbottom, false);
+    }
     for (int t = nb - 1; t >= 0; t--) {
         const Dims D = P.lv[t].D;
         tail_prolong(Z(t), Z(t + 1), D);

@@ -139,6 +139,17 @@ class MGPCG:
         _lib.check(self._lib.flub_mg_set_schedule(self._h, nu, nb, rs), "flub_mg_set_schedule")
         self.schedule = schedule if isinstance(schedule, str) else (nu, nb, rs)
 
+    def set_bottom_precision(self, bits):
+        """Bottom-level smoothing in FP32 (the reference's) or FP64 (no
+        reference counterpart; the mixed-precision handle's default).  See
+        flub_mg_set_bottom_precision."""
+        _lib.check(self._lib.flub_mg_set_bottom_precision(self._h, int(bits)), "flub_mg_set_bottom_precision")
+
+    def bottom_precision(self):
+        b = ctypes.c_int(0)
+        _lib.check(self._lib.flub_mg_get_bottom_precision(self._h, ctypes.byref(b)), "flub_mg_get_bottom_precision")
+        return int(b.value)
+
     def set_initial_guess_scaled(self, d):
         """Warm start x0 = gamma d, gamma = (d . b) / (d . L d) computed on the
         device (no reference counterpart; the guess is never worse than 0 in

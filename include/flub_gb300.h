@@ -364,6 +364,18 @@ int flub_vcycle_noalloc(const int32_t *tag, const float *r, float *z, int nx, in
  * schedule changes (the captured solve graphs are rebuilt). */
 int flub_mg_set_schedule(flub_mg *mg, int smooth_iters, int bottom_iters, float restrict_scale);
 
+/* Arithmetic of the bottom level's smoothing (no reference counterpart: the
+ * reference smooths its coarsest level in FP32, multigrid/mgpcg.py:319-336):
+ * bits = 32, or 64 -- the bottom's red-black sweeps in FP64 on the FP32
+ * restricted residual, the result rounded to FP32 once for the prolongation.
+ * FP64 needs the bottom inside the one-block tail of the coarse-level kernels
+ * (FLUB_ERR_UNSUPPORTED otherwise).  Handles created with
+ * FLUB_PRECISION_MIXED start at 64, FP32 handles at 32 (the reference's
+ * arithmetic).  Synchronises the device when the setting changes (the
+ * captured solve graphs are rebuilt). */
+int flub_mg_set_bottom_precision(flub_mg *mg, int bits);
+int flub_mg_get_bottom_precision(flub_mg *mg, int *bits);
+
 /* Warm start scaled on the device (no reference counterpart): x0 = gamma d
  * with gamma = (d . b) / (d . L d) over fluid cells, b the current right-hand
  * side (flub_mg_init + flub_mg_mask_interior), L the solver's operator --

@@ -71,6 +71,8 @@ def _declare(L):
     L.oracle_num_threads.restype = i32
     L.oracle_set_schedule.argtypes = [i32, i32, f64]
     L.oracle_set_schedule.restype = None
+    L.oracle_set_bottom_fp64.argtypes = [i32]
+    L.oracle_set_bottom_fp64.restype = None
     L.oracle_solid_vel.argtypes = [vp, vp, i32, i32, i32, i32, f32, vp, vp, vp, i32]
     L.oracle_fraction_quad.argtypes = [f32, f32, f32, f32, f32]
     L.oracle_fraction_quad.restype = f32
@@ -110,6 +112,20 @@ class schedule:
 
     def __exit__(self, *exc):
         lib().oracle_set_schedule(*REFERENCE_SCHEDULE)
+        return False
+
+
+class bottom_fp64:
+    """Context manager: the FP32 V-cycle smooths its bottom level in FP64
+    (the library's flub_mg_set_bottom_precision(64)); no reference
+    counterpart."""
+
+    def __enter__(self):
+        lib().oracle_set_bottom_fp64(1)
+        return self
+
+    def __exit__(self, *exc):
+        lib().oracle_set_bottom_fp64(0)
         return False
 
 

@@ -35,6 +35,14 @@ void oracle_set_schedule(int nu, int bottom, double rscale) {
     oracle_sched_rscale = rscale;
 }
 
+/* FP64 bottom level for the FP32 V-cycle (no reference counterpart; the
+ * library's flub_mg_set_bottom_precision(64)): the bottom's sweeps run on
+ * doubles from z = 0 with the FP32 residual converted exactly, the result is
+ * rounded to FP32 once.  Off by default (the reference smooths in FP32). */
+static int oracle_bottom64 = 0;
+void oracle_set_bottom_fp64(int on) { oracle_bottom64 = on; }
+static void oracle_bottom_fp64_f32(float *z, const float *r, const int32_t *tag, int nx, int ny, int nz);
+
 /* ---------------- precision-generic solver pieces ---------------- */
 #define REAL float
 #define FN(name) name##_f32
@@ -791,6 +799,24 @@ void oracle_tag_levels(int32_t **tagl, int levels, int nx, int ny, int nz) {
 }
 
 /* Level-hierarchy helpers so that Python can drive the V-cycle directly. */
+static void oracle_bottom_fp64_f32(float *z, const float *r, const int32_t *tag, int nx, int ny, int nz) {
+    int64_t n = (int64_t)nx * ny * nz;
+    double *zd = (double *)calloc((size_t)n, sizeof(double));
+    double *rd = (double *)malloc(sizeof(double) * (size_t)n);
+    for (int64_t c = 0; c < n; c++) rd[c] = (double)r[c];
+    for (int it = 0; it < oracle_sched_bottom; it++) {
+        oracle_smooth_f64(zd, rd, tag, nx, ny, nz, 0);
+        oracle_smooth_f64(zd, rd, tag, nx, ny, nz, 1);
+    }
+    for (int it = 0; it < oracle_sched_bottom; it++) {
+        oracle_smooth_f64(zd, rd, tag, nx, ny, nz, 1);
+        oracle_smooth_f64(zd, rd, tag, nx, ny, nz, 0);
+    }
+    for (int64_t c = 0; c < n; c++) z[c] = (float)zd[c];
+    free(zd);
+    free(rd);
+}
+
 void oracle_vcycle_levels_f32(float *r0, float *z0, int32_t **tagl, int levels, int nx, int ny, int nz) {
     float **rl = (float **)malloc(sizeof(float *) * (size_t)levels);
     float **zl = (float **)malloc(sizeof(float *) * (size_t)levels);

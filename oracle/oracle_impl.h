@@ -145,7 +145,10 @@ void FN(oracle_vcycle)(REAL **rl, REAL **zl, int32_t **tagl, int levels, int nx,
         memset(zl[l + 1], 0, (size_t)nc * sizeof(REAL));
         FN(oracle_restrict)(rl[l], zl[l], tagl[l], rl[l + 1], tagl[l + 1], ax / 2, ay / 2, az / 2);
     }
-    {
+    if (oracle_bottom64 && sizeof(REAL) == sizeof(float)) {
+        int l = levels - 1;
+        oracle_bottom_fp64_f32((float *)zl[l], (const float *)rl[l], tagl[l], nx >> l, ny >> l, nz >> l);
+    } else {
         int l = levels - 1;
         int ax = nx >> l, ay = ny >> l, az = nz >> l;
         for (int it = 0; it < oracle_sched_bottom; it++) {

@@ -578,6 +578,44 @@ def test_light_schedule_projection_matches_fp64_oracle(precision):
     assert err <= PRESSURE_RTOL, err
 
 
+@pytest.mark.parametrize("no_cluster", ["0", "1"])
+@pytest.mark.parametrize("sched", ["reference", "v22"])
+def test_fp64_bottom_vcycle_bit_exact(sched, no_cluster, monkeypatch):
+    """The bottom level smoothed in FP64 (flub_mg_set_bottom_precision(64), no
+    reference counterpart) against the oracle doing the same, bit for bit, in
+    the cluster kernel's tail and in the one-block tail kernel."""
+    monkeypatch.setenv("FLUB_NO_CLUSTER", no_cluster)
+    scene = SCENES["dam64"]()
+    tag_o, r0, mg = _setup(scene)
+    assert mg.bottom_precision() == 32
+    mg.set_schedule(sched)
+    z32 = host(mg.apply_preconditioner(dev(r0)))
+    mg.set_bottom_precision(64)
+    assert mg.bottom_precision() == 64
+    z64 = host(mg.apply_preconditioner(dev(r0)))
+    tags = O.tag_levels(tag_o, scene.levels)
+    nu, nb, rs = (-1, 3, 1.0) if sched == "reference" else (2, 4, 0.5)
+    with O.schedule(nu, nb, rs):
+        assert np.array_equal(z32, O.vcycle(r0, tags, np.float32))
+        with O.bottom_fp64():
+            z64_o = O.vcycle(r0, tags, np.float32)
+    assert np.array_equal(z64, z64_o)
+    assert not np.array_equal(z64, z32)  # the bottom's arithmetic did change
+    info = mg.solve(200, 1e-12, 0.0, 1e-12, smoother="phases")
+    assert info["converged"]
+
+
+def test_mixed_handle_defaults_to_fp64_bottom():
+    scene = SCENES["dam64"]()
+    tag_o, r0, _ = _setup(scene)
+    mgm = MGPCG(3, scene.shape, scene.levels, float, precision="mixed")
+    assert mgm.bottom_precision() == 64
+    mgm.set_bottom_precision(32)
+    assert mgm.bottom_precision() == 32
+    with pytest.raises(FlubError):
+        mgm.set_bottom_precision(16)
+
+
 def test_schedule_rejects_bad_values():
     mg = MGPCG(3, (32, 32, 32), 3, float)
     for bad in [(0, 8, 0.5), (2, 0, 0.5), (2, 8, 0.0), (2, 8, 2.0), (65, 8, 0.5)]:

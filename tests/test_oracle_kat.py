@@ -403,3 +403,21 @@ def test_subtract_gradient_batty_kat():
     uf[:] = 0.0
     O.subtract_gradient_batty(uf, p, frac, phi, ur, 1, 0.0, 1.0 / nx)
     assert uf[1, 0, 0] == 7.0                                            # zero fraction: rigid velocity
+
+
+def test_fp64_bottom_changes_only_the_rounding():
+    """The FP64 bottom (no reference counterpart) leaves the V-cycle within FP32
+    rounding of the FP32 one, and exactly equal to it when the bottom is
+    already exact (no fluid at the bottom)."""
+    from flub_gb300 import scenes
+    s = scenes.dam(32, seed=60, levels=3)
+    tag, _ = O.classify(s.phi, s.prims, s.h, s.h0)
+    div = O.divergence(s.u, s.v, s.w, s.ur, s.vr, s.wr, tag)
+    r0 = np.where(tag == 1, div, 0).astype(np.float32)
+    tags = O.tag_levels(tag, 3)
+    z32 = O.vcycle(r0, tags, np.float32)
+    with O.bottom_fp64():
+        z64 = O.vcycle(r0, tags, np.float32)
+    assert not np.array_equal(z32, z64)
+    assert np.linalg.norm(z64 - z32) <= 1e-5 * np.linalg.norm(z32)
+    assert np.array_equal(O.vcycle(r0, tags, np.float32), z32)  # the switch is restored on exit
