@@ -70,6 +70,9 @@ def parse_args():
                     help="skip the FP64 host projection that checks each variant's pressure")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-scale512", action="store_true", help="skip the 512^3 dam-break timings")
+    ap.add_argument("--no-oracle512", action="store_true",
+                    help="skip the FP64 host projection of the 512^3 scene (about a minute on 16 cores)")
+    ap.add_argument("--no-sphere128", action="store_true", help="skip the 128^3 flow-past-a-sphere block")
     ap.add_argument("--profile-kernel",
                     choices=["smooth", "restrict", "matvec", "solve", "project", "advect", "warmstart"],
                     default=None,
@@ -650,6 +653,44 @@ def run_ours(args):
                                  "(N = 16..64) whose per-tap operand loads bound them, far from the tensor peak"}
         del tnet, div_b, tag_b, x_b
 
+    # ---- config 1: 128^3 flow past a sphere, plain vs mixed precision, both
+    # schedules, each against the FP64 oracle's projection of the same scene
+    sphere128 = None
+    if rank == 0 and not args.no_sphere128:
+        import oracle as O
+        s1 = scenes.CONFIGS["sphere128"]()
+        ref1 = O.project(s1, max_iters=200, rel_tol=1e-12, abs_tol=0.0, dtype=np.float64)
+        p1 = torch.from_numpy(ref1["p"].astype(np.float64)).cuda()
+        dv = lambda a: torch.from_numpy(np.ascontiguousarray(a)).cuda()
+        v1_0 = [dv(a) for a in (s1.u, s1.v, s1.w)]
+        v1 = MACGrid(*(Field(a.clone(), d=d + 1) for d, a in enumerate(v1_0)))
+        vr1 = MACGrid(*(Field(dv(a), d=d + 1) for d, a in enumerate((s1.ur, s1.vr, s1.wr))))
+        phi1 = dv(s1.phi)
+        sphere128 = {"scene": "sphere128: 128^3, solid sphere r = 0.15 at the centre, solid inflow layer (u = 1), "
+                              "air outflow layer", "levels": s1.levels, "fp64_oracle_iterations": int(ref1["iters"])}
+        for name in ("plain", "mixed", "plain-v22", "mixed-v22"):
+            prec, sched, _ = VARIANT_SETUP[name]
+            pj = Projection(s1.shape, s1.levels, precision=prec, schedule=sched)
+            times = []
+            for rep in range(6):
+                for a, b in zip((v1.u.f, v1.v.f, v1.w.f), v1_0):
+                    a.copy_(b)
+                e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+                e0.record(stream)
+                pj.project(v1, vr1, phi1, s1.prims, sync=False, **solve_kw)
+                e1.record(stream)
+                torch.cuda.synchronize()
+                if rep >= 2:
+                    times.append(e0.elapsed_time(e1))
+            inf = pj.mg.info()
+            sphere128[name] = {"ms_per_solve": statistics.median(times), "iterations": inf["iterations"],
+                               "converged": bool(inf["converged"]),
+                               "pressure_rel_l2_vs_fp64_oracle": float((pj.p.f.double() - p1).norm() / p1.norm()),
+                               "max_abs_div_after": pj.max_abs_div(v1, vr1)}
+            del pj
+        del v1, vr1, v1_0, phi1, p1
+        torch.cuda.empty_cache()
+
     # ---- the 512^3 dam break (the 256^3 scene scaled up, generated on the
     # device): ms per solve of plain FP32 (reference schedule), plain-v22 and
     # learned+mixed-v22, each to relative residual 1e-6; the pressures of the
@@ -666,6 +707,7 @@ def run_ours(args):
         scale512 = {"scene": "dam512 (device-generated, same layout as dam256)", "cells": s5.n_cells,
                     "levels": s5.levels}
         p_plain = None
+        p5 = {}
         for name in ("plain", "plain-v22", "learned+mixed-v22"):
             prec, sched, use_net = VARIANT_SETUP[name]
             if use_net and net is None:
@@ -688,28 +730,44 @@ def run_ours(args):
                      "converged": bool(inf["converged"]), "max_abs_div_after": pj.max_abs_div(v5, vr5)}
             if p_plain is None:
                 p_plain = pj.p.f.detach().double().clone()
-                # the level-0 half-sweep at 512^3 (8x the groups of the 256^3 launch)
-                for ph in (0, 1):
-                    pj.mg.smooth(0, ph)
+                # the level-0 half-sweep at 512^3 (8x the groups of the 256^3 launch),
+                # the kernel the V-cycle runs there (two half-sweeps per call)
+                kind = pj.mg.smooth_iteration(0, 0)
                 torch.cuda.synchronize()
                 e0.record(stream)
-                for q in range(24):
-                    pj.mg.smooth(0, q & 1)
+                for q in range(12):
+                    pj.mg.smooth_iteration(0, q & 1)
                 e1.record(stream)
                 torch.cuda.synchronize()
-                sweep_ms = e0.elapsed_time(e1) / 24
+                sweep_ms = e0.elapsed_time(e1) / 12 / (1 if kind == 1 else 2)
                 f5 = (pj.tag.f == 1).view(512, 512, 64, 8).any(dim=-1)
                 na = int(f5.sum().item())
                 ab = SMOOTH_HALF_SWEEP_BYTES_PER_CELL * 8 * na + 4.0 * na
-                scale512["k_smooth8_level0"] = {"launch_ms": sweep_ms, "active_groups": na, "alg_bytes": ab,
-                                                "achieved_GBps": ab / (sweep_ms * 1e-3) / 1e9,
-                                                "frac_of_measured_peak": ab / (sweep_ms * 1e-3) / 1e9 / peak}
+                scale512["level0_half_sweep"] = {
+                    "kernel": "k_smooth_split<kInPlace>" if kind == 2 else "k_smooth8<false,false>",
+                    "launch_ms": sweep_ms, "active_groups": na, "alg_bytes": ab,
+                    "achieved_GBps": ab / (sweep_ms * 1e-3) / 1e9,
+                    "frac_of_measured_peak": ab / (sweep_ms * 1e-3) / 1e9 / peak}
             else:
                 entry["pressure_rel_l2_vs_plain"] = float((pj.p.f.double() - p_plain).norm() / p_plain.norm())
+            p5[name] = pj.p.f.detach().clone()
             scale512[name] = entry
             del pj, ws5
             torch.cuda.empty_cache()
-        del s5, v5, vr5, v5_0, p_plain
+        if not args.no_oracle512:
+            # the FP64 oracle's projection of the same scene on the host cores
+            import oracle as O
+            t_o = time.time()
+            host = scenes.Scene("dam512", s5.shape, s5.levels, s5.phi.cpu().numpy(), s5.prims,
+                                *(a.cpu().numpy() for a in v5_0), *(a.f.cpu().numpy() for a in (vr5.u, vr5.v, vr5.w)))
+            ref5 = O.project(host, max_iters=200, rel_tol=1e-12, abs_tol=0.0, dtype=np.float64)
+            p64 = torch.from_numpy(ref5["p"].astype(np.float64)).cuda()
+            for name, pv in p5.items():
+                scale512[name]["pressure_rel_l2_vs_fp64_oracle"] = float((pv.double() - p64).norm() / p64.norm())
+            scale512["fp64_oracle"] = {"iterations": int(ref5["iters"]), "host_s": time.time() - t_o,
+                                       "threads": O.num_threads()}
+            del host, ref5, p64
+        del s5, v5, vr5, v5_0, p_plain, p5
         torch.cuda.empty_cache()
 
     # ---- CPU baseline: the oracle on the host cores (rank 0, N = 1 only)
@@ -746,7 +804,8 @@ def run_ours(args):
                        "parallelism": f"replicas x{world}"},
             "roofline": roofline, "cpu_baseline": cpu, "e2e": e2e, "gpu_launches": int(launches),
             "extrapolation": extrapolation, "advection": advection, "redistance": redistance_info,
-            "tile_smoother": tile_smoother, "dam512": scale512, "unet_training": unet_training,
+            "tile_smoother": tile_smoother, "sphere128": sphere128, "dam512": scale512,
+            "unet_training": unet_training,
             "clocks": clocks,
         }
         print(json.dumps(out), flush=True)

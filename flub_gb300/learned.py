@@ -191,14 +191,18 @@ class WarmStart:
         return d
 
 
-def evaluate(net, data, precision="fp32", rel_tol=1e-12, max_iters=200, log=None):
+def evaluate(net, data, precision="fp32", rel_tol=1e-12, max_iters=200, log=None, schedule="reference", level=0):
     """Solve every scene cold (x0 = 0) and warm (x0 = scaled network guess)
-    to the same tolerance.  Returns per-scene iteration counts and the
-    network's relative L2 error against the converged solution on fluid."""
+    to the same tolerance, with the V-cycle ``schedule`` and the network on
+    hierarchy ``level``.  Returns per-scene iteration counts and the network's
+    relative L2 error against the converged solution on fluid; the summary
+    also times the guess and a cold solve (CUDA events, warm) and gives the
+    break-even: the iterations a guess must save to pay for itself."""
     shape = data.shape
     n = shape[0]
-    mg = MGPCG(3, shape, scenes._default_levels(n), float, precision=precision, device=data.rhs.device)
-    ws = WarmStart(net, level=0)
+    mg = MGPCG(3, shape, scenes._default_levels(n), float, precision=precision, device=data.rhs.device,
+               schedule=schedule)
+    ws = WarmStart(net, level=level)
     rows = []
     for s in range(len(data)):
         tag = data.tag[s]
@@ -225,11 +229,36 @@ def evaluate(net, data, precision="fp32", rel_tol=1e-12, max_iters=200, log=None
             log(f"evaluated {s + 1}/{len(data)}")
     cold = np.array([r["cold"] for r in rows])
     warm = np.array([r["warm"] for r in rows])
-    summary = dict(scenes=len(rows), precision=precision, cold_mean=float(cold.mean()), warm_mean=float(warm.mean()),
-                   saved_mean=float((cold - warm).mean()), saved_min=int((cold - warm).min()),
-                   saved_max=int((cold - warm).max()),
+    # cost of a guess and of one CG iteration, on the last scene
+    ev = [torch.cuda.Event(enable_timing=True) for _ in range(4)]
+    reps = 10
+    ws.apply(mg)
+    torch.cuda.synchronize()
+    ev[0].record()
+    for _ in range(reps):
+        ws.apply(mg)
+    ev[1].record()
+    for _ in range(reps):
+        mg.init(data.rhs[len(data) - 1], 1.0)
+        mg.mask_interior()
+        info = mg.solve(max_iters, 1e-12, 0.0, rel_tol, smoother="phases", sync=False)
+    ev[2].record()
+    torch.cuda.synchronize()
+    guess_ms = ev[0].elapsed_time(ev[1]) / reps
+    solve_ms = ev[1].elapsed_time(ev[2]) / reps
+    iters_last = mg.info()["iterations"]
+    ms_per_iter = solve_ms / max(iters_last, 1)
+    saved = cold - warm
+    summary = dict(scenes=len(rows), precision=precision, schedule=schedule, network_level=level,
+                   network_grid=list(mg.level_shape(level)), cold_mean=float(cold.mean()),
+                   warm_mean=float(warm.mean()), saved_mean=float(saved.mean()), saved_min=int(saved.min()),
+                   saved_max=int(saved.max()),
+                   saved_histogram={str(int(k)): int(v) for k, v in zip(*np.unique(saved, return_counts=True))},
                    err_net_mean=float(np.mean([r["err_net"] for r in rows])),
-                   all_converged=all(r["converged"] for r in rows))
+                   gamma_mean=float(np.mean([r["gamma"] for r in rows])),
+                   all_converged=all(r["converged"] for r in rows), guess_ms=guess_ms, cold_solve_ms=solve_ms,
+                   ms_per_iteration=ms_per_iter, break_even_iterations=guess_ms / ms_per_iter,
+                   net_gain_ms_mean=float(saved.mean()) * ms_per_iter - guess_ms)
     return summary, rows
 
 
@@ -245,9 +274,17 @@ def main(argv=None):
     ap.add_argument("--out", default=WEIGHTS)
     ap.add_argument("--report", default=None, help="JSON report path")
     ap.add_argument("--init", default=None, help="start from these weights")
+    ap.add_argument("--eval-only", action="store_true",
+                    help="evaluate the weights at --out on the held-out scenes under every schedule of "
+                         "--schedules and network level of --levels, fp32 and mixed, and add the results to "
+                         "--report (an existing report is updated)")
+    ap.add_argument("--schedules", default="reference,v22")
+    ap.add_argument("--levels", default="0,1")
     args = ap.parse_args(argv)
     dev = torch.device("cuda", 0)
     log = lambda m: print(m, flush=True)
+    if args.eval_only:
+        return _eval_only(args, dev, log)
     t0 = time.time()
     train_set = generate(args.train, args.n, seed0=100000 + args.seed * 1000003, device=dev, log=log)
     eval_set = generate(args.eval, args.n, seed0=900000 + args.seed * 1000003, device=dev, log=log)
@@ -276,6 +313,30 @@ def main(argv=None):
     if args.report:
         with open(args.report, "w") as f:
             json.dump(dict(report, rows_fp32=rows, rows_mixed=rows_m), f, indent=1)
+    return report
+
+
+def _eval_only(args, dev, log):
+    net = UNet3D.load(args.out, device=dev)
+    eval_set = generate(args.eval, args.n, seed0=900000 + args.seed * 1000003, device=dev, log=log)
+    held_out = []
+    for sched in args.schedules.split(","):
+        for level in (int(v) for v in args.levels.split(",")):
+            for prec in ("fp32", "mixed"):
+                summary, _ = evaluate(net, eval_set, prec, schedule=sched, level=level, log=log)
+                log(json.dumps(summary))
+                held_out.append(summary)
+    report = {}
+    if args.report and os.path.exists(args.report):
+        with open(args.report) as f:
+            report = json.load(f)
+    report["held_out"] = held_out
+    report["held_out_command"] = ("python -m flub_gb300.learned --eval-only --eval %d --n %d --schedules %s "
+                                  "--levels %s --report <report.json>" % (args.eval, args.n, args.schedules,
+                                                                          args.levels))
+    if args.report:
+        with open(args.report, "w") as f:
+            json.dump(report, f, indent=1)
     return report
 
 

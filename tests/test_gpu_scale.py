@@ -1,16 +1,19 @@
 """The 512^3 dam break (the benchmark scene scaled up, generated on the
 device): the light-schedule FP32 and learned + mixed-precision solves
-converge, and their pressures agree.  At this size the FP64 host oracle would
-take minutes, so the checks are size-independent: the solver's own residual
-test, the true residual ||b - L x|| / ||b|| evaluated in FP64 (a gross-error
-check only: rounding even the exact solution to FP32 leaves ~1e-3 there,
-since ||x|| / ||b|| ~ 1e4 at this size), and the agreement of two differently
-computed solutions (FP32 V(2,2) vs FP16 V-cycle with a learned guess)."""
+converge to relative residual 1e-6, and their pressures are within relative
+L2 1e-5 of the FP64 oracle's projection of the same scene (run on the host
+cores).  The true residual ||b - L x|| / ||b|| of each FP32 solution,
+evaluated in FP64, must be within 4x of that of the oracle's FP64 solution
+rounded to FP32: at this size ||x|| / ||b|| ~ 1e4, so FP32 rounding of even
+the exact solution leaves ~6e-5 there, and the FP32 updates x += alpha p of
+a 24-iteration solve add a few times that (measured 2.7x)."""
 import os
 
+import numpy as np
 import pytest
 import torch
 
+import oracle as O
 from flub_gb300 import Projection, learned, scenes
 from flub_gb300.fields import Field, MACGrid
 
@@ -43,21 +46,30 @@ def _lap64(x, tag):
     return torch.where(tag == 1, out, torch.zeros_like(out))
 
 
-def _true_residual(proj):
-    """||b - L x|| / ||b|| in FP64 for the FP32 solution x."""
+def _true_residual(proj, x=None):
+    """||b - L x|| / ||b|| in FP64 for an FP32 solution x (the solver's own by
+    default)."""
     mg = proj.mg
     tag = proj.tag.f
     div = proj.div.f
     b = torch.where(tag == 1, div * torch.tensor(-proj.h0, dtype=torch.float32, device=div.device),
                     torch.zeros_like(div)).double()
-    res = b - _lap64(mg.x.view(mg.shape).double(), tag)
+    x = mg.x.view(mg.shape) if x is None else x
+    res = b - _lap64(x.double(), tag)
     return float(res.norm() / b.norm())
 
 
-def test_dam512_light_and_learned_mixed_agree():
+def test_dam512_light_and_learned_mixed_against_fp64_oracle():
     s = scenes.dam_device(512, 2, "cuda")
     v0 = [a.clone() for a in (s.u, s.v, s.w)]
     vr = MACGrid(*(Field(a, d=d + 1) for d, a in enumerate((s.ur, s.vr, s.wr))))
+    host = scenes.Scene("dam512", s.shape, s.levels, s.phi.cpu().numpy(), s.prims, *(a.cpu().numpy() for a in v0),
+                        *(a.cpu().numpy() for a in (s.ur, s.vr, s.wr)))
+    ref = O.project(host, max_iters=200, rel_tol=1e-12, abs_tol=0.0, dtype=np.float64)
+    assert ref["converged"]
+    p64 = torch.from_numpy(ref["p"].astype(np.float64)).cuda()
+    x64_32 = torch.from_numpy(ref["x"].astype(np.float32)).cuda()
+    del host
     out = {}
     for name, prec, use_net in (("plain-v22", "fp32", False), ("learned+mixed-v22", "mixed", True)):
         if use_net and not os.path.exists(learned.WEIGHTS):
@@ -68,7 +80,13 @@ def test_dam512_light_and_learned_mixed_agree():
         info = proj.project(vel, vr, s.phi, s.prims, max_iters=200, eps=1e-12, abs_tol=0.0, rel_tol=1e-12,
                             smoother="phases", warm_start=ws)
         assert info["converged"] and info["rtr"] < 1e-12 * info["rtr0"], (name, info)
-        assert _true_residual(proj) < 1e-3, name
+        floor = _true_residual(proj, x64_32)
+        true_res = _true_residual(proj)
+        err = float((proj.p.f.double() - p64).norm() / p64.norm())
+        print(f"\n{name}: {info['iterations']} iterations (FP64 oracle {ref['iters']}), pressure rel. L2 vs FP64 "
+              f"{err:.2e}, true residual {true_res:.2e} (FP32 rounding floor {floor:.2e})")
+        assert true_res <= 4.0 * floor, (name, true_res, floor)
+        assert err <= RTOL_PRESSURE, (name, err)
         out[name] = proj.p.f.double().clone()
         assert proj.max_abs_div(vel, vr) < 1e-2
         del proj
