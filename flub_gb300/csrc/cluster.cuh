@@ -23,6 +23,8 @@
 #include <cuda_fp16.h>
 
 #include "mg_kernels.cuh"
+#include "restrict8.cuh"
+#include "smooth8.cuh"
 #include "tail.cuh"
 
 namespace flub {
@@ -42,7 +44,33 @@ struct ClusterLevel {
     int off_z, off_c, off_r;  // shared-memory byte offsets
 };
 
+// The level just above the distributed ones, run by the same cluster in
+// global memory (where it stays resident in L2) over its active list: its
+// pre-smoothing and restriction before the distributed levels, its
+// prolongation and post-smoothing after them, one cluster barrier between
+// passes instead of one kernel launch per pass.  The passes are k_smooth8's
+// and k_restrict8's (smooth8.cuh, restrict8.cuh) with L2-only loads of what
+// other blocks of the cluster wrote.
+struct ClusterGlobal {
+    int on, half;  // half: FP16 level storage (mixed precision)
+    Dims D;
+    const uint8_t *code;
+    const uint16_t *sw;
+    const int *act, *act_n;
+    void *r, *z, *z2;  // the level's residual and corrections (float or __half)
+    int iters;         // red-black iterations per side
+    float rscale;      // restriction output scale
+    float zc_scale;    // prolongation input scale
+    // the first distributed level (restriction target, prolongation source)
+    Dims CD;
+    const uint8_t *ccode;
+    const int *cact, *cact_n;
+    void *cr;
+    const void *cz;
+};
+
 struct ClusterParams {
+    ClusterGlobal g;
     int nl;
     ClusterLevel lv[kClusterMaxLevels];
     const float *r_top;  // residual of the first cluster level (global)
@@ -301,11 +329,67 @@ __device__ __forceinline__ void cl_prolong(const ClusterCtx &x, const ClusterPar
     x.cl.sync();
 }
 
+// Pre-smoothing of the global level, then its restriction into the first
+// distributed level's global r (read back into shared memory afterwards).
+template <typename T>
+__device__ __noinline__ void cl_global_down(const ClusterCtx &x, const ClusterGlobal &G) {
+    const int b = (int)x.rank, nb = (int)x.cl.num_blocks();
+    const T *r = static_cast<const T *>(G.r);
+    T *z2 = static_cast<T *>(G.z2);
+    for (int it = 0; it < G.iters; it++) {
+        if (it == 0)
+            smooth8_pass<true, false, false, T, T, T, T>(z2, z2, nullptr, 1.0f, r, G.code, G.sw, G.D, 0, G.act,
+                                                         G.act_n, b, nb);
+        else
+            smooth8_pass<false, false, false, T, T, T, T>(z2, z2, nullptr, 1.0f, r, G.code, G.sw, G.D, 0, G.act,
+                                                          G.act_n, b, nb);
+        x.cl.sync();
+        smooth8_pass<false, false, false, T, T, T, T>(z2, z2, nullptr, 1.0f, r, G.code, G.sw, G.D, 1, G.act,
+                                                      G.act_n, b, nb);
+        x.cl.sync();
+    }
+    restrict8_pass<false, false>(r, (const T *)z2, G.code, G.sw, static_cast<T *>(G.cr), G.ccode, G.CD, G.rscale,
+                                 G.cact, G.cact_n, b, nb);
+    x.cl.sync();
+}
+
+// Prolongation of the first distributed level's z (written back to global
+// memory) into the global level, fused with its first post-smoothing
+// half-sweep, then the other half-sweeps.
+template <typename T>
+__device__ __noinline__ void cl_global_up(const ClusterCtx &x, const ClusterGlobal &G) {
+    const int b = (int)x.rank, nb = (int)x.cl.num_blocks();
+    const T *r = static_cast<const T *>(G.r);
+    T *z = static_cast<T *>(G.z);
+    for (int it = 0; it < G.iters; it++) {
+        if (it == 0)
+            smooth8_pass<false, true, false, T, T, T, T>(z, static_cast<const T *>(G.z2),
+                                                         static_cast<const T *>(G.cz), G.zc_scale, r, G.code, G.sw,
+                                                         G.D, 1, G.act, G.act_n, b, nb);
+        else
+            smooth8_pass<false, false, false, T, T, T, T>(z, z, nullptr, 1.0f, r, G.code, G.sw, G.D, 1, G.act,
+                                                          G.act_n, b, nb);
+        x.cl.sync();
+        smooth8_pass<false, false, false, T, T, T, T>(z, z, nullptr, 1.0f, r, G.code, G.sw, G.D, 0, G.act,
+                                                      G.act_n, b, nb);
+        if (it + 1 < G.iters) x.cl.sync();
+    }
+}
+
+// kGlobal: P.g holds the global level above the distributed ones (a separate
+// instantiation, so that the kernel without it keeps its register budget).
+template <bool kGlobal>
 __global__ void __launch_bounds__(kClusterThreads, 1) k_cluster_vcycle(const ClusterParams P, unsigned long long *kc) {
     extern __shared__ __align__(16) unsigned char cluster_smem[];
     count_kernel(kc);
     ClusterCtx x{cg::this_cluster(), 0u, cluster_smem};
     x.rank = x.cl.block_rank();
+    if (kGlobal) {
+        if (P.g.half)
+            cl_global_down<__half>(x, P.g);
+        else
+            cl_global_down<float>(x, P.g);
+    }
     // cell codes of the owned planes and both ghost planes (0 outside the domain)
     for (int t = 0; t < P.nl; t++) {
         const ClusterLevel &L = P.lv[t];
@@ -328,10 +412,11 @@ __global__ void __launch_bounds__(kClusterThreads, 1) k_cluster_vcycle(const Clu
             const int lg_pl = L.lg_ny + L.lg_nz;
             const int n = L.P << lg_pl;
             const int base = (int)x.rank * L.P << lg_pl;
+            // L2-only loads: the global level's restriction above wrote r_top
             if (P.r_top_h)
-                for (int q = threadIdx.x; q < n; q += blockDim.x) rs[q] = __half2float(P.r_top_h[base + q]);
+                for (int q = threadIdx.x; q < n; q += blockDim.x) rs[q] = St<__half>::ld_cg(P.r_top_h + base + q);
             else
-                for (int q = threadIdx.x; q < n; q += blockDim.x) rs[q] = __ldg(P.r_top + base + q);
+                for (int q = threadIdx.x; q < n; q += blockDim.x) rs[q] = __ldcg(P.r_top + base + q);
         }
     }
     x.cl.sync();
@@ -399,6 +484,13 @@ __global__ void __launch_bounds__(kClusterThreads, 1) k_cluster_vcycle(const Clu
             for (int q = threadIdx.x; q < n; q += blockDim.x) P.z_top_h[base + q] = __float2half_rn(zs[(1 << lg_pl) + q]);
         else
             for (int q = threadIdx.x; q < n; q += blockDim.x) P.z_top[base + q] = zs[(1 << lg_pl) + q];
+    }
+    if (kGlobal) {
+        x.cl.sync();
+        if (P.g.half)
+            cl_global_up<__half>(x, P.g);
+        else
+            cl_global_up<float>(x, P.g);
     }
 }
 

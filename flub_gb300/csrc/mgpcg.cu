@@ -363,9 +363,13 @@ static int choose_cluster(flub_mg *mg) {
             ClusterParams P;
             const size_t b = cluster_layout(mg, l, C, &P);
             if (b == 0 || b > (size_t)max_smem) break;
-            if (cudaFuncSetAttribute(k_cluster_vcycle, cudaFuncAttributeNonPortableClusterSizeAllowed, 1) !=
+            if (cudaFuncSetAttribute(k_cluster_vcycle<false>, cudaFuncAttributeNonPortableClusterSizeAllowed, 1) !=
                     cudaSuccess ||
-                cudaFuncSetAttribute(k_cluster_vcycle, cudaFuncAttributeMaxDynamicSharedMemorySize, max_smem) !=
+                cudaFuncSetAttribute(k_cluster_vcycle<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, max_smem) !=
+                    cudaSuccess ||
+                cudaFuncSetAttribute(k_cluster_vcycle<true>, cudaFuncAttributeNonPortableClusterSizeAllowed, 1) !=
+                    cudaSuccess ||
+                cudaFuncSetAttribute(k_cluster_vcycle<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, max_smem) !=
                     cudaSuccess) {
                 cudaGetLastError();
                 break;
@@ -375,7 +379,7 @@ static int choose_cluster(flub_mg *mg) {
             cluster_launch_config(C, b, nullptr, &cfg, attr);
             cfg.numAttrs = 1;  // the cluster dimension only
             int nclusters = 0;
-            if (cudaOccupancyMaxActiveClusters(&nclusters, k_cluster_vcycle, &cfg) != cudaSuccess || nclusters < 1) {
+            if (cudaOccupancyMaxActiveClusters(&nclusters, k_cluster_vcycle<false>, &cfg) != cudaSuccess || nclusters < 1) {
                 cudaGetLastError();
                 break;
             }
@@ -473,6 +477,48 @@ static int launch_leg(flub_mg *mg, const LaunchCtx &c, bool down, int l0, int l1
     }
     count_launches(1);
     return FLUB_OK;
+}
+
+// Opt-in (FLUB_CLUSTER_GLOBAL=1): the cluster kernel also runs the level just
+// above its distributed levels (cluster.cuh, ClusterGlobal) when that level is
+// below level 0, walks an active list with stencil words, the sweeps may skip
+// fluid-free groups, and neither the persistent legs nor tiled smoothing are
+// asked for there.  Measured on the 256^3 dam break it is slower than one
+// launch per pass on all SMs (V(2,2) solve 2.89 against 2.68 ms, the
+// reference schedule 25.5 against 23.3 ms): the 16 SMs of one cluster take
+// longer over a 64^3 level's sweep than the launch boundary costs.
+static bool use_cluster_global(const flub_mg *mg, int lt, int sk) {
+    if (!(mg->cl_start < mg->levels) || lt != mg->cl_start) return false;
+    const char *e = getenv("FLUB_CLUSTER_GLOBAL");
+    if (!(e && e[0] == '1')) return false;
+    const int G = lt - 1;
+    if (G < 1 || sk != 1 || !mg->skip_ok || mg->persist_blocks > 0) return false;
+    const Level &L = mg->lv[G];
+    if (L.D.nz % 8 != 0 || !L.act || !L.sw) return false;
+    return !(mg->tile_ok && L.n_tiles > 0);
+}
+
+static void fill_cluster_global(const flub_mg *mg, int G, bool half, ClusterGlobal *g) {
+    const Level &L = mg->lv[G], &C = mg->lv[G + 1];
+    g->on = 1;
+    g->half = half ? 1 : 0;
+    g->D = L.D;
+    g->code = L.code;
+    g->sw = L.sw;
+    g->act = L.act;
+    g->act_n = L.act_n;
+    g->r = half ? (void *)L.rh : (void *)L.r;
+    g->z = half ? (void *)L.zh : (void *)L.z;
+    g->z2 = half ? (void *)L.z2h : (void *)L.z2;
+    g->iters = level_iters(mg, G);
+    g->rscale = (half ? 0.125f : 1.0f) * mg->sched_rscale;
+    g->zc_scale = half ? 8.0f : 1.0f;
+    g->CD = C.D;
+    g->ccode = C.code;
+    g->cact = C.act;
+    g->cact_n = C.act_n;
+    g->cr = half ? (void *)C.rh : (void *)C.r;
+    g->cz = half ? (const void *)C.zh : (const void *)C.z;
 }
 
 // Whether the bottom level runs inside the one-block tail (tail.cuh), alone or
@@ -746,9 +792,13 @@ static int enqueue_vcycle(flub_mg *mg, const LaunchCtx &c, const float *r0, floa
     auto TILED_POST = [&](int l) { return mg->tile_ok && mg->lv[l].n_tiles > 0 && SK(l) == 1; };
     // levels 1 .. lg-1 in the persistent cooperative kernels, or one launch per pass
     const bool pers = use_persist(mg, lg);
+    // the level above the cluster's in the cluster kernel: the launches per
+    // pass stop one level earlier
+    const bool clg = use_cl && use_cluster_global(mg, lt, sk);
+    const int lge = clg ? lt - 1 : lg;
     // level 0 on colour-split storage (smooth_split.cuh)
-    const bool split0 = use_split(mg, lg, sk, r0, z0);
-    for (int l = 0; l < (pers ? 1 : lg); l++) {
+    const bool split0 = use_split(mg, lge, sk, r0, z0);
+    for (int l = 0; l < (pers ? 1 : lge); l++) {
         const Level &L = mg->lv[l];
         const int iters = level_iters(mg, l);
         if (l == 0 && split0) {
@@ -798,10 +848,12 @@ static int enqueue_vcycle(flub_mg *mg, const LaunchCtx &c, const float *r0, floa
         cluster_layout(mg, lt, mg->cl_size, &P);
         P.r_top = R(lt);
         P.z_top = ZF(lt);
+        if (clg) fill_cluster_global(mg, lt - 1, false, &P.g);
         cudaLaunchConfig_t cfg;
         cudaLaunchAttribute attr[2];
         cluster_launch_config(mg->cl_size, mg->cl_smem, c.s, &cfg, attr);
-        const cudaError_t e = cudaLaunchKernelEx(&cfg, k_cluster_vcycle, (const ClusterParams)P, c.kc);
+        const cudaError_t e = P.g.on ? cudaLaunchKernelEx(&cfg, k_cluster_vcycle<true>, (const ClusterParams)P, c.kc)
+                                     : cudaLaunchKernelEx(&cfg, k_cluster_vcycle<false>, (const ClusterParams)P, c.kc);
         if (e != cudaSuccess) {
             set_last_error("cluster V-cycle launch: %s", cudaGetErrorString(e));
             cudaGetLastError();
@@ -827,7 +879,7 @@ static int enqueue_vcycle(flub_mg *mg, const LaunchCtx &c, const float *r0, floa
         }
     }
     if (pers) FLUB_TRY(launch_leg<float>(mg, c, false, 1, lg));
-    for (int l = pers ? 0 : lg - 1; l >= 0; l--) {
+    for (int l = pers ? 0 : lge - 1; l >= 0; l--) {
         const Level &L = mg->lv[l];
         const int iters = level_iters(mg, l);
         if (l == 0 && split0) {
@@ -866,7 +918,7 @@ static int enqueue_vcycle(flub_mg *mg, const LaunchCtx &c, const float *r0, floa
 // Cluster or one-block kernel for the coarse levels from lt down, with FP16
 // (mixed precision) or FP32 top-level residual/correction.
 static int launch_coarse(flub_mg *mg, const LaunchCtx &c, int lt, const float *r_top, float *z_top,
-                         const __half *r_top_h, __half *z_top_h) {
+                         const __half *r_top_h, __half *z_top_h, bool global_half = false) {
     if (mg->cl_start < mg->levels) {
         ClusterParams P = {};
         cluster_layout(mg, lt, mg->cl_size, &P);
@@ -874,10 +926,12 @@ static int launch_coarse(flub_mg *mg, const LaunchCtx &c, int lt, const float *r
         P.z_top = z_top;
         P.r_top_h = r_top_h;
         P.z_top_h = z_top_h;
+        if (global_half) fill_cluster_global(mg, lt - 1, true, &P.g);
         cudaLaunchConfig_t cfg;
         cudaLaunchAttribute attr[2];
         cluster_launch_config(mg->cl_size, mg->cl_smem, c.s, &cfg, attr);
-        const cudaError_t e = cudaLaunchKernelEx(&cfg, k_cluster_vcycle, (const ClusterParams)P, c.kc);
+        const cudaError_t e = P.g.on ? cudaLaunchKernelEx(&cfg, k_cluster_vcycle<true>, (const ClusterParams)P, c.kc)
+                                     : cudaLaunchKernelEx(&cfg, k_cluster_vcycle<false>, (const ClusterParams)P, c.kc);
         if (e != cudaSuccess) {
             set_last_error("cluster V-cycle launch: %s", cudaGetErrorString(e));
             cudaGetLastError();
@@ -905,8 +959,10 @@ static int enqueue_vcycle_mixed(flub_mg *mg, const LaunchCtx &c, float *z0, bool
     const int sk0 = z0_clean ? sk : 0;
     const int lg = lt < Lm - 1 ? lt : Lm - 1;
     const bool pers = use_persist(mg, lg);
-    const bool split0 = use_split(mg, lg, sk0, mg->lv[0].rh, z0);
-    for (int l = 0; l < (pers ? 1 : lg); l++) {
+    const bool clg = use_cl && use_cluster_global(mg, lt, sk);
+    const int lge = clg ? lt - 1 : lg;
+    const bool split0 = use_split(mg, lge, sk0, mg->lv[0].rh, z0);
+    for (int l = 0; l < (pers ? 1 : lge); l++) {
         const Level &L = mg->lv[l];
         const int iters = level_iters(mg, l);
         if (l == 0 && split0) {
@@ -948,7 +1004,7 @@ static int enqueue_vcycle_mixed(flub_mg *mg, const LaunchCtx &c, float *z0, bool
         if (lt == 0)
             FLUB_TRY(launch_coarse(mg, c, 0, nullptr, z0, mg->lv[0].rh, nullptr));
         else
-            FLUB_TRY(launch_coarse(mg, c, lt, nullptr, nullptr, mg->lv[lt].rh, mg->lv[lt].zh));
+            FLUB_TRY(launch_coarse(mg, c, lt, nullptr, nullptr, mg->lv[lt].rh, mg->lv[lt].zh, clg));
     } else {
         const int b = Lm - 1;
         const Level &L = mg->lv[b];
@@ -968,7 +1024,7 @@ static int enqueue_vcycle_mixed(flub_mg *mg, const LaunchCtx &c, float *z0, bool
         }
     }
     if (pers) FLUB_TRY(launch_leg<__half>(mg, c, false, 1, lg));
-    for (int l = pers ? 0 : lg - 1; l >= 0; l--) {
+    for (int l = pers ? 0 : lge - 1; l >= 0; l--) {
         const Level &L = mg->lv[l];
         const __half *zc = mg->lv[l + 1].zh;
         const int iters = level_iters(mg, l);

@@ -49,7 +49,7 @@ __device__ __forceinline__ void residual_row8(const TR *__restrict__ r, const TZ
     const int sj = D.nz, si = D.ny * D.nz;
     const int c0 = g << 3;
     float rv[8];
-    if (kNC) St<TR>::ld8_ro(r + c0, rv); else St<TR>::ld8(r + c0, rv);
+    if (kNC) St<TR>::ld8_ro(r + c0, rv); else St<TR>::ld8_cg(r + c0, rv);
     const uint4 wd = load_words8(sw, code, D, i, j, k0, c0);
     if (!words_have_fluid(wd)) {
 #pragma unroll
@@ -60,9 +60,9 @@ __device__ __forceinline__ void residual_row8(const TR *__restrict__ r, const TZ
     const bool hkp = k0 + 8 < D.nz, hkm = k0 > 0;
     float xc[8], xip[8], xim[8], xjp[8], xjm[8];
     auto ld8 = [&](const TZ *p, float o[8]) {
-        if (kNC) St<TZ>::ld8_ro(p, o); else St<TZ>::ld8(p, o);
+        if (kNC) St<TZ>::ld8_ro(p, o); else St<TZ>::ld8_cg(p, o);
     };
-    auto ld1 = [&](const TZ *p) { return kNC ? St<TZ>::ld_ro(p) : St<TZ>::ld(p); };
+    auto ld1 = [&](const TZ *p) { return kNC ? St<TZ>::ld_ro(p) : St<TZ>::ld_cg(p); };
 #pragma unroll
     for (int m = 0; m < 8; m++) xip[m] = xim[m] = xjp[m] = xjm[m] = 0.0f;
     float xkm = 0.0f, xkp = 0.0f;

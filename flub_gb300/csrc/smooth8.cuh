@@ -124,7 +124,7 @@ __device__ __forceinline__ void add_coarse_row8(Row8 &o, const TC *__restrict__ 
 
 template <bool kNC, typename TC>
 __device__ __forceinline__ float coarse_at(const TC *__restrict__ p, float scale) {
-    return __fmul_rn(kNC ? St<TC>::ld_ro(p) : St<TC>::ld(p), scale);
+    return __fmul_rn(kNC ? St<TC>::ld_ro(p) : St<TC>::ld_cg(p), scale);
 }
 
 // One cell's red-black update (multigrid/mgpcg.py:72-86 in the reference's
@@ -167,9 +167,10 @@ __device__ __forceinline__ float smooth_cell(uint32_t w, float xc, float xip, fl
 // well: 5 blocks per SM (51 registers) instead of 6 (40) keep it free of
 // spills.
 // kNC: r and zc may be read through the read-only (non-coherent) path, i.e.
-// nothing writes them while the kernel runs; false inside the persistent
-// V-cycle kernels (persist.cuh), where other blocks wrote them earlier in the
-// same launch.  bid / nblk: this block's index and the number of blocks that
+// nothing writes them while the kernel runs; false inside the persistent and
+// cluster V-cycle kernels (persist.cuh, cluster.cuh), where other blocks wrote
+// them (and z) earlier in the same launch: then r, zc and z are read with
+// L2-only loads.  bid / nblk: this block's index and the number of blocks that
 // share the grid-stride loop.
 // kc != NULL: called at the start of a kernel launched with programmatic
 // dependent launch: the list reads come first, then pdl_wait(kc).
@@ -217,15 +218,22 @@ __device__ __forceinline__ void smooth8_pass(TO *zout, const TI *zin, const TC *
                 const uint4 w8 = words8_from_codes(code, D, i, j, k0, c0);
                 wd = h ? make_uint2(w8.z, w8.w) : make_uint2(w8.x, w8.y);
             }
-            if (kNC) St<TR>::ld4_ro(r + ch, rr); else St<TR>::ld4(r + ch, rr);
+            if (kNC) St<TR>::ld4_ro(r + ch, rr); else St<TR>::ld4_cg(r + ch, rr);
             if (!kFromZero) {
-                St<TI>::ld4(zin + ch, zc0);
-                if (hip) St<TI>::ld4(zin + ch + si, zip);
-                if (him) St<TI>::ld4(zin + ch - si, zim);
-                if (hjp) St<TI>::ld4(zin + ch + sj, zjp);
-                if (hjm) St<TI>::ld4(zin + ch - sj, zjm);
-                if (h == 0 && hkm) zout_k = St<TI>::ld(zin + c0 - 1);
-                if (h == 1 && hkp) zout_k = St<TI>::ld(zin + c0 + 8);
+                // z: plain loads (rows of the other colour do not change during the
+                // launch), or L2-only ones where other blocks of the same launch
+                // wrote it in an earlier pass (kNC false)
+                auto ldz4 = [&](const TI *q, float o[4]) {
+                    if (kNC) St<TI>::ld4(q, o); else St<TI>::ld4_cg(q, o);
+                };
+                auto ldz = [&](const TI *q) { return kNC ? St<TI>::ld(q) : St<TI>::ld_cg(q); };
+                ldz4(zin + ch, zc0);
+                if (hip) ldz4(zin + ch + si, zip);
+                if (him) ldz4(zin + ch - si, zim);
+                if (hjp) ldz4(zin + ch + sj, zjp);
+                if (hjm) ldz4(zin + ch - sj, zjm);
+                if (h == 0 && hkm) zout_k = ldz(zin + c0 - 1);
+                if (h == 1 && hkp) zout_k = ldz(zin + c0 + 8);
                 if (kProlong) {
                     const int cy = D.ny >> 1, cz = D.nz >> 1;
                     const int ci = i >> 1, cj = j >> 1, ck = (k0 >> 1) + 2 * h;
@@ -233,7 +241,7 @@ __device__ __forceinline__ void smooth8_pass(TO *zout, const TI *zin, const TC *
                     float cv[2];
 #define FLUB_ADD_COARSE(row, p)                                                         \
     {                                                                                   \
-        if (kNC) St<TC>::ld2_ro((p), cv); else St<TC>::ld2((p), cv);                    \
+        if (kNC) St<TC>::ld2_ro((p), cv); else St<TC>::ld2_cg((p), cv);                 \
         _Pragma("unroll") for (int mm = 0; mm < 4; mm++)                                \
             row[mm] = __fadd_rn(row[mm], __fmul_rn(cv[mm >> 1], zc_scale));             \
     }

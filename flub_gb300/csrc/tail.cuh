@@ -257,8 +257,9 @@ __device__ __forceinline__ void tail_half64(double *z, const TailCache &tc, cons
 }
 
 // The bottom's 2 x nbottom red-black iterations in FP64, starting from z = 0,
-// then z rounded to FP32 into zf.
-__device__ __forceinline__ void tail_bottom64(double *zd, float *zf, const TailCache &tc, const Dims D, int nbottom) {
+// then z rounded to FP32 into zf.  Not inlined: its FP64 registers would
+// otherwise count against the whole tail / cluster kernel.
+__device__ __noinline__ void tail_bottom64(double *zd, float *zf, const TailCache &tc, const Dims D, int nbottom) {
     const int n = D.nx * D.ny * D.nz;
     for (int q = threadIdx.x; q < n; q += blockDim.x) zd[q] = 0.0;
     __syncthreads();

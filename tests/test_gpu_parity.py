@@ -616,6 +616,37 @@ def test_mixed_handle_defaults_to_fp64_bottom():
         mgm.set_bottom_precision(16)
 
 
+@pytest.mark.parametrize("name", ["dam128", "rand128"])
+@pytest.mark.parametrize("precision", ["fp32", "mixed"])
+def test_cluster_global_level_bit_exact(name, precision, monkeypatch):
+    """The level above the cluster's distributed levels (64^3 at 128^3) run in
+    the cluster kernel from global memory (opt-in, FLUB_CLUSTER_GLOBAL=1)
+    against one launch per pass (the default): the same V-cycle and solve, bit
+    for bit, with the reference schedule and the light one; FP32 also against
+    the oracle."""
+    scene = TILE_SCENES[name]()
+    out = []
+    for on in ("1", "0"):
+        monkeypatch.setenv("FLUB_CLUSTER_GLOBAL", on)
+        tag_o, r0, _ = _setup(scene)
+        mg = MGPCG(3, scene.shape, scene.levels, float, precision=precision)
+        mg.set_tags(dev(tag_o))
+        z = host(mg.apply_preconditioner(dev(r0)))
+        mg.set_schedule("v22")
+        z22 = host(mg.apply_preconditioner(dev(r0)))
+        mg.init(dev(r0), 1.0)
+        mg.mask_interior()
+        info = mg.solve(200, 1e-12, 0.0, 1e-12, smoother="phases")
+        out.append((z, z22, info["iterations"], host(mg.x).copy()))
+    assert np.array_equal(out[0][0], out[1][0]) and np.array_equal(out[0][1], out[1][1])
+    assert out[0][2] == out[1][2] and np.array_equal(out[0][3], out[1][3])
+    if precision == "fp32":
+        tags = O.tag_levels(tag_o, scene.levels)
+        assert np.array_equal(out[0][0], O.vcycle(r0, tags, np.float32))
+        with O.schedule(2, 4, 0.5):
+            assert np.array_equal(out[0][1], O.vcycle(r0, tags, np.float32))
+
+
 def test_schedule_rejects_bad_values():
     mg = MGPCG(3, (32, 32, 32), 3, float)
     for bad in [(0, 8, 0.5), (2, 0, 0.5), (2, 8, 0.0), (2, 8, 2.0), (65, 8, 0.5)]:
