@@ -61,8 +61,23 @@ __device__ __forceinline__ uint32_t sw_ns(uint32_t w) { return (w | (w >> 1)) & 
 // operation order: per neighbour (i+, i-, j+, j-, k+, k-) 0 when solid, else
 // (x_n - x_c) with x_n = 0 for air, summed in pairs per axis.  Bit tests on
 // the word replace the per-neighbour code compares.
+// Stencil word of a fluid cell whose six neighbours are all fluid (code 2 in
+// all seven 2-bit fields): most cells of a water body.
+constexpr uint32_t kInteriorWord = 0x2AAAu;
+
+// sw_nbsum for an interior word: every neighbour counts and enters with its
+// value, so the bit tests and selects drop out; the FP32 operations and their
+// order are sw_nbsum's (pair sums per axis).
+__device__ __forceinline__ float interior_nbsum(float xc, float xip, float xim, float xjp, float xjm, float xkp,
+                                                float xkm) {
+    float ret = __fadd_rn(0.0f, __fadd_rn(__fsub_rn(xip, xc), __fsub_rn(xim, xc)));
+    ret = __fadd_rn(ret, __fadd_rn(__fsub_rn(xjp, xc), __fsub_rn(xjm, xc)));
+    return __fadd_rn(ret, __fadd_rn(__fsub_rn(xkp, xc), __fsub_rn(xkm, xc)));
+}
+
 __device__ __forceinline__ float sw_nbsum(uint32_t w, float xc, float xip, float xim, float xjp, float xjm,
                                           float xkp, float xkm) {
+    if (w == kInteriorWord) return interior_nbsum(xc, xip, xim, xjp, xjm, xkp, xkm);
     const uint32_t ns = sw_ns(w);
     auto term = [&](int q, float xn) {
         const float v = (w & (2u << (2 * q))) ? xn : 0.0f;
@@ -135,6 +150,10 @@ __device__ __forceinline__ float coarse_at(const TC *__restrict__ p, float scale
 template <bool kFromZero>
 __device__ __forceinline__ float smooth_cell(uint32_t w, float xc, float xip, float xim, float xjp, float xjm,
                                              float xkp, float xkm, float r) {
+    if (w == kInteriorWord)  // d = 6
+        return kFromZero ? __fdiv_rn(r, 6.0f)
+                         : __fadd_rn(xc, __fdiv_rn(__fadd_rn(r, interior_nbsum(xc, xip, xim, xjp, xjm, xkp, xkm)),
+                                                   6.0f));
     if (sw_code(w, 0) != kCodeFluid) return 0.0f;
     const int d = __popc(sw_ns(w));
     if (d == 0) return 0.0f;

@@ -66,15 +66,10 @@ struct SplitArgs {
 // both halves of its 8-byte word load equal this.
 constexpr uint32_t kInteriorWord2 = 0x2AAA2AAAu;
 
-// smooth_cell for an interior word: every neighbour counts (d = 6) and enters
-// with its value, so the bit tests and selects drop out; the FP32 operations
-// and their order are smooth_cell's (sw_nbsum's pair sums per axis).
+// smooth_cell for an interior word (d = 6), without the per-cell word test.
 __device__ __forceinline__ float smooth_interior(float xc, float xip, float xim, float xjp, float xjm, float xkp,
                                                  float xkm, float r) {
-    float ret = __fadd_rn(0.0f, __fadd_rn(__fsub_rn(xip, xc), __fsub_rn(xim, xc)));
-    ret = __fadd_rn(ret, __fadd_rn(__fsub_rn(xjp, xc), __fsub_rn(xjm, xc)));
-    ret = __fadd_rn(ret, __fadd_rn(__fsub_rn(xkp, xc), __fsub_rn(xkm, xc)));
-    return __fadd_rn(xc, __fdiv_rn(__fadd_rn(r, ret), 6.0f));
+    return __fadd_rn(xc, __fdiv_rn(__fadd_rn(r, interior_nbsum(xc, xip, xim, xjp, xjm, xkp, xkm)), 6.0f));
 }
 
 __device__ __forceinline__ uint32_t word4_at(uint2 w, int m) {
