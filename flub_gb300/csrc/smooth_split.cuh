@@ -81,8 +81,11 @@ __device__ __forceinline__ uint32_t word4_at(uint2 w, int m) {
 // neighbour bits.
 __device__ __forceinline__ uint32_t word_kcode(uint32_t w, bool kp) { return sw_code(w, kp ? 5 : 6); }
 
+// 5 resident blocks of 256 threads per SM for the lean modes (48 registers),
+// 4 for the prolongation and the natural-order output, which hold more.
 template <int kMode, typename TRN, typename TR, typename TZI, typename TZ, typename TC>
-__global__ void __launch_bounds__(256, 4) k_smooth_split(const SplitArgs A, int phase, unsigned long long *kc) {
+__global__ void __launch_bounds__(256, (kMode == kProlong || kMode == kLast) ? 4 : 5)
+    k_smooth_split(const SplitArgs A, int phase, unsigned long long *kc) {
     pdl_open();
     const Dims D = A.D;
     const int hz = D.nz >> 1;             // split row length
