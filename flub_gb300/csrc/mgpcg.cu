@@ -628,8 +628,9 @@ static int sweep(const LaunchCtx &c, const Level &L, int phase, int mode, int sk
 // One level-0 half-sweep on colour-split storage (smooth_split.cuh).
 template <int kMode, typename TRN, typename TR, typename TZI, typename TZ, typename TC>
 static int split_sweep(const LaunchCtx &c, const Level &L, int phase, const TRN *rn, TR *rs, const TZI *zin, TZ *z,
-                       const TC *zc, float zc_scale, float *zn) {
+                       const TC *zc, float zc_scale, float *zn, const SplitArgs *dot = nullptr) {
     SplitArgs A = {};
+    if (dot) A = *dot;  // kLast with z.r folded in: dot, rdot, pinit, st, partials
     A.D = L.D;
     A.act = L.act;
     A.act_n = L.act_n;
@@ -776,7 +777,12 @@ static int tile_side(flub_mg *mg, const LaunchCtx &c, int l, bool post, int iter
 
 // multigrid/mgpcg.py:296-349 apply_preconditioner; level 0 uses (r0, z0).
 // z0_clean: z0 holds 0 on every non-fluid cell (true for the handle's own z).
-static int enqueue_vcycle(flub_mg *mg, const LaunchCtx &c, const float *r0, float *z0, bool z0_clean) {
+// dot_mode 1 / 2: the caller's next step is z.r (the prologue's p = z / the
+// iteration's beta); when the last level-0 half-sweep can fold it in, it does
+// and *dot_fused is set.
+static int enqueue_vcycle(flub_mg *mg, const LaunchCtx &c, const float *r0, float *z0, bool z0_clean,
+                          int dot_mode = 0, bool *dot_fused = nullptr) {
+    if (dot_fused) *dot_fused = false;
     const bool use_cl = mg->cl_start < mg->levels;
     const int Lm = mg->levels, lt = use_cl ? mg->cl_start : mg->tail_start;
     const int sk = mg->skip_ok ? 1 : 0;
@@ -893,9 +899,19 @@ static int enqueue_vcycle(flub_mg *mg, const LaunchCtx &c, const float *r0, floa
                 else
                     FLUB_TRY((split_sweep<kInPlace, float, float, float, float, float>(
                         c, L, 1, nullptr, L.rs, nullptr, L.zs, nullptr, 1.0f, nullptr)));
-                if (it + 1 == iters)
-                    FLUB_TRY((split_sweep<kLast, float, float, float, float, float>(c, L, 0, nullptr, L.rs, nullptr,
-                                                                                  L.zs, nullptr, 1.0f, z0)));
+                if (it + 1 == iters) {
+                    SplitArgs D = {};
+                    if (dot_mode && dot_fused) {
+                        D.dot = dot_mode;
+                        D.rdot = r0;
+                        D.pinit = mg->p;
+                        D.st = mg->st;
+                        D.partials = mg->partials;
+                        *dot_fused = true;
+                    }
+                    FLUB_TRY((split_sweep<kLast, float, float, float, float, float>(
+                        c, L, 0, nullptr, L.rs, nullptr, L.zs, nullptr, 1.0f, z0, D.dot ? &D : nullptr)));
+                }
                 else
                     FLUB_TRY((split_sweep<kInPlace, float, float, float, float, float>(
                         c, L, 0, nullptr, L.rs, nullptr, L.zs, nullptr, 1.0f, nullptr)));
@@ -1148,7 +1164,9 @@ static int enqueue_prologue(flub_mg *mg, const LaunchCtx &c, int smoother) {
         FLUB_TRY(launch_pdl(k_residual_x0, dim3(blocks_for(mg->n, 256)), dim3(256), 0, c.s, mg->st, L0.r, mg->x,
                             L0.code, L0.D, c.kc));
     if (smoother == FLUB_SMOOTHER_FRACTION) FLUB_TRY(enqueue_mean_removal(mg, c, 2));
-    FLUB_TRY(enqueue_vcycle(mg, c, L0.r, L0.z, true));
+    bool fused = false;
+    FLUB_TRY(enqueue_vcycle(mg, c, L0.r, L0.z, true, 1, &fused));
+    if (fused) return FLUB_OK;  // p = z and z.r in the last level-0 half-sweep
     if (v8)
         return launch_pdl(k8_dot_zr<true, false>, dim3(bg), dim3(kRedThreads), 0, c.s, mg->st, L0.z, L0.r, mg->p, L0.code,
                           mg->n, mg->partials, (const int *)L0.act, (const int *)L0.act_n, c.kc);
@@ -1192,12 +1210,14 @@ static int enqueue_second_half(flub_mg *mg, const LaunchCtx &c) {
     if (mg->precision == FLUB_PRECISION_MIXED) return enqueue_second_half_mixed(mg, c);
     const unsigned b = red_blocks(mg->n);
     const Level &L0 = mg->lv[0];
-    FLUB_TRY(enqueue_vcycle(mg, c, L0.r, L0.z, true));
+    bool fused = false;
+    FLUB_TRY(enqueue_vcycle(mg, c, L0.r, L0.z, true, 2, &fused));
     if ((L0.D.nz % 8) == 0) {
         const unsigned bg = red_blocks(mg->n / 8 + 1);
-        FLUB_TRY(launch_pdl(k8_dot_zr<false>, dim3(bg), dim3(kRedThreads), 0, c.s, mg->st, L0.z, L0.r,
-                            (float *)nullptr, L0.code, mg->n, mg->partials, (const int *)L0.act,
-                            (const int *)L0.act_n, c.kc));
+        if (!fused)  // else beta came with the last level-0 half-sweep
+            FLUB_TRY(launch_pdl(k8_dot_zr<false>, dim3(bg), dim3(kRedThreads), 0, c.s, mg->st, L0.z, L0.r,
+                                (float *)nullptr, L0.code, mg->n, mg->partials, (const int *)L0.act,
+                                (const int *)L0.act_n, c.kc));
         return launch_pdl(k8_update_xp<false>, dim3(blocks_for(mg->n / 8, 256, kNumSMs * 8)), dim3(256), 0, c.s,
                           mg->st, mg->x, mg->p, L0.z, L0.code, mg->n, (const int *)L0.act, (const int *)L0.act_n,
                           c.kc);

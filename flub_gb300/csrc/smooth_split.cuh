@@ -59,6 +59,15 @@ struct SplitArgs {
     const void *zc;             // kProlong: next level's correction, natural order (TC)
     float zc_scale;
     float *zn;                  // kLast: natural-order output
+    // kLast, FP32 solve: z.r of the CG step folded in (mgpcg.py:401, 451):
+    // dot 1 -- zr_old = z.r and p = z (the solve's prologue), dot 2 -- beta =
+    // z.r / zr_old, zr_old = z.r (each iteration); 0 -- none.  rdot is the
+    // natural-order r; the per-group sums are k8_dot_zr's.
+    int dot;
+    const float *rdot;
+    float *pinit;
+    MgState *st;
+    double *partials;
 };
 
 // Stencil word of a fluid cell whose six neighbours are all fluid (code 2 in
@@ -108,6 +117,7 @@ __global__ void __launch_bounds__(256, (kMode == kProlong || kMode == kLast) ? 4
     }
     pdl_wait(kc);
     bool first = true;
+    double zr = 0.0;  // kLast with A.dot: this thread's part of z.r
     for (; t < total; t += stride) {
         const int g = g_next;
         const int tn = t + stride;
@@ -244,9 +254,31 @@ __global__ void __launch_bounds__(256, (kMode == kProlong || kMode == kLast) ? 4
                 o8[2 * m + 1 - q] = vo[m];
             }
             St<float>::st8(A.zn + ((size_t)g << 3), o8);
+            if (A.dot) {
+                float rv[8];
+                St<float>::ld8_ro(A.rdot + ((size_t)g << 3), rv);
+                zr += dot8_ff(o8, rv);
+                if (A.dot == 1) St<float>::st8(A.pinit + ((size_t)g << 3), o8);
+            }
         } else {
             St<TZ>::st4(z + uoff + h, out);
             if (kMode == kProlong) St<TZ>::st4(z + voff + h, vo);
+        }
+    }
+    if (kMode == kLast && A.dot) {
+        // the grid's z.r in FP64 (deterministic two-level reduction) and the
+        // CG scalars, as k8_dot_zr sets them
+        __shared__ double red[32];
+        double tot;
+        if (finish_partials(zr, A.partials, &A.st->ticket, red, &tot) && threadIdx.x == 0) {
+            if (A.dot == 1) {
+                A.st->zr_old = tot;
+            } else {
+                const double beta = tot / (A.st->zr_old + A.st->eps);
+                A.st->beta = beta;
+                A.st->zr_old = tot;
+                if (!isfinite(beta)) A.st->status = FLUB_ERR_BREAKDOWN;
+            }
         }
     }
 }
