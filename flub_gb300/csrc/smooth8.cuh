@@ -65,6 +65,22 @@ __device__ __forceinline__ uint32_t sw_ns(uint32_t w) { return (w | (w >> 1)) & 
 // all seven 2-bit fields): most cells of a water body.
 constexpr uint32_t kInteriorWord = 0x2AAAu;
 
+// a / 6 rounded to nearest, as __fdiv_rn(a, 6.0f), with Markstein's FMA
+// correction of the product by the rounded reciprocal (P. Markstein, IBM J.
+// Res. Dev. 34(1), 1990; q0 = a y, r = a - 6 q0 exactly, q = q0 + r y): three
+// FP32 operations instead of a division.  tests/test_div6_exhaustive.py checks
+// it bit for bit against IEEE division for every float32 with |a| in
+// [2^-100, 2^100]; other inputs (zeros, tiny, huge, inf, NaN) take __fdiv_rn.
+__device__ __forceinline__ float div6_rn(float a) {
+    constexpr float y = 0x1.555556p-3f;  // 1/6 rounded to nearest
+    const float m = fabsf(a);
+    if (m >= 0x1p-100f && m <= 0x1p100f) {
+        const float q0 = __fmul_rn(a, y);
+        return __fmaf_rn(__fmaf_rn(-q0, 6.0f, a), y, q0);
+    }
+    return __fdiv_rn(a, 6.0f);
+}
+
 // sw_nbsum for an interior word: every neighbour counts and enters with its
 // value, so the bit tests and selects drop out; the FP32 operations and their
 // order are sw_nbsum's (pair sums per axis).
@@ -151,9 +167,8 @@ template <bool kFromZero>
 __device__ __forceinline__ float smooth_cell(uint32_t w, float xc, float xip, float xim, float xjp, float xjm,
                                              float xkp, float xkm, float r) {
     if (w == kInteriorWord)  // d = 6
-        return kFromZero ? __fdiv_rn(r, 6.0f)
-                         : __fadd_rn(xc, __fdiv_rn(__fadd_rn(r, interior_nbsum(xc, xip, xim, xjp, xjm, xkp, xkm)),
-                                                   6.0f));
+        return kFromZero ? div6_rn(r)
+                         : __fadd_rn(xc, div6_rn(__fadd_rn(r, interior_nbsum(xc, xip, xim, xjp, xjm, xkp, xkm))));
     if (sw_code(w, 0) != kCodeFluid) return 0.0f;
     const int d = __popc(sw_ns(w));
     if (d == 0) return 0.0f;

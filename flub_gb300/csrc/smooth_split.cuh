@@ -78,7 +78,7 @@ constexpr uint32_t kInteriorWord2 = 0x2AAA2AAAu;
 // smooth_cell for an interior word (d = 6), without the per-cell word test.
 __device__ __forceinline__ float smooth_interior(float xc, float xip, float xim, float xjp, float xjm, float xkp,
                                                  float xkm, float r) {
-    return __fadd_rn(xc, __fdiv_rn(__fadd_rn(r, interior_nbsum(xc, xip, xim, xjp, xjm, xkp, xkm)), 6.0f));
+    return __fadd_rn(xc, div6_rn(__fadd_rn(r, interior_nbsum(xc, xip, xim, xjp, xjm, xkp, xkm))));
 }
 
 __device__ __forceinline__ uint32_t word4_at(uint2 w, int m) {
