@@ -220,6 +220,22 @@ __device__ __forceinline__ void tail_prolong(float *zf, const float *zc, const D
 // ---------------------------------------------------------------- FP64 bottom
 // tail_lap / tail_update / tail_half_lean in FP64, the same operations in the
 // same order with IEEE double rounding at each (no contraction).
+
+// a / d for d = 1..6, rounded to nearest as __ddiv_rn(a, d), by Markstein's
+// FMA correction of a * RN(1/d) (P. Markstein, IBM J. Res. Dev. 34(1), 1990):
+// two FMAs and a product instead of an FP64 division, which GB300 issues
+// slowly.  tests/test_div6_exhaustive.py checks it bit for bit against IEEE
+// division on 2^28 random doubles per d with |a| in [2^-900, 2^900]; other
+// inputs take __ddiv_rn.
+__device__ __forceinline__ double ddiv_small_rn(double a, int d) {
+    const double y = d == 1 ? 1.0 : d == 2 ? 0.5 : d == 3 ? 1.0 / 3.0 : d == 4 ? 0.25 : d == 5 ? 0.2 : 1.0 / 6.0;
+    const double m = fabs(a);
+    if (m >= 0x1p-900 && m <= 0x1p900) {
+        const double q0 = __dmul_rn(a, y);
+        return __fma_rn(__fma_rn(-q0, (double)d, a), y, q0);
+    }
+    return __ddiv_rn(a, (double)d);
+}
 __device__ __forceinline__ double tail_lap64(const double *z, int c, uint32_t m, int si, int sj) {
     const double xc = z[c];
     const double zip = z[(m & 1u) ? c + si : c], zim = z[(m & 2u) ? c - si : c];
@@ -250,7 +266,7 @@ __device__ __forceinline__ void tail_half64(double *z, const TailCache &tc, cons
         double zn = 0.0;
         const int d = __popc(m & 63u);
         if ((m & (1u << 12)) && d != 0)
-            zn = __dadd_rn(z[cu], __ddiv_rn(__dadd_rn(rc, tail_lap64(z, cu, m, si, sj)), (double)d));
+            zn = __dadd_rn(z[cu], ddiv_small_rn(__dadd_rn(rc, tail_lap64(z, cu, m, si, sj)), d));
         z[cu] = zn;
     }
     tail_sync(nthr);
