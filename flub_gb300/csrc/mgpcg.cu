@@ -968,7 +968,9 @@ static int launch_coarse(flub_mg *mg, const LaunchCtx &c, int lt, const float *r
 // Mixed-precision V-cycle: the levels in global memory are FP16 at scale 8^-l
 // (mixed.cuh); the level-0 residual is read from its FP16 copy lv[0].rh, the
 // result z0 is FP32.  Same schedule as enqueue_vcycle.
-static int enqueue_vcycle_mixed(flub_mg *mg, const LaunchCtx &c, float *z0, bool z0_clean) {
+static int enqueue_vcycle_mixed(flub_mg *mg, const LaunchCtx &c, float *z0, bool z0_clean, int dot_mode = 0,
+                                bool *dot_fused = nullptr) {
+    if (dot_fused) *dot_fused = false;
     const bool use_cl = mg->cl_start < mg->levels;
     const int Lm = mg->levels, lt = use_cl ? mg->cl_start : mg->tail_start;
     const int sk = mg->skip_ok ? 1 : 0;
@@ -1054,9 +1056,22 @@ static int enqueue_vcycle_mixed(flub_mg *mg, const LaunchCtx &c, float *z0, bool
                 else
                     FLUB_TRY((split_sweep<kInPlace, H, H, float, float, float>(c, L, 1, nullptr, L.rsh, nullptr,
                                                                                L.zs, nullptr, 1.0f, nullptr)));
-                if (it + 1 == iters)
+                if (it + 1 == iters) {
+                    SplitArgs D = {};
+                    if (dot_mode && dot_fused) {
+                        D.dot = dot_mode;  // 1: p = zscale z and zr_old, 3: flexible beta
+                        D.zscaled = 1;
+                        D.rdot = mg->lv[0].r;
+                        D.rold = mg->r_old;
+                        D.pinit = mg->p;
+                        D.st = mg->st;
+                        D.partials = mg->partials;
+                        *dot_fused = true;
+                    }
                     FLUB_TRY((split_sweep<kLast, H, H, float, float, float>(c, L, 0, nullptr, L.rsh, nullptr, L.zs,
-                                                                            nullptr, 1.0f, z0)));
+                                                                            nullptr, 1.0f, z0,
+                                                                            D.dot ? &D : nullptr)));
+                }
                 else
                     FLUB_TRY((split_sweep<kInPlace, H, H, float, float, float>(c, L, 0, nullptr, L.rsh, nullptr,
                                                                                L.zs, nullptr, 1.0f, nullptr)));
@@ -1108,7 +1123,9 @@ static int enqueue_prologue_mixed(flub_mg *mg, const LaunchCtx &c, int smoother)
     if (smoother == FLUB_SMOOTHER_FRACTION) FLUB_TRY(enqueue_mean_removal(mg, c, 2));
     FLUB_TRY(launch_pdl(k8_to_half, dim3(blocks_for(mg->n / 8, 256)), dim3(256), 0, c.s, mg->st, (const float *)L0.r, L0.rh,
                         mg->n, c.kc));
-    FLUB_TRY(enqueue_vcycle_mixed(mg, c, L0.z, true));
+    bool fused = false;
+    FLUB_TRY(enqueue_vcycle_mixed(mg, c, L0.z, true, 1, &fused));
+    if (fused) return FLUB_OK;  // p = zscale z and z.r in the last level-0 half-sweep
     return launch_pdl(k8_dot_zr<true, true>, dim3(bg), dim3(kRedThreads), 0, c.s, mg->st, L0.z, L0.r, mg->p, L0.code,
                       mg->n, mg->partials, (const int *)L0.act, (const int *)L0.act_n, c.kc);
 }
@@ -1136,9 +1153,11 @@ static int enqueue_first_half_mixed(flub_mg *mg, const LaunchCtx &c, int smoothe
 static int enqueue_second_half_mixed(flub_mg *mg, const LaunchCtx &c) {
     const Level &L0 = mg->lv[0];
     const unsigned bg = red_blocks(mg->n / 8 + 1);
-    FLUB_TRY(enqueue_vcycle_mixed(mg, c, L0.z, true));
-    FLUB_TRY(launch_pdl(k8_dot_zr_flex, dim3(bg), dim3(kRedThreads), 0, c.s, mg->st, L0.z, L0.r, mg->r_old, L0.code,
-                        mg->n, mg->partials, (const int *)L0.act, (const int *)L0.act_n, c.kc));
+    bool fused = false;
+    FLUB_TRY(enqueue_vcycle_mixed(mg, c, L0.z, true, 3, &fused));
+    if (!fused)  // else the flexible beta came with the last level-0 half-sweep
+        FLUB_TRY(launch_pdl(k8_dot_zr_flex, dim3(bg), dim3(kRedThreads), 0, c.s, mg->st, L0.z, L0.r, mg->r_old,
+                            L0.code, mg->n, mg->partials, (const int *)L0.act, (const int *)L0.act_n, c.kc));
     return launch_pdl(k8_update_xp<true>, dim3(blocks_for(mg->n / 8, 256, kNumSMs * 8)), dim3(256), 0, c.s, mg->st,
                       mg->x, mg->p, L0.z, L0.code, mg->n, (const int *)L0.act, (const int *)L0.act_n, c.kc);
 }

@@ -59,12 +59,15 @@ struct SplitArgs {
     const void *zc;             // kProlong: next level's correction, natural order (TC)
     float zc_scale;
     float *zn;                  // kLast: natural-order output
-    // kLast, FP32 solve: z.r of the CG step folded in (mgpcg.py:401, 451):
-    // dot 1 -- zr_old = z.r and p = z (the solve's prologue), dot 2 -- beta =
-    // z.r / zr_old, zr_old = z.r (each iteration); 0 -- none.  rdot is the
-    // natural-order r; the per-group sums are k8_dot_zr's.
-    int dot;
-    const float *rdot;
+    // kLast: z.r of the CG step folded in (mgpcg.py:401, 451): dot 1 --
+    // zr_old = z.r and p = z (the solve's prologue), dot 2 -- beta = z.r /
+    // zr_old, zr_old = z.r (each iteration), dot 3 -- the flexible beta =
+    // (z.r - z.r_old) / zr_old of the mixed-precision solve; 0 -- none.  rdot
+    // and rold are natural-order FP32 vectors; zscaled: the CG's z is
+    // st->zscale times the V-cycle's output (mixed precision).  The per-group
+    // sums are k8_dot_zr's / k8_dot_zr_flex's.
+    int dot, zscaled;
+    const float *rdot, *rold;
     float *pinit;
     MgState *st;
     double *partials;
@@ -117,7 +120,8 @@ __global__ void __launch_bounds__(256, (kMode == kProlong || kMode == kLast) ? 4
     }
     pdl_wait(kc);
     bool first = true;
-    double zr = 0.0;  // kLast with A.dot: this thread's part of z.r
+    double zr = 0.0, zro = 0.0;  // kLast with A.dot: this thread's parts of z.r and z.r_old
+    const float zsc = (kMode == kLast && A.dot && A.zscaled) ? A.st->zscale : 1.0f;
     for (; t < total; t += stride) {
         const int g = g_next;
         const int tn = t + stride;
@@ -255,10 +259,17 @@ __global__ void __launch_bounds__(256, (kMode == kProlong || kMode == kLast) ? 4
             }
             St<float>::st8(A.zn + ((size_t)g << 3), o8);
             if (A.dot) {
-                float rv[8];
+                float zv[8], rv[8];
+#pragma unroll
+                for (int m = 0; m < 8; m++) zv[m] = A.zscaled ? __fmul_rn(o8[m], zsc) : o8[m];
                 St<float>::ld8_ro(A.rdot + ((size_t)g << 3), rv);
-                zr += dot8_ff(o8, rv);
-                if (A.dot == 1) St<float>::st8(A.pinit + ((size_t)g << 3), o8);
+                zr += dot8_ff(zv, rv);
+                if (A.dot == 3) {
+                    float ov[8];
+                    St<float>::ld8_ro(A.rold + ((size_t)g << 3), ov);
+                    zro += dot8_ff(zv, ov);
+                }
+                if (A.dot == 1) St<float>::st8(A.pinit + ((size_t)g << 3), zv);
             }
         } else {
             St<TZ>::st4(z + uoff + h, out);
@@ -269,15 +280,29 @@ __global__ void __launch_bounds__(256, (kMode == kProlong || kMode == kLast) ? 4
         // the grid's z.r in FP64 (deterministic two-level reduction) and the
         // CG scalars, as k8_dot_zr sets them
         __shared__ double red[32];
+        if (A.dot == 3) {
+            const double bo = block_sum(zro, red);
+            __syncthreads();
+            if (threadIdx.x == 0) A.partials[kMaxRedBlocks + blockIdx.x] = bo;
+        }
         double tot;
-        if (finish_partials(zr, A.partials, &A.st->ticket, red, &tot) && threadIdx.x == 0) {
-            if (A.dot == 1) {
-                A.st->zr_old = tot;
-            } else {
-                const double beta = tot / (A.st->zr_old + A.st->eps);
-                A.st->beta = beta;
-                A.st->zr_old = tot;
-                if (!isfinite(beta)) A.st->status = FLUB_ERR_BREAKDOWN;
+        if (finish_partials(zr, A.partials, &A.st->ticket, red, &tot)) {
+            double t2 = 0.0;
+            if (A.dot == 3) {
+                __syncthreads();
+                for (unsigned q = threadIdx.x; q < gridDim.x; q += blockDim.x)
+                    t2 += __ldcg(&A.partials[kMaxRedBlocks + q]);
+                t2 = block_sum(t2, red);
+            }
+            if (threadIdx.x == 0) {
+                if (A.dot == 1) {
+                    A.st->zr_old = tot;
+                } else {
+                    const double beta = (A.dot == 3 ? tot - t2 : tot) / (A.st->zr_old + A.st->eps);
+                    A.st->beta = beta;
+                    A.st->zr_old = tot;
+                    if (!isfinite(beta)) A.st->status = FLUB_ERR_BREAKDOWN;
+                }
             }
         }
     }
