@@ -140,9 +140,13 @@ def run_profile_kernel(args):
     torch.cuda.synchronize()
     torch.cuda.empty_cache()
     if args.profile_kernel == "smooth":
-        # z is defined (set_tags clears every level's z): three level-0
-        # red-black iterations (the tiled kernel where the level has tiles) are
-        # the only smoother launches of this process
+        # one V-cycle of a seeded uniform residual on the fluid cells gives the
+        # level-0 buffers generic values, as the benchmark's timing does (its
+        # level-0 smoothing: launches 0-7 of k_smooth_split); then three level-0
+        # red-black iterations, launches 8-13 (ncu -k regex:k_smooth_split -s 8)
+        gen = torch.Generator(device="cuda")
+        gen.manual_seed(7)
+        mg.apply_preconditioner(r=torch.rand(scene.shape, generator=gen, device="cuda") * (tag == 1))
         for q in range(3):
             mg.smooth_iteration(0, q & 1)
     elif args.profile_kernel == "matvec":
@@ -476,12 +480,21 @@ def run_ours(args):
                              "overlap the solves on two copy streams; the first upload and the last read-back "
                              "are inside the timed region"}
 
-    # ---- roofline of the dominant kernel of the plain path: one level-0
-    # red-black iteration (the TMA-tiled kernel, two half-sweeps per launch),
-    # timed on the plain handle's level-0 buffers
+    # ---- roofline of the dominant kernel of the plain path: the level-0
+    # red-black half-sweep (flub_mg_smooth_iteration: the colour-split row
+    # kernel, or with FLUB_TILE=1 the TMA-tiled one, two half-sweeps per
+    # launch), timed on the plain handle's level-0 buffers
     peak, peak_kind = load_peaks()
     reps = 24
     plain_mg = variants["plain"].mg
+    fluid = (variants["plain"].tag.f == 1)
+    # the operands of the timed sweeps: the level-0 buffers of one V-cycle of a
+    # seeded uniform residual on the fluid cells (generic values; what a
+    # converged solve leaves behind holds exact zeros, which some updates
+    # shortcut)
+    gen = torch.Generator(device=fluid.device)
+    gen.manual_seed(7)
+    plain_mg.apply_preconditioner(r=torch.rand(fluid.shape, generator=gen, device=fluid.device) * fluid)
     smoother = plain_mg.smooth_iteration(0, 0)  # 0 natural-order rows, 1 TMA tiles, 2 colour-split rows
     tiled = smoother == 1
     plain_mg.smooth_iteration(0, 0)
@@ -494,7 +507,6 @@ def run_ours(args):
     torch.cuda.synchronize()
     launch_ms = k0.elapsed_time(k1) / reps / (1 if tiled else 2)
     nx_, ny_, nz_ = scene.shape
-    fluid = (proj.tag.f == 1)
     if tiled:
         # a CTA stages and updates the whole of every tile (8 x 8 x 32 cells)
         # that holds a fluid cell: the canonical 13 B per cell per iteration
@@ -694,8 +706,8 @@ def run_ours(args):
     # ---- the 512^3 dam break (the 256^3 scene scaled up, generated on the
     # device): ms per solve of plain FP32 (reference schedule), plain-v22 and
     # learned+mixed-v22, each to relative residual 1e-6; the pressures of the
-    # light variants against the plain one (an FP64 host solve at 512^3 would
-    # take minutes)
+    # light variants against the plain one, and of all three against the FP64
+    # oracle's solve of the same scene on the host cores (--no-oracle512 skips it)
     scale512 = None
     if rank == 0 and not args.no_scale512:
         del variants
@@ -731,7 +743,13 @@ def run_ours(args):
             if p_plain is None:
                 p_plain = pj.p.f.detach().double().clone()
                 # the level-0 half-sweep at 512^3 (8x the groups of the 256^3 launch),
-                # the kernel the V-cycle runs there (two half-sweeps per call)
+                # the kernel the V-cycle runs there (two half-sweeps per call), on
+                # the buffers of one V-cycle of a seeded residual as at 256^3
+                g5 = torch.Generator(device=v5.u.f.device)
+                g5.manual_seed(7)
+                fl5 = pj.tag.f == 1
+                pj.mg.apply_preconditioner(r=torch.rand(fl5.shape, generator=g5, device=fl5.device) * fl5)
+                del fl5
                 kind = pj.mg.smooth_iteration(0, 0)
                 torch.cuda.synchronize()
                 e0.record(stream)

@@ -70,14 +70,14 @@ constexpr uint32_t kInteriorWord = 0x2AAAu;
 // Res. Dev. 34(1), 1990; q0 = a y, r = a - 6 q0 exactly, q = q0 + r y): three
 // FP32 operations instead of a division.  tests/test_div6_exhaustive.py checks
 // it bit for bit against IEEE division for every float32 with |a| in
-// [2^-100, 2^100]; other inputs (zeros, tiny, huge, inf, NaN) take __fdiv_rn.
+// [2^-100, 2^100] and for the zeros, which return q0 (a zero of a's sign, as
+// a / 6); the other inputs (tiny, huge, inf, NaN) take __fdiv_rn.
 __device__ __forceinline__ float div6_rn(float a) {
     constexpr float y = 0x1.555556p-3f;  // 1/6 rounded to nearest
     const float m = fabsf(a);
-    if (m >= 0x1p-100f && m <= 0x1p100f) {
-        const float q0 = __fmul_rn(a, y);
-        return __fmaf_rn(__fmaf_rn(-q0, 6.0f, a), y, q0);
-    }
+    const float q0 = __fmul_rn(a, y);
+    if (m >= 0x1p-100f && m <= 0x1p100f) return __fmaf_rn(__fmaf_rn(-q0, 6.0f, a), y, q0);
+    if (m == 0.0f) return q0;
     return __fdiv_rn(a, 6.0f);
 }
 

@@ -93,10 +93,15 @@ __device__ __forceinline__ uint32_t word4_at(uint2 w, int m) {
 // neighbour bits.
 __device__ __forceinline__ uint32_t word_kcode(uint32_t w, bool kp) { return sw_code(w, kp ? 5 : 6); }
 
-// 5 resident blocks of 256 threads per SM for the lean modes (48 registers),
-// 4 for the prolongation and the natural-order output, which hold more.
+// Register bound of 3 blocks of 256 threads per SM for the lean modes (the
+// in-place FP32 sweep then takes 64 registers and 4 blocks are resident), 4
+// for the prolongation and the natural-order output.  Measured on the 256^3
+// and 512^3 dam breaks: the lean modes at 5 blocks (48 registers) are as fast
+// at 256^3 and 10 % slower at 512^3 (fewer groups in flight at once stream
+// from DRAM more efficiently), 6 spills, and 2 blocks, or two groups per lane
+// with their loads issued together, are slower at both sizes.
 template <int kMode, typename TRN, typename TR, typename TZI, typename TZ, typename TC>
-__global__ void __launch_bounds__(256, (kMode == kProlong || kMode == kLast) ? 4 : 5)
+__global__ void __launch_bounds__(256, (kMode == kProlong || kMode == kLast) ? 4 : 3)
     k_smooth_split(const SplitArgs A, int phase, unsigned long long *kc) {
     pdl_open();
     const Dims D = A.D;
