@@ -218,39 +218,49 @@ __device__ __forceinline__ void tail_prolong(float *zf, const float *zc, const D
 }
 
 // ---------------------------------------------------------------- FP64 bottom
-// tail_lap / tail_update / tail_half_lean in FP64, the same operations in the
-// same order with IEEE double rounding at each (no contraction).
+// No reference counterpart (the reference smooths its bottom level in FP32).
+// The red-black Gauss-Seidel update of the other levels, z_c + (r + L z) / d
+// with L z the sum over non-solid neighbours of (z_n - z_c), z_n = 0 for air,
+// is in exact arithmetic (r + sum of the fluid neighbours' z) / d: the z_c
+// terms cancel.  The bottom uses that form, which takes 6 FP64 additions and
+// the division where the other takes 14 operations (this GPU issues FP64 at a
+// small fraction of its FP32 rate, and the bottom runs on one SM): neighbours
+// summed in the order i+, i-, j+, j-, k+, k- onto r, each non-fluid one adding
+// +0.0, IEEE double rounding at each operation.  The oracle's FP64 bottom
+// (oracle_bottom_half64) is the same sequence.
 
 // a / d for d = 1..6, rounded to nearest as __ddiv_rn(a, d), by Markstein's
 // FMA correction of a * RN(1/d) (P. Markstein, IBM J. Res. Dev. 34(1), 1990):
 // two FMAs and a product instead of an FP64 division, which GB300 issues
 // slowly.  tests/test_div6_exhaustive.py checks it bit for bit against IEEE
-// division on 2^28 random doubles per d with |a| in [2^-900, 2^900]; other
-// inputs take __ddiv_rn.
+// division on 2^28 random doubles per d with |a| in [2^-900, 2^900] and on the
+// zeros (which return a * RN(1/d), a zero of a's sign); other inputs take
+// __ddiv_rn.
 __device__ __forceinline__ double ddiv_small_rn(double a, int d) {
     const double y = d == 1 ? 1.0 : d == 2 ? 0.5 : d == 3 ? 1.0 / 3.0 : d == 4 ? 0.25 : d == 5 ? 0.2 : 1.0 / 6.0;
     const double m = fabs(a);
-    if (m >= 0x1p-900 && m <= 0x1p900) {
-        const double q0 = __dmul_rn(a, y);
-        return __fma_rn(__fma_rn(-q0, (double)d, a), y, q0);
-    }
+    const double q0 = __dmul_rn(a, y);
+    if (m >= 0x1p-900 && m <= 0x1p900) return __fma_rn(__fma_rn(-q0, (double)d, a), y, q0);
+    if (m == 0.0) return q0;
     return __ddiv_rn(a, (double)d);
 }
-__device__ __forceinline__ double tail_lap64(const double *z, int c, uint32_t m, int si, int sj) {
-    const double xc = z[c];
+
+// r + the fluid neighbours' z of cell c (mask m as in TailCache), in the
+// order above.  All six neighbours are loaded (an excluded one reads the cell
+// itself) so the loads issue together.
+__device__ __forceinline__ double tail_gs_sum64(const double *z, int c, uint32_t m, double rc, int si, int sj) {
     const double zip = z[(m & 1u) ? c + si : c], zim = z[(m & 2u) ? c - si : c];
     const double zjp = z[(m & 4u) ? c + sj : c], zjm = z[(m & 8u) ? c - sj : c];
     const double zkp = z[(m & 16u) ? c + 1 : c], zkm = z[(m & 32u) ? c - 1 : c];
-    double tp, tm, ret = 0.0;
-    tp = (m & 1u) ? __dsub_rn((m & 64u) ? 0.0 : zip, xc) : 0.0;
-    tm = (m & 2u) ? __dsub_rn((m & 128u) ? 0.0 : zim, xc) : 0.0;
-    ret = __dadd_rn(ret, __dadd_rn(tp, tm));
-    tp = (m & 4u) ? __dsub_rn((m & 256u) ? 0.0 : zjp, xc) : 0.0;
-    tm = (m & 8u) ? __dsub_rn((m & 512u) ? 0.0 : zjm, xc) : 0.0;
-    ret = __dadd_rn(ret, __dadd_rn(tp, tm));
-    tp = (m & 16u) ? __dsub_rn((m & 1024u) ? 0.0 : zkp, xc) : 0.0;
-    tm = (m & 32u) ? __dsub_rn((m & 2048u) ? 0.0 : zkm, xc) : 0.0;
-    return __dadd_rn(ret, __dadd_rn(tp, tm));
+    // neighbour q is fluid: in the domain and not solid (bit q), not air (bit q + 6)
+    const uint32_t fl = (m & 63u) & ~((m >> 6) & 63u);
+    double s = rc;
+    s = __dadd_rn(s, (fl & 1u) ? zip : 0.0);
+    s = __dadd_rn(s, (fl & 2u) ? zim : 0.0);
+    s = __dadd_rn(s, (fl & 4u) ? zjp : 0.0);
+    s = __dadd_rn(s, (fl & 8u) ? zjm : 0.0);
+    s = __dadd_rn(s, (fl & 16u) ? zkp : 0.0);
+    return __dadd_rn(s, (fl & 32u) ? zkm : 0.0);
 }
 
 __device__ __forceinline__ void tail_half64(double *z, const TailCache &tc, const Dims D, int phase, int nthr) {
@@ -265,8 +275,7 @@ __device__ __forceinline__ void tail_half64(double *z, const TailCache &tc, cons
         const double rc = (double)(odd ? tc.r1[q] : tc.r0[q]);
         double zn = 0.0;
         const int d = __popc(m & 63u);
-        if ((m & (1u << 12)) && d != 0)
-            zn = __dadd_rn(z[cu], ddiv_small_rn(__dadd_rn(rc, tail_lap64(z, cu, m, si, sj)), d));
+        if ((m & (1u << 12)) && d != 0) zn = ddiv_small_rn(tail_gs_sum64(z, cu, m, rc, si, sj), d);
         z[cu] = zn;
     }
     tail_sync(nthr);

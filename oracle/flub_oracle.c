@@ -799,18 +799,44 @@ void oracle_tag_levels(int32_t **tagl, int levels, int nx, int ny, int nz) {
 }
 
 /* Level-hierarchy helpers so that Python can drive the V-cycle directly. */
+/* FP64 bottom half-sweep (no reference counterpart; the red-black order of
+ * oracle_smooth): the Gauss-Seidel update z_c + (r + L z) / d written as
+ * (r + the fluid neighbours' z) / d, which it equals in exact arithmetic (the
+ * z_c terms cancel).  The neighbours are added onto r in the order i+, i-,
+ * j+, j-, k+, k-, each non-fluid or out-of-domain one adding +0.0; d counts
+ * the in-domain non-solid neighbours (0: z = 0). */
+static void oracle_bottom_half64(double *z, const double *r, const int32_t *tag, int nx, int ny, int nz, int phase) {
+    int par = 1 - phase;
+    for (int i = 0; i < nx; i++)
+        for (int j = 0; j < ny; j++)
+            for (int k = (par - ((i + j) & 1) + 2) & 1; k < nz; k += 2) {
+                int64_t c = IX(i, j, k);
+                int d = divd_f64(tag, nx, ny, nz, i, j, k);
+                if (d == 0) { z[c] = 0.0; continue; }
+                double s = r[c];
+                int64_t nb;
+                nb = IX(i + 1, j, k); s = s + ((i + 1 < nx && tag[nb] == 1) ? z[nb] : 0.0);
+                nb = IX(i - 1, j, k); s = s + ((i - 1 >= 0 && tag[nb] == 1) ? z[nb] : 0.0);
+                nb = IX(i, j + 1, k); s = s + ((j + 1 < ny && tag[nb] == 1) ? z[nb] : 0.0);
+                nb = IX(i, j - 1, k); s = s + ((j - 1 >= 0 && tag[nb] == 1) ? z[nb] : 0.0);
+                nb = IX(i, j, k + 1); s = s + ((k + 1 < nz && tag[nb] == 1) ? z[nb] : 0.0);
+                nb = IX(i, j, k - 1); s = s + ((k - 1 >= 0 && tag[nb] == 1) ? z[nb] : 0.0);
+                z[c] = s / (double)d;
+            }
+}
+
 static void oracle_bottom_fp64_f32(float *z, const float *r, const int32_t *tag, int nx, int ny, int nz) {
     int64_t n = (int64_t)nx * ny * nz;
     double *zd = (double *)calloc((size_t)n, sizeof(double));
     double *rd = (double *)malloc(sizeof(double) * (size_t)n);
     for (int64_t c = 0; c < n; c++) rd[c] = (double)r[c];
     for (int it = 0; it < oracle_sched_bottom; it++) {
-        oracle_smooth_f64(zd, rd, tag, nx, ny, nz, 0);
-        oracle_smooth_f64(zd, rd, tag, nx, ny, nz, 1);
+        oracle_bottom_half64(zd, rd, tag, nx, ny, nz, 0);
+        oracle_bottom_half64(zd, rd, tag, nx, ny, nz, 1);
     }
     for (int it = 0; it < oracle_sched_bottom; it++) {
-        oracle_smooth_f64(zd, rd, tag, nx, ny, nz, 1);
-        oracle_smooth_f64(zd, rd, tag, nx, ny, nz, 0);
+        oracle_bottom_half64(zd, rd, tag, nx, ny, nz, 1);
+        oracle_bottom_half64(zd, rd, tag, nx, ny, nz, 0);
     }
     for (int64_t c = 0; c < n; c++) z[c] = (float)zd[c];
     free(zd);

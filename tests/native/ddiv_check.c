@@ -2,7 +2,8 @@
  * (1..6) in flub_gb300/csrc/tail.cuh: Markstein's FMA correction of
  * a * RN(1/d) against IEEE double a / d, bit for bit, for 2^28 random
  * doubles per d with |a| in [2^-900, 2^900] (uniform exponent, random
- * mantissa and sign).  Exits 1 on any mismatch. */
+ * mantissa and sign), and the zeros, for which the kernel returns the
+ * product a * RN(1/d).  Exits 1 on any mismatch. */
 #include <math.h>
 #include <stdint.h>
 #include <stdio.h>
@@ -38,6 +39,15 @@ int main(void) {
             bad += b1 != b2;
         }
     }
+    /* the zeros return the product a * RN(1/d), a zero of a's sign */
+    for (int d = 1; d <= 6; d++)
+        for (int sg = 0; sg < 2; sg++) {
+            const double a = sg ? -0.0 : 0.0, ref = a / (double)d, q = a * (1.0 / (double)d);
+            uint64_t b1, b2;
+            memcpy(&b1, &ref, 8);
+            memcpy(&b2, &q, 8);
+            bad += b1 != b2;
+        }
     printf("checked %lld, mismatches %lld\n", checked, bad);
     return bad != 0;
 }
