@@ -24,10 +24,10 @@ __device__ __forceinline__ void store_row8(float *p, const float v[8]) {
 }
 
 // L x for the 8 cells of the row starting at c0 (group g), same operation
-// order as lap_at, from the stencil words (sw, or the codes when sw is NULL).
-// Non-fluid cells get 0.
-__device__ __forceinline__ void lap_row8(const float *__restrict__ x, const uint8_t *__restrict__ code,
-                                         const uint16_t *__restrict__ sw, const Dims D, int g, float out[8], Row8 &xc) {
+// order as lap_at, from the stencil words wd of the row.  Non-fluid cells get
+// 0.
+__device__ __forceinline__ void lap_row8_w(const float *__restrict__ x, const uint4 wd, const Dims D, int g,
+                                           float out[8], Row8 &xc) {
     int i, j, kg;
     group_ijk(g, D, i, j, kg);
     const int k0 = kg << 3;
@@ -35,7 +35,6 @@ __device__ __forceinline__ void lap_row8(const float *__restrict__ x, const uint
     const int c0 = g << 3;
     const bool hip = i + 1 < D.nx, him = i > 0, hjp = j + 1 < D.ny, hjm = j > 0;
     const bool hkp = k0 + 8 < D.nz, hkm = k0 > 0;
-    const uint4 wd = load_words8(sw, code, D, i, j, k0, c0);
     Row8 xip, xim, xjp, xjm;
     load_row8(x + c0, xc);
     if (hip) load_row8(x + c0 + si, xip); else zero_row8(xip);
@@ -54,22 +53,50 @@ __device__ __forceinline__ void lap_row8(const float *__restrict__ x, const uint
     }
 }
 
+// lap_row8_w with the words from sw, or from the codes when sw is NULL.
+__device__ __forceinline__ void lap_row8(const float *__restrict__ x, const uint8_t *__restrict__ code,
+                                         const uint16_t *__restrict__ sw, const Dims D, int g, float out[8], Row8 &xc) {
+    int i, j, kg;
+    group_ijk(g, D, i, j, kg);
+    lap_row8_w(x, load_words8(sw, code, D, i, j, kg << 3, g << 3), D, g, out, xc);
+}
+
 // Ap = L p, p.Ap -> alpha (mgpcg.py:410-419); guarded like k_matvec_pap.
-__global__ void __launch_bounds__(kRedThreads) k8_matvec_pap(MgState *st, const float *__restrict__ p,
+// The active-list length, the first list entry and the first group's stencil
+// words do not change during a solve (set_tags writes them before it): they
+// are read before the wait on the previous kernel, and each next list entry one
+// group ahead.  Launched with one resident wave of blocks.
+__global__ void __launch_bounds__(kRedThreads, 4) k8_matvec_pap(MgState *st, const float *__restrict__ p,
                                                              float *__restrict__ Ap, const uint8_t *__restrict__ code,
-                                                             const uint16_t *__restrict__ sw, Dims D, double *partials, const int *__restrict__ act,
+                                                             const uint16_t *__restrict__ sw, Dims D, double *partials,
+                                                             const int *__restrict__ act,
                                                              const int *__restrict__ act_n, unsigned long long *kc) {
     __shared__ double red[32];
-    count_kernel(kc);
-    if (st->it >= st->max_iters || st->converged || st->status) return;
+    pdl_open();
     const int ng = (int)(D.n() >> 3);
+    const int tot = act ? *act_n : ng;
+    const int stride = gridDim.x * blockDim.x;
+    int t = blockIdx.x * blockDim.x + threadIdx.x;
+    int g_next = t < tot ? (act ? __ldg(act + t) : t) : 0;
+    uint4 wd_first = make_uint4(0u, 0u, 0u, 0u);
+    if (t < tot && sw) wd_first = __ldg(reinterpret_cast<const uint4 *>(sw + ((size_t)g_next << 3)));
+    pdl_wait(kc);
+    if (st->it >= st->max_iters || st->converged || st->status) return;
     double s = 0.0;
-    FLUB_ACT_LOOP(g, act, act_n, ng) {
-        const uint2 cc = load_codes8(code + (g << 3));
-        if (!act && !group_has_fluid(cc)) continue;  // Ap = 0 there already
+    bool first = true;
+    for (; t < tot; t += stride) {
+        const int g = g_next;
+        const int tn = t + stride;
+        g_next = tn < tot ? (act ? __ldg(act + tn) : tn) : 0;
+        const bool use_first = first && sw;
+        first = false;
+        if (!act && !group_has_fluid(load_codes8(code + (g << 3)))) continue;  // Ap = 0 there already
+        int i, j, kg;
+        group_ijk(g, D, i, j, kg);
+        const uint4 wd = use_first ? wd_first : load_words8(sw, code, D, i, j, kg << 3, g << 3);
         float a[8];
         Row8 pc;
-        lap_row8(p, code, sw, D, g, a, pc);
+        lap_row8_w(p, wd, D, g, a, pc);
         store_row8(Ap + (g << 3), a);
         s += dot8_ff(pc.v, a);
     }

@@ -546,6 +546,22 @@ static int validate_shape(int nx, int ny, int nz, int levels, int precision) {
 
 static inline unsigned red_blocks(int64_t n) { return blocks_for(n, kRedThreads, 152 * 6); }
 
+// Grid of k8_matvec_pap over the level-0 groups: one resident wave (its
+// registers allow fewer blocks per SM than red_blocks assumes, which left a
+// second, partial wave).
+static unsigned matvec_blocks(int64_t groups) {
+    static int resident = 0;
+    if (resident <= 0) {
+        int b = 0;
+        if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, k8_matvec_pap, kRedThreads, 0) != cudaSuccess || b < 1) {
+            cudaGetLastError();
+            b = 4;
+        }
+        resident = b;
+    }
+    return blocks_for(groups + 1, kRedThreads, (int64_t)kNumSMs * resident);
+}
+
 // ---------------------------------------------------------------- enqueue helpers
 
 #define FLUB_TRY(...)              \
@@ -1133,8 +1149,9 @@ static int enqueue_prologue_mixed(flub_mg *mg, const LaunchCtx &c, int smoother)
 static int enqueue_first_half_mixed(flub_mg *mg, const LaunchCtx &c, int smoother) {
     const Level &L0 = mg->lv[0];
     const unsigned b = red_blocks(mg->n), bg = red_blocks(mg->n / 8 + 1);
-    FLUB_TRY(launch_pdl(k8_matvec_pap, dim3(bg), dim3(kRedThreads), 0, c.s, mg->st, mg->p, mg->Ap, L0.code,
-                        (const uint16_t *)L0.sw, L0.D, mg->partials, (const int *)L0.act, (const int *)L0.act_n, c.kc));
+    FLUB_TRY(launch_pdl(k8_matvec_pap, dim3(matvec_blocks(mg->n / 8)), dim3(kRedThreads), 0, c.s, mg->st, mg->p,
+                        mg->Ap, L0.code, (const uint16_t *)L0.sw, L0.D, mg->partials, (const int *)L0.act,
+                        (const int *)L0.act_n, c.kc));
     if (smoother == FLUB_SMOOTHER_FRACTION) {
         FLUB_CHECK_CUDA(cudaMemcpyAsync(mg->r_old, L0.r, sizeof(float) * mg->n, cudaMemcpyDeviceToDevice, c.s));
         FLUB_TRY(launch_pdl(k_update_r, dim3(b), dim3(kRedThreads), 0, c.s, mg->st, L0.r, mg->Ap, mg->n, c.kc));
@@ -1201,8 +1218,9 @@ static int enqueue_first_half(flub_mg *mg, const LaunchCtx &c, int smoother) {
     const bool v8 = (L0.D.nz % 8) == 0;
     const unsigned bg = red_blocks(mg->n / 8 + 1);
     if (v8)
-        FLUB_TRY(launch_pdl(k8_matvec_pap, dim3(bg), dim3(kRedThreads), 0, c.s, mg->st, mg->p, mg->Ap, L0.code,
-                            (const uint16_t *)L0.sw, L0.D, mg->partials, (const int *)L0.act, (const int *)L0.act_n, c.kc));
+        FLUB_TRY(launch_pdl(k8_matvec_pap, dim3(matvec_blocks(mg->n / 8)), dim3(kRedThreads), 0, c.s, mg->st,
+                            mg->p, mg->Ap, L0.code, (const uint16_t *)L0.sw, L0.D, mg->partials, (const int *)L0.act,
+                            (const int *)L0.act_n, c.kc));
     else
         FLUB_TRY(launch_pdl(k_matvec_pap, dim3(b), dim3(kRedThreads), 0, c.s, mg->st, mg->p, mg->Ap, L0.code, L0.D,
                             mg->partials, c.kc));
