@@ -82,7 +82,9 @@ def _cases():
 
 
 def import_reference(reference):
-    """Import the reference modules with the CPU stand-in as ``warp``."""
+    """Import the reference modules with the CPU stand-in as ``warp``.  No
+    bytecode is written: the reference tree stays as it is."""
+    sys.dont_write_bytecode = True
     stand_in = os.path.join(ROOT, "oracle", "warp_cpu")
     for p in (reference, stand_in):
         if p in sys.path:
