@@ -19,10 +19,15 @@ code):
   sequential order.
 * ``float`` in a kernel is FP32: arrays hold ``numpy.float32``, scalar kernel
   arguments annotated ``float`` are rounded to FP32 at launch, ``constant``
-  turns Python floats into FP32, and vector components are FP32.  Python
-  float literals combine with FP32 values as FP32 (numpy >= 2 promotion
-  rules), so every arithmetic operation of the kernel bodies is an IEEE FP32
-  operation, evaluated without FMA contraction.
+  turns Python floats into FP32, and vector components are FP32.  The bodies
+  of ``@kernel`` and ``@func`` functions are recompiled from their source so
+  that every float literal, and every module-level Python float they read, is
+  an FP32 constant, as Warp's code generator makes them: ``2.0 / 9.0`` is an
+  FP32 division at run time, not a double folded by Python.  Every arithmetic
+  operation of the bodies is then an IEEE FP32 operation (numpy >= 2
+  promotion rules keep Python ints and floats produced at run time, such as
+  ``float(i)``, weak against FP32), evaluated without FMA contraction.  Host
+  code of the reference modules is left as it is.
 * ``empty`` returns zero-filled memory (Warp leaves it uninitialised).
 * Between ``capture_begin`` and ``capture_end`` launches and array fills are
   recorded, not executed; ``capture_launch`` replays them.  This is what makes
@@ -35,9 +40,11 @@ reductions, ``where``, ``clamp``, ``length`` = sqrt(dot), ``dot`` summed left to
 right, ``cross``, ``quat_rotate_inv(q, x) = x (2w^2 - 1) - cross(q.xyz, x) w 2 +
 q.xyz dot(q.xyz, x) 2``, ``atomic_add`` returning the old value.
 """
+import ast
 import builtins
 import inspect
 import math
+import textwrap
 
 import numpy as np
 
@@ -87,6 +94,9 @@ class _Vec:
     __slots__ = ("c",)
     N = 3
     FLOAT = True
+    # numpy scalars defer to the vector's own operators (an FP32 scalar times
+    # a vector is a vector, not an array built from its components)
+    __array_ufunc__ = None
 
     def __init__(self, *args):
         if len(args) == 1 and isinstance(args[0], (_Vec, list, tuple, np.ndarray)):
@@ -179,6 +189,35 @@ class quat(_Vec):
                     a[3] * b[1] + b[3] * a[1] + a[2] * b[0] - a[0] * b[2],
                     a[3] * b[2] + b[3] * a[2] + a[0] * b[1] - a[1] * b[0],
                     a[3] * b[3] - (a[0] * b[0] + a[1] * b[1] + a[2] * b[2]))
+
+
+class transform:
+    """wp.transform: a position and a rotation (the reference only names the
+    type in kernel signatures and builds it from (p, q))."""
+
+    def __init__(self, p=None, q=None):
+        self.p = vec3(p) if p is not None else vec3()
+        self.q = quat(q) if q is not None else quat(0.0, 0.0, 0.0, 1.0)
+
+
+class spatial_vector(_Vec):
+    """wp.spatial_vector: 6 FP32 components (angular, then linear)."""
+    __slots__ = ()
+    N = 6
+
+    def __init__(self, *args):
+        if len(args) == 2 and all(isinstance(a, _Vec) for a in args):
+            args = (list(args[0]) + list(args[1]),)
+        super().__init__(*args)
+
+
+class types:
+    """wp.types.vector(length, dtype): a fixed-length FP32 (or int) vector type."""
+
+    @staticmethod
+    def vector(length, dtype=builtins.float):
+        return type(f"vec{length}", (_Vec,), {"__slots__": (), "N": builtins.int(length),
+                                              "FLOAT": dtype is not builtins.int and dtype is not np.int32})
 
 
 def quat_identity():
@@ -436,13 +475,71 @@ def _enqueue(fn):
         fn()
 
 
+def _wp_f32(x):
+    return _f32(x)
+
+
+def _wp_glob(x):
+    """A module-level name read by kernel code: Python floats are FP32
+    constants there (bool is left alone)."""
+    return _f32(x) if type(x) is builtins.float else x
+
+
+class _Fp32Source(ast.NodeTransformer):
+    """Float literals -> _wp_f32(literal); reads of names that are not local
+    to the function -> _wp_glob(name)."""
+
+    def __init__(self, local_names):
+        self.local_names = local_names
+
+    def visit_Constant(self, node):
+        if type(node.value) is builtins.float:
+            return ast.copy_location(ast.Call(ast.Name("_wp_f32", ast.Load()), [node], []), node)
+        return node
+
+    def visit_Name(self, node):
+        if isinstance(node.ctx, ast.Load) and node.id not in self.local_names:
+            return ast.copy_location(ast.Call(ast.Name("_wp_glob", ast.Load()), [node], []), node)
+        return node
+
+
+def _fp32_function(f):
+    """f recompiled from its source with _Fp32Source, in f's own module
+    namespace (which gains the two helper names)."""
+    src = textwrap.dedent(inspect.getsource(f))
+    tree = ast.parse(src)
+    ast.increment_lineno(tree, f.__code__.co_firstlineno - 1)  # tracebacks point into the reference file
+    fn = tree.body[0]
+    fn.decorator_list = []
+    local_names = {a.arg for a in fn.args.args + fn.args.kwonlyargs + fn.args.posonlyargs}
+    if fn.args.vararg:
+        local_names.add(fn.args.vararg.arg)
+    if fn.args.kwarg:
+        local_names.add(fn.args.kwarg.arg)
+    for node in ast.walk(fn):
+        if isinstance(node, ast.Name) and isinstance(node.ctx, (ast.Store, ast.Del)):
+            local_names.add(node.id)
+    # defaults and annotations are evaluated at definition time: leave them
+    new_body = [_Fp32Source(local_names).visit(b) for b in fn.body]
+    fn.body = new_body
+    ast.fix_missing_locations(tree)
+    g = f.__globals__
+    g.setdefault("_wp_f32", _wp_f32)
+    g.setdefault("_wp_glob", _wp_glob)
+    ns = {}
+    exec(compile(tree, inspect.getsourcefile(f) or "<kernel>", "exec"), g, ns)
+    out = ns[f.__name__]
+    out.__wrapped__ = f
+    return out
+
+
 def func(f):
-    return f
+    return _fp32_function(f)
 
 
 class Kernel:
     def __init__(self, f):
-        self.func = f
+        self.func = _fp32_function(f)
         self.__name__ = f.__name__
         self.key = f.__name__
         sig = inspect.signature(f)
