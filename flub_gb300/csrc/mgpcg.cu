@@ -69,6 +69,11 @@ struct Level {
     unsigned char *tflags;
     int *tiles, *tiles_n;
     int n_tiles;
+    // levels small enough for the one-block tail (tail.cuh), nz even: the
+    // neighbour masks of each k-pair of cells the tail's sweeps use, built once
+    // by set_tags (the tail otherwise rebuilds them from the codes at every
+    // level entry of every V-cycle); NULL elsewhere
+    uint32_t *pmask;
 };
 
 struct LaunchCtx {
@@ -197,6 +202,8 @@ static size_t carve(flub_mg *mg, char *base) {
             L.tiles = (int *)take(sizeof(int) * (size_t)L.n_tiles);
             L.tiles_n = (int *)take(sizeof(int));
         }
+        L.pmask = nullptr;
+        if (nl <= kTailMaxCells && L.D.nz % 2 == 0) L.pmask = (uint32_t *)take(sizeof(uint32_t) * (size_t)(nl >> 1));
     }
     // per-block counts of the active-list build (level 0 has the most blocks)
     mg->act_scratch = (int *)take(sizeof(int) * (size_t)((n / 8 + kActPerBlock - 1) / kActPerBlock + 1));
@@ -220,6 +227,7 @@ static size_t tail_layout(const flub_mg *mg, int lt, TailParams *P) {
         TailLevel &T = P->lv[l - lt];
         T.D = D;
         T.code = mg->lv[l].code;
+        T.pmask = mg->lv[l].pmask;
         T.abs_level = l;
         T.off_z = take(sizeof(float) * n);
         T.off_r = take(sizeof(float) * n);
@@ -1666,6 +1674,12 @@ int flub_mg_set_tags(flub_mg *mg, const int32_t *tag, void *stream) {
         k_restrict_codes<<<blocks_for(C.D.n(), 256), 256, 0, s>>>(mg->lv[l].code, C.code, C.D);
         FLUB_CHECK_LAUNCH();
     }
+    for (int l = 0; l < mg->levels; l++) {
+        const Level &L = mg->lv[l];
+        if (!L.pmask) continue;
+        k_tail_masks<<<blocks_for(L.D.n() >> 1, 256), 256, 0, s>>>(L.code, L.D, L.pmask);
+        FLUB_CHECK_LAUNCH();
+    }
     // stencil words and active 8-cell groups of every level that has them
     for (int l = 0; l < mg->levels; l++) {
         const Level &L = mg->lv[l];
@@ -2040,6 +2054,7 @@ static size_t noalloc_layout(flub_mg *mg, char *base) {
         L.r = l ? (float *)take(sizeof(float) * L.D.n()) : nullptr;
         L.z = l ? (float *)take(sizeof(float) * L.D.n()) : nullptr;
         L.z2 = (float *)take(sizeof(float) * L.D.n());
+        L.pmask = nullptr;  // the tail builds its masks from the codes
     }
     return off;
 }

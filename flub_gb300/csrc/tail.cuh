@@ -22,6 +22,7 @@ constexpr int kTailMaxCells = 4096;  // the first tail level has at most this ma
 struct TailLevel {
     Dims D;
     const uint8_t *code;  // global cell codes of this level
+    const uint32_t *pmask;  // the pairs' masks of tail_cache, built by set_tags (NULL: from the codes)
     int abs_level;        // level index in the full hierarchy (sets 6 << l)
     int off_z, off_r, off_c;  // byte offsets in shared memory
     int off_v;                // fine residual scratch for the restriction (-1 at the bottom level)
@@ -78,7 +79,27 @@ __device__ __forceinline__ uint32_t cell_mask(const uint8_t *code, const Dims D,
     return m;
 }
 
-__device__ __forceinline__ void tail_cache(TailCache &tc, const uint8_t *code, const float *r, const Dims D) {
+// The masks of k-pair t (cells 2 kk and 2 kk + 1 of row (i, j)): even cell in
+// the low 16 bits, odd cell in the high.
+__device__ __forceinline__ uint32_t pair_mask(const uint8_t *code, const Dims D, int t) {
+    const int hz = D.nz >> 1;
+    const int kk = t % hz, qq = t / hz;
+    const int j = qq % D.ny, i = qq / D.ny;
+    const int c = (i * D.ny + j) * D.nz + 2 * kk;
+    return cell_mask(code, D, i, j, 2 * kk, c) | (cell_mask(code, D, i, j, 2 * kk + 1, c + 1) << 16);
+}
+
+// set_tags: every pair's masks of a tail-sized level into pm (nz even).
+__global__ void k_tail_masks(const uint8_t *__restrict__ code, Dims D, uint32_t *__restrict__ pm) {
+    const int npairs = D.nx * D.ny * (D.nz >> 1);
+    for (int t = blockIdx.x * blockDim.x + threadIdx.x; t < npairs; t += gridDim.x * blockDim.x)
+        pm[t] = pair_mask(code, D, t);
+}
+
+// pm: the masks from set_tags (one coalesced load per pair), else built from
+// the codes.
+__device__ __forceinline__ void tail_cache(TailCache &tc, const uint8_t *code, const float *r, const Dims D,
+                                           const uint32_t *pm) {
     const int hz = D.nz >> 1, npairs = D.nx * D.ny * hz;
     tc.upd0 = 0;
 #pragma unroll
@@ -92,7 +113,7 @@ __device__ __forceinline__ void tail_cache(TailCache &tc, const uint8_t *code, c
             const int j = qq % D.ny, i = qq / D.ny;
             const int c = (i * D.ny + j) * D.nz + 2 * kk;
             tc.idx[q] = c;
-            tc.msk[q] = cell_mask(code, D, i, j, 2 * kk, c) | (cell_mask(code, D, i, j, 2 * kk + 1, c + 1) << 16);
+            tc.msk[q] = pm ? __ldg(pm + t) : pair_mask(code, D, t);
             tc.r0[q] = r[c];
             tc.r1[q] = r[c + 1];
             // phase 0 updates (i+j+k) odd cells: the odd-k cell iff i+j is even
@@ -345,11 +366,11 @@ __device__ __forceinline__ void tail_run(const TailParams &P, unsigned char *sme
     TailCache tc;
     for (int t = 0; t < nb; t++) {
         const Dims D = P.lv[t].D;
-        tail_cache(tc, C(t), R(t), D);
+        tail_cache(tc, C(t), R(t), D, P.lv[t].pmask);
         sweeps(t, tc, P.nu < 0 ? (6 << P.lv[t].abs_level) : P.nu, true);
         tail_restrict_cached(V(t), Z(t), tc, D, R(t + 1), C(t + 1), P.lv[t + 1].D, P.rscale);
     }
-    tail_cache(tc, C(nb), R(nb), P.lv[nb].D);
+    tail_cache(tc, C(nb), R(nb), P.lv[nb].D, P.lv[nb].pmask);
     if (P.bottom64) {
         tail_bottom64(reinterpret_cast<double *>(smem + P.off_zd), Z(nb), tc, P.lv[nb].D, P.nbottom);
     } else {
@@ -359,7 +380,7 @@ __device__ __forceinline__ void tail_run(const TailParams &P, unsigned char *sme
     for (int t = nb - 1; t >= 0; t--) {
         const Dims D = P.lv[t].D;
         tail_prolong(Z(t), Z(t + 1), D);
-        tail_cache(tc, C(t), R(t), D);
+        tail_cache(tc, C(t), R(t), D, P.lv[t].pmask);
         sweeps(t, tc, P.nu < 0 ? (6 << P.lv[t].abs_level) : P.nu, false);
     }
     if (io) {
